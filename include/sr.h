@@ -1,0 +1,207 @@
+/*
+ * sr.h — C ABI of the GB300 scanline path renderer.
+ *
+ * This is the drop-in boundary for the scanline rasterizer of
+ * galaxysailing/VkScanlinePR.  The reference exposes an abstract C++ class
+ * (VkScanlinePR/src/core/rasterizer.h:9-20):
+ *
+ *     class VGRasterizer {
+ *         virtual void initialize(void* window, uint32_t w, uint32_t h) = 0;
+ *         virtual void render() = 0;
+ *         virtual void loadVG(std::shared_ptr<VGContainer> vg) = 0;
+ *         virtual void setMVP(const glm::mat4& m) = 0;
+ *     };
+ *
+ * implemented by ScanlineVGRasterizer (core/scanline/scanline_rasterizer.h:31-49).
+ * Each entry point below names the reference member it replaces.  All calls
+ * take plain pointers and sizes; no C++ or torch types cross this boundary and
+ * no exception escapes it.  A context is not thread-safe: use one context per
+ * host thread or lock externally.  All device work runs on the caller's stream.
+ */
+#ifndef SR_H_
+#define SR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SR_ABI_VERSION 1
+
+/* Status codes.  The reference reports failures by C++ exceptions
+ * (app/vg_app.cpp:181, core/scanline/scanline_rasterizer.cpp:219-225) and by
+ * VK_CHECK_RESULT assert/exit (core/vk/vk_util.h:21-29); here every call
+ * returns one of these and sr_last_error() gives the message. */
+typedef enum sr_status {
+    SR_OK = 0,
+    SR_ERR_INVALID_ARG = 1,   /* bad pointer, size, curve type or fill rule  */
+    SR_ERR_OOM = 2,           /* device or host allocation failed             */
+    SR_ERR_OVERFLOW_REFIT = 3,/* a pre-sized buffer overflowed; rerun exact   */
+    SR_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up           */
+    SR_ERR_CUDA = 5,          /* a CUDA runtime call failed                   */
+    SR_ERR_NO_SCENE = 6,      /* render called before a scene was loaded      */
+    SR_ERR_INTERNAL = 7       /* a device-side consistency check failed       */
+} sr_status;
+
+/* Curve types, same values as Galaxysailing::CurveType
+ * (core/vg/vg_container.h:9-15).  QUADRIC is listed as TODO in every
+ * reference shader; this library defines it natively (3 control points,
+ * monotonised at the derivative root, evaluated by a 2-level lerp). */
+enum { SR_CURVE_LINE = 0x02, SR_CURVE_QUADRIC = 0x03, SR_CURVE_CUBIC = 0x04 };
+
+/* Fill rules, same values as Galaxysailing::FillRule (vg_container.h:16-19). */
+enum { SR_FILL_NONZERO = 0, SR_FILL_EVENODD = 1 };
+
+/* Render modes.
+ * SR_MODE_REFERENCE: the reference's own semantics — 2-px fragment grid
+ *   (FRAG_SIZE 2), winding sampled on the line y = cell_y + 1, every boundary
+ *   cell painted whole, and the draw list painted with blending off (the last
+ *   path wins), as the reference's line pipeline does
+ *   (core/scanline/scanline_rasterizer.cpp:881-944, blendEnable FALSE).
+ * SR_MODE_PIXEL: 1 sample per pixel at the pixel centre — 1-px grid, winding
+ *   sampled on the pixel-centre row, a boundary pixel painted when its centre
+ *   passes the fill rule, and integer source-over compositing in path order
+ *   over white. */
+enum { SR_MODE_REFERENCE = 0, SR_MODE_PIXEL = 1 };
+
+/* The flattened scene, structure-of-arrays, in exactly the layout the
+ * reference's loadVG builds (core/scanline/scanline_rasterizer.cpp:67-189):
+ * points grouped by curve, curves grouped by path, every curve owning its
+ * control points privately (a cubic owns 4, a quadric 3, a line 2).
+ * fill_info is the packed colour: bytes R,G,B,A in memory order (little-
+ * endian uint32), alpha already multiplied by opacity, zero when alpha is 0
+ * (scanline_rasterizer.cpp:107-118). */
+typedef struct sr_scene_view {
+    uint32_t n_points;
+    uint32_t n_curves;
+    uint32_t n_paths;
+    const float*    position;       /* [2*n_points] x,y pairs               */
+    const uint32_t* pos_path_idx;   /* [n_points]  path of each point       */
+    const uint32_t* curve_pos_map;  /* [n_curves]  first point of the curve */
+    const uint32_t* curve_type;     /* [n_curves]  SR_CURVE_*               */
+    const uint32_t* curve_path_idx; /* [n_curves]  path of each curve       */
+    const uint32_t* fill_rule;      /* [n_paths]   SR_FILL_*                */
+    const uint32_t* fill_info;      /* [n_paths]   packed RGBA8             */
+} sr_scene_view;
+
+typedef struct sr_options {
+    uint32_t struct_size;   /* sizeof(sr_options)                          */
+    int32_t  mode;          /* SR_MODE_REFERENCE or SR_MODE_PIXEL          */
+    int32_t  device;        /* CUDA device ordinal                         */
+    uint32_t flags;         /* SR_FLAG_*                                   */
+} sr_options;
+
+/* Keep every intermediate stage buffer after sr_render so that
+ * sr_debug_dump can read it (parity testing; costs extra device writes). */
+#define SR_FLAG_KEEP_STAGES 0x1u
+
+typedef struct sr_ctx sr_ctx;
+
+/* Replaces VGRasterizer::initialize(window, w, h) (rasterizer.h:11).  There
+ * is no window: the canvas is a headless w x h RGBA8 framebuffer. */
+sr_status sr_create(uint32_t width, uint32_t height, const sr_options* opt, sr_ctx** out);
+
+/* Replaces VGRasterizer::loadVG (rasterizer.h:15).  Copies the scene into
+ * device memory owned by the context; it stays resident until the next load
+ * or sr_destroy.  Rejects curve types other than line/quadric/cubic, fill
+ * rules other than nonzero/even-odd and out-of-range indices. */
+sr_status sr_load_scene(sr_ctx* ctx, const sr_scene_view* scene);
+
+/* Replaces VGRasterizer::setMVP (rasterizer.h:17).  m holds the four rows
+ * m0..m3 of the transform, 16 floats: a point (x,y) maps to
+ * (dot((x,y,0,1), m0) / dot(.., m3), dot((x,y,0,1), m1) / dot(.., m3)),
+ * which is ScanlineVGRasterizer::setMVP (scanline_rasterizer.cpp:191-197)
+ * given transpose(camera.mv()) as the application passes it
+ * (app/vg_app.cpp:159-160). */
+sr_status sr_set_mvp(sr_ctx* ctx, const float m[16]);
+
+/* Replaces VGRasterizer::render (rasterizer.h:13).  Renders one frame on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) into
+ * rgba_out: width*height*4 bytes, row y of the canvas at byte offset
+ * y*width*4 (no vertical flip).  rgba_out may be host memory (copied
+ * synchronously at the end) or device memory (out_is_device = 1; the call
+ * returns once the frame is enqueued).  rgba_out may be NULL to render
+ * into the context's own device framebuffer only. */
+sr_status sr_render(sr_ctx* ctx, void* rgba_out, int out_is_device, void* stream);
+
+/* Per-frame counters of the last sr_render. */
+typedef struct sr_stats {
+    uint64_t n_intersections;  /* N: intersection records (n_fragments)  */
+    uint64_t n_draw_records;   /* O: merged fragments + spans            */
+    uint64_t n_merged_fragments;
+    uint64_t n_spans;
+    uint32_t key_bits;         /* bits of the sort key                   */
+    uint32_t sort_passes;      /* radix passes run                       */
+} sr_stats;
+sr_status sr_get_stats(const sr_ctx* ctx, sr_stats* out);
+
+/* Stage identifiers for sr_debug_dump; the layouts follow the reference's
+ * buffers so that each can be compared with the CPU restatement. */
+typedef enum sr_stage {
+    SR_STAGE_TRANSFORMED_POS = 0, /* float2[n_points]  (transform_pos.comp:85)             */
+    SR_STAGE_PATH_VISIBLE = 1,    /* int32[n_paths]    (transform_pos.comp:71-82)          */
+    SR_STAGE_CUTPOINTS = 2,       /* float[5*n_curves] (make_intersection_0.comp:368-372)  */
+    SR_STAGE_CURVE_COUNT = 3,     /* int32[n_curves]   (make_intersection_0.comp:410)      */
+    SR_STAGE_CURVE_OFFSET = 4,    /* int32[n_curves+1] exclusive scan of the counts        */
+    SR_STAGE_INTERSECTION = 5,    /* int32x2[N] (curve, t bits | flags) (make_intersection_1.comp:370-372) */
+    SR_STAGE_FRAG_KEY = 6,        /* int32[N] packed yx or 0xFFFEFFFE (gen_fragment.comp:221) */
+    SR_STAGE_FRAG_WINDING = 7,    /* int32[N] winding change (gen_fragment.comp:224)       */
+    SR_STAGE_SORTED_KEY = 8,      /* int32[N] yx after the per-path sort                   */
+    SR_STAGE_SORTED_INDEX = 9,    /* int32[N] record index after the per-path sort         */
+    SR_STAGE_WINDING_SCAN = 10,   /* int32[N+1] exclusive scan of sorted winding changes   */
+    SR_STAGE_FRAG_FLAG = 11,      /* int32[N] merged-fragment flags                        */
+    SR_STAGE_SPAN_FLAG = 12,      /* int32[N] span flags                                   */
+    SR_STAGE_DRAW_LIST = 13,      /* int32x4[O] draw records (gen_merged_fragment_and_span.comp:170,195) */
+    SR_STAGE_IMAGE = 14,          /* uint8[w*h*4] RGBA8                                    */
+    SR_STAGE_FRAG_LEFT = 15       /* int32[N] centre-sample winding part (pixel mode)      */
+} sr_stage;
+
+/* Copies one stage of the last sr_render (made with SR_FLAG_KEEP_STAGES) to
+ * host memory.  If dst is NULL only *bytes is set to the size needed;
+ * otherwise *bytes must hold the capacity of dst on entry. */
+sr_status sr_debug_dump(sr_ctx* ctx, int stage, void* dst, size_t* bytes);
+
+/* Replaces the destructor of ScanlineVGRasterizer. */
+void sr_destroy(sr_ctx* ctx);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* sr_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Scene sources: synthetic generator and RVG loader (host only).      */
+/* ------------------------------------------------------------------ */
+
+/* A scene owned by the library (host memory). */
+typedef struct sr_scene_buf sr_scene_buf;
+
+/* Synthetic scene parameters.  preset 0: closed star paths of cubics;
+ * preset 1: mixed cubic/quadric/line paths with even-odd paths,
+ * figure-eights and full-canvas backgrounds.  Fields left 0 take the
+ * preset's default. */
+typedef struct sr_synth_params {
+    uint32_t struct_size;
+    int32_t  preset;
+    uint64_t seed;
+    uint32_t scene_index;   /* independent stream per scene of a batch */
+    uint32_t width, height;
+    uint32_t n_paths;
+} sr_synth_params;
+
+sr_status sr_synth_scene(const sr_synth_params* p, sr_scene_buf** out);
+
+/* Parses an .rvg file the way RVG::load does (core/vg/rvg.cpp:9-255):
+ * M/L/C/Z/fL commands, nzfill/ofill, solid rgb/rgba paint, the last open
+ * contour closed by a line; other elements are skipped. */
+sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]);
+
+/* Points `view` at the arrays of `buf` (valid until sr_scene_buf_free). */
+sr_status sr_scene_buf_view(const sr_scene_buf* buf, sr_scene_view* view);
+void sr_scene_buf_free(sr_scene_buf* buf);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SR_H_ */
