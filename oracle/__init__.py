@@ -199,9 +199,10 @@ class Frame:
         dt = _DTYPES.get(name, np.int32)
         n = b.value // np.dtype(dt).itemsize
         if n == 0:
-            return np.zeros(0, dt)
-        a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt))),
-                                  shape=(n,)).copy()
+            a = np.zeros(0, dt)
+        else:
+            a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                      shape=(n,)).copy()
         if name == "image":
             a = a.reshape(self.height, self.width, 4)
         elif name == "draw_list":

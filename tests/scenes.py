@@ -1,0 +1,130 @@
+"""Hand-made scenes with known answers, shared by the oracle and GPU tests.
+
+Each builder returns a flattened scene (numpy SoA, the reference's loadVG
+layout) as a dict accepted by both oracle.Scene and
+vkscanlinepr_gb300.VGContainer.from_arrays.
+"""
+import math
+
+import numpy as np
+
+LINE, QUADRIC, CUBIC = 2, 3, 4
+
+
+class Builder:
+    def __init__(self, w, h):
+        self.w, self.h = w, h
+        self.pos, self.pos_path = [], []
+        self.curve_pos, self.curve_type, self.curve_path = [], [], []
+        self.fill_rule, self.fill_info = [], []
+
+    def path(self, rule=0, rgba=(0, 0, 0, 255)):
+        r, g, b, a = rgba
+        self.fill_rule.append(rule)
+        self.fill_info.append((r | (g << 8) | (b << 16) | (a << 24)) if a else 0)
+        return self
+
+    def curve(self, ctype, pts):
+        p = len(self.fill_rule) - 1
+        self.curve_pos.append(len(self.pos_path))
+        self.curve_type.append(ctype)
+        self.curve_path.append(p)
+        for x, y in pts:
+            self.pos.append((x, y))
+            self.pos_path.append(p)
+        return self
+
+    def polygon(self, pts):
+        for i in range(len(pts)):
+            self.curve(LINE, [pts[i], pts[(i + 1) % len(pts)]])
+        return self
+
+    def arrays(self):
+        return dict(
+            width=self.w, height=self.h,
+            position=np.asarray(self.pos, np.float32).reshape(-1),
+            pos_path_idx=np.asarray(self.pos_path, np.uint32),
+            curve_pos_map=np.asarray(self.curve_pos, np.uint32),
+            curve_type=np.asarray(self.curve_type, np.uint32),
+            curve_path_idx=np.asarray(self.curve_path, np.uint32),
+            fill_rule=np.asarray(self.fill_rule, np.uint32),
+            fill_info=np.asarray(self.fill_info, np.uint32))
+
+
+def to_oracle(d):
+    import oracle
+    return oracle.Scene(d["width"], d["height"], d["position"], d["pos_path_idx"], d["curve_pos_map"],
+                        d["curve_type"], d["curve_path_idx"], d["fill_rule"], d["fill_info"])
+
+
+def to_container(d):
+    import vkscanlinepr_gb300 as sr
+    return sr.VGContainer.from_arrays(d["width"], d["height"], d["position"], d["pos_path_idx"],
+                                      d["curve_pos_map"], d["curve_type"], d["curve_path_idx"],
+                                      d["fill_rule"], d["fill_info"])
+
+
+RED = (255, 0, 0, 255)
+BLUE = (0, 0, 255, 255)
+
+
+def square(w=8, h=8, x0=2, y0=2, x1=6, y1=6, rgba=RED, rule=0):
+    return Builder(w, h).path(rule, rgba).polygon([(x0, y0), (x1, y0), (x1, y1), (x0, y1)]).arrays()
+
+
+def star(w=64, h=64, rule=0, rgba=RED):
+    cx, cy, r = 32.0, 32.0, 28.0
+    pts = []
+    for k in range(5):
+        a = math.pi / 2 + k * 4 * math.pi / 5
+        pts.append((cx + r * math.cos(a), cy + r * math.sin(a)))
+    return Builder(w, h).path(rule, rgba).polygon(pts).arrays()
+
+
+def figure_eight(w=64, h=32, rule=0, rgba=RED):
+    # two diamonds joined by crossing edges: orientation flips between lobes
+    pts = [(8, 8), (32, 24), (56, 8), (56, 24), (32, 8), (8, 24)]
+    return Builder(w, h).path(rule, rgba).polygon(pts).arrays()
+
+
+def mixed_curves(w=96, h=80):
+    b = Builder(w, h)
+    # cubic blob, nonzero
+    b.path(0, (20, 200, 40, 255))
+    b.curve(CUBIC, [(10, 40), (10, 5), (60, 5), (60, 40)])
+    b.curve(CUBIC, [(60, 40), (60, 75), (10, 75), (10, 40)])
+    # quadric lens, even-odd, semi-transparent
+    b.path(1, (200, 30, 90, 160))
+    b.curve(QUADRIC, [(30, 20), (55, 70), (85, 20)])
+    b.curve(QUADRIC, [(85, 20), (55, 0), (30, 20)])
+    # line triangle that hits integer grid lines exactly
+    b.path(0, (0, 0, 255, 200))
+    b.polygon([(40, 30), (90, 30), (40, 76)])
+    return b.arrays()
+
+
+def offcanvas(w=32, h=32):
+    b = Builder(w, h)
+    b.path(0, RED).polygon([(-40, -40), (-10, -40), (-10, -10), (-40, -10)])   # fully outside
+    b.path(0, BLUE).polygon([(-8, -8), (12, -8), (12, 12), (-8, 12)])          # clipped
+    b.path(0, (0, 200, 0, 255)).polygon([(20, 20), (60, 20), (60, 60), (20, 60)])
+    return b.arrays()
+
+
+def degenerate(w=32, h=32):
+    b = Builder(w, h)
+    b.path(0, RED).polygon([(4, 10), (20, 10), (28, 10)])        # zero-area, horizontal
+    b.path(0, BLUE).polygon([(10, 4), (10, 20), (10, 28)])       # zero-area, vertical
+    b.path(0, (0, 200, 0, 255)).polygon([(5, 5), (5, 5), (5, 5)])  # a single point
+    return b.arrays()
+
+
+ALL = {
+    "square": square,
+    "star_nonzero": lambda: star(rule=0),
+    "star_evenodd": lambda: star(rule=1),
+    "figure_eight": figure_eight,
+    "mixed_curves": mixed_curves,
+    "offcanvas": offcanvas,
+    "degenerate": degenerate,
+}

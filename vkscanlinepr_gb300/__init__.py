@@ -1,0 +1,354 @@
+"""GB300 scanline path renderer — Python host side over the libsr.so C ABI.
+
+Mirrors the reference's public interface for this path
+(VkScanlinePR/src/core/rasterizer.h:9-20 and core/vg/vg_container.h:21-87):
+
+    r = ScanlineVGRasterizer()
+    r.initialize(None, w, h)        # VGRasterizer::initialize (no window: headless)
+    r.loadVG(container)             # VGRasterizer::loadVG
+    r.setMVP(m)                     # VGRasterizer::setMVP (rows m0..m3)
+    img = r.render()                # VGRasterizer::render -> RGBA8 (h, w, 4)
+
+Every call goes through libsr.so (hand-written sm_103a CUDA).  There is no
+CPU fallback: if the library is missing or a CUDA call fails, the call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsr.so")
+
+MODE_REFERENCE = 0
+MODE_PIXEL = 1
+FLAG_KEEP_STAGES = 0x1
+
+LINE, QUADRIC, CUBIC = 0x02, 0x03, 0x04
+NON_ZERO, EVEN_ODD = 0, 1
+
+STAGES = {
+    "transformed_pos": 0, "path_visible": 1, "cutpoints": 2, "curve_count": 3,
+    "curve_offset": 4, "intersection": 5, "frag_key": 6, "frag_winding": 7,
+    "sorted_key": 8, "sorted_index": 9, "winding_scan": 10, "frag_flag": 11,
+    "span_flag": 12, "draw_list": 13, "image": 14, "frag_left": 15,
+}
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "OVERFLOW_REFIT", 4: "TIMEOUT",
+          5: "CUDA", 6: "NO_SCENE", 7: "INTERNAL"}
+
+
+class SRError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class SceneView(ctypes.Structure):
+    _fields_ = [
+        ("n_points", ctypes.c_uint32), ("n_curves", ctypes.c_uint32),
+        ("n_paths", ctypes.c_uint32),
+        ("position", ctypes.c_void_p), ("pos_path_idx", ctypes.c_void_p),
+        ("curve_pos_map", ctypes.c_void_p), ("curve_type", ctypes.c_void_p),
+        ("curve_path_idx", ctypes.c_void_p), ("fill_rule", ctypes.c_void_p),
+        ("fill_info", ctypes.c_void_p),
+    ]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("mode", ctypes.c_int32),
+                ("device", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_intersections", ctypes.c_uint64), ("n_draw_records", ctypes.c_uint64),
+                ("n_merged_fragments", ctypes.c_uint64), ("n_spans", ctypes.c_uint64),
+                ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32)]
+
+
+class SynthParams(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32), ("preset", ctypes.c_int32),
+        ("seed", ctypes.c_uint64), ("scene_index", ctypes.c_uint32),
+        ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+        ("n_paths", ctypes.c_uint32),
+    ]
+
+
+# every symbol include/sr.h declares
+EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stats", "sr_debug_dump",
+           "sr_destroy", "sr_last_error", "sr_synth_scene", "sr_rvg_load", "sr_scene_buf_view",
+           "sr_scene_buf_free"]
+
+_lib = None
+
+
+def build(force=False):
+    """Compile libsr.so in-tree (nvcc, sm_103a)."""
+    from . import builder
+    return builder.build(force=force)
+
+
+def lib():
+    """Load libsr.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libsr.so not built: run vkscanlinepr_gb300.build() first")
+    L = ctypes.CDLL(LIB_PATH)
+    vp = ctypes.c_void_p
+    L.sr_create.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Options), ctypes.POINTER(vp)]
+    L.sr_load_scene.argtypes = [vp, ctypes.POINTER(SceneView)]
+    L.sr_set_mvp.argtypes = [vp, vp]
+    L.sr_render.argtypes = [vp, vp, ctypes.c_int, vp]
+    L.sr_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.sr_debug_dump.argtypes = [vp, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_size_t)]
+    L.sr_destroy.argtypes = [vp]
+    L.sr_destroy.restype = None
+    L.sr_last_error.restype = ctypes.c_char_p
+    L.sr_synth_scene.argtypes = [ctypes.POINTER(SynthParams), ctypes.POINTER(vp)]
+    L.sr_rvg_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
+    L.sr_scene_buf_view.argtypes = [vp, ctypes.POINTER(SceneView)]
+    L.sr_scene_buf_free.argtypes = [vp]
+    L.sr_scene_buf_free.restype = None
+    L.sr_scene_buf_size.argtypes = [vp, vp]
+    L.sr_host_alloc.argtypes = [ctypes.c_size_t]
+    L.sr_host_alloc.restype = vp
+    L.sr_host_free.argtypes = [vp]
+    L.sr_host_free.restype = None
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise SRError(rc, lib().sr_last_error().decode(errors="replace"))
+
+
+class VGContainer:
+    """Flattened scene, the reference's VGContainer after loadVG's flattening
+    (scanline_rasterizer.cpp:67-189): points grouped by curve, curves grouped
+    by path, packed RGBA8 fill colours."""
+
+    def __init__(self, width=0, height=0):
+        self.width, self.height = int(width), int(height)
+        self._pos, self._pos_path = [], []
+        self._curve_pos, self._curve_type, self._curve_path = [], [], []
+        self._fill_rule, self._fill_info = [], []
+        self._arrays = None
+
+    # builder API, after VGContainer::newPath/newCurve/addCurve (vg_container.h:49-86)
+    def new_path(self, fill_rule=NON_ZERO, rgba=(0, 0, 0, 255)):
+        r, g, b, a = (int(v) & 0xFF for v in rgba)
+        c = r | (g << 8) | (b << 16) | (a << 24)
+        self._fill_rule.append(int(fill_rule))
+        self._fill_info.append(c if a else 0)
+        self._arrays = None
+        return len(self._fill_rule) - 1
+
+    def add_curve(self, ctype, points):
+        pts = np.asarray(points, np.float32).reshape(-1, 2)
+        if pts.shape[0] != (ctype & 7):
+            raise ValueError("curve type 0x%x needs %d points" % (ctype, ctype & 7))
+        path = len(self._fill_rule) - 1
+        if path < 0:
+            raise ValueError("new_path() first")
+        self._curve_pos.append(len(self._pos_path))
+        self._curve_type.append(int(ctype))
+        self._curve_path.append(path)
+        for x, y in pts:
+            self._pos.append((float(x), float(y)))
+            self._pos_path.append(path)
+        self._arrays = None
+
+    @classmethod
+    def from_arrays(cls, width, height, position, pos_path_idx, curve_pos_map, curve_type, curve_path_idx,
+                    fill_rule, fill_info):
+        c = cls(width, height)
+        c._arrays = dict(
+            position=np.ascontiguousarray(position, np.float32).reshape(-1),
+            pos_path_idx=np.ascontiguousarray(pos_path_idx, np.uint32),
+            curve_pos_map=np.ascontiguousarray(curve_pos_map, np.uint32),
+            curve_type=np.ascontiguousarray(curve_type, np.uint32),
+            curve_path_idx=np.ascontiguousarray(curve_path_idx, np.uint32),
+            fill_rule=np.ascontiguousarray(fill_rule, np.uint32),
+            fill_info=np.ascontiguousarray(fill_info, np.uint32))
+        return c
+
+    def arrays(self):
+        if self._arrays is None:
+            self._arrays = dict(
+                position=np.asarray(self._pos, np.float32).reshape(-1),
+                pos_path_idx=np.asarray(self._pos_path, np.uint32),
+                curve_pos_map=np.asarray(self._curve_pos, np.uint32),
+                curve_type=np.asarray(self._curve_type, np.uint32),
+                curve_path_idx=np.asarray(self._curve_path, np.uint32),
+                fill_rule=np.asarray(self._fill_rule, np.uint32),
+                fill_info=np.asarray(self._fill_info, np.uint32))
+        return self._arrays
+
+    @property
+    def n_points(self):
+        return self.arrays()["pos_path_idx"].size
+
+    @property
+    def n_curves(self):
+        return self.arrays()["curve_type"].size
+
+    @property
+    def n_paths(self):
+        return self.arrays()["fill_rule"].size
+
+    def view(self):
+        a = self.arrays()
+        v = SceneView()
+        v.n_points = a["pos_path_idx"].size
+        v.n_curves = a["curve_type"].size
+        v.n_paths = a["fill_rule"].size
+        for k in ("position", "pos_path_idx", "curve_pos_map", "curve_type", "curve_path_idx",
+                  "fill_rule", "fill_info"):
+            setattr(v, k, a[k].ctypes.data if a[k].size else None)
+        return v
+
+
+def _from_buf(h, width=None, height=None):
+    L = lib()
+    v = SceneView()
+    _check(L.sr_scene_buf_view(h, ctypes.byref(v)))
+    wh = np.zeros(2, np.uint32)
+    L.sr_scene_buf_size(h, wh.ctypes.data)
+
+    def arr(ptr, n, dt):
+        if n == 0 or not ptr:
+            return np.zeros(0, dt)
+        return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(np.ctypeslib.as_ctypes_type(dt))),
+                                     shape=(n,)).copy()
+    return VGContainer.from_arrays(
+        wh[0] if width is None else width, wh[1] if height is None else height,
+        arr(v.position, 2 * v.n_points, np.float32), arr(v.pos_path_idx, v.n_points, np.uint32),
+        arr(v.curve_pos_map, v.n_curves, np.uint32), arr(v.curve_type, v.n_curves, np.uint32),
+        arr(v.curve_path_idx, v.n_curves, np.uint32), arr(v.fill_rule, v.n_paths, np.uint32),
+        arr(v.fill_info, v.n_paths, np.uint32))
+
+
+def synth_scene(preset, seed, scene_index=0, width=0, height=0, n_paths=0):
+    """Seeded synthetic scene (preset 0: 1024x1024 star cubics; preset 1:
+    4096x4096 mixed curves with backgrounds)."""
+    L = lib()
+    p = SynthParams(ctypes.sizeof(SynthParams), preset, seed, scene_index, width, height, n_paths)
+    h = ctypes.c_void_p()
+    _check(L.sr_synth_scene(ctypes.byref(p), ctypes.byref(h)))
+    try:
+        return _from_buf(h)
+    finally:
+        L.sr_scene_buf_free(h)
+
+
+def load_rvg(path):
+    """Read an .rvg file the way the reference's RVG::load does; returns
+    (container, viewport[4])."""
+    L = lib()
+    h = ctypes.c_void_p()
+    vp = np.zeros(4, np.float32)
+    _check(L.sr_rvg_load(path.encode(), ctypes.byref(h), vp.ctypes.data))
+    try:
+        return _from_buf(h), vp
+    finally:
+        L.sr_scene_buf_free(h)
+
+
+class PinnedBuffer:
+    """Page-locked host buffer (cudaMallocHost) viewed as a numpy array."""
+
+    def __init__(self, nbytes):
+        self.nbytes = int(nbytes)
+        self.ptr = lib().sr_host_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError("pinned host allocation of %d bytes failed" % nbytes)
+        self.array = np.ctypeslib.as_array(ctypes.cast(self.ptr, ctypes.POINTER(ctypes.c_uint8)),
+                                           shape=(self.nbytes,))
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().sr_host_free(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class ScanlineVGRasterizer:
+    """Headless drop-in for the reference's ScanlineVGRasterizer
+    (core/scanline/scanline_rasterizer.h:31-49)."""
+
+    def __init__(self, mode=MODE_PIXEL, device=0, keep_stages=False):
+        self.mode, self.device = mode, device
+        self.flags = FLAG_KEEP_STAGES if keep_stages else 0
+        self._ctx = None
+        self._scene = None
+        self.width = self.height = 0
+
+    def initialize(self, window, w, h):
+        L = lib()
+        o = Options(ctypes.sizeof(Options), self.mode, self.device, self.flags)
+        ctx = ctypes.c_void_p()
+        _check(L.sr_create(int(w), int(h), ctypes.byref(o), ctypes.byref(ctx)))
+        self._ctx = ctx
+        self.width, self.height = int(w), int(h)
+
+    def loadVG(self, container):
+        self._scene = container
+        v = container.view()
+        _check(lib().sr_load_scene(self._ctx, ctypes.byref(v)))
+
+    def setMVP(self, m):
+        a = np.ascontiguousarray(m, np.float32).reshape(16)
+        _check(lib().sr_set_mvp(self._ctx, a.ctypes.data))
+
+    def render(self, out=None, stream=None):
+        """Renders one frame; returns RGBA8 as (h, w, 4) uint8.  `out` may be
+        a (pinned or pageable) host array of h*w*4 bytes."""
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.uint8)
+        ptr = out.ctypes.data if isinstance(out, np.ndarray) else out
+        _check(lib().sr_render(self._ctx, ptr, 0, stream))
+        return out
+
+    def render_device(self, dev_ptr=None, stream=None):
+        """Renders into device memory (dev_ptr or the context's framebuffer)
+        without waiting for the frame."""
+        _check(lib().sr_render(self._ctx, dev_ptr, 1, stream))
+
+    def stats(self):
+        s = Stats()
+        _check(lib().sr_get_stats(self._ctx, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def dump(self, stage):
+        L = lib()
+        sid = STAGES[stage]
+        n = ctypes.c_size_t(0)
+        _check(L.sr_debug_dump(self._ctx, sid, None, ctypes.byref(n)))
+        dt = np.float32 if stage in ("transformed_pos", "cutpoints") else (np.uint8 if stage == "image" else np.int32)
+        a = np.zeros(n.value // np.dtype(dt).itemsize, dt)
+        if n.value:
+            _check(L.sr_debug_dump(self._ctx, sid, a.ctypes.data, ctypes.byref(n)))
+        if stage == "image":
+            a = a.reshape(self.height, self.width, 4)
+        elif stage == "draw_list":
+            a = a.reshape(-1, 4)
+        elif stage in ("intersection", "transformed_pos"):
+            a = a.reshape(-1, 2)
+        return a
+
+    def close(self):
+        if self._ctx:
+            lib().sr_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,149 @@
+// common.cuh — device helpers shared by the scanline kernels.
+//
+// Arithmetic that decides a pixel is written with explicit round-to-nearest
+// intrinsics (__fadd_rn, __fmul_rn, __fsub_rn, __fdiv_rn) so that no
+// multiply-add is ever fused, whatever the compiler flags; the library is
+// also built with --fmad=false.  The semantics GLSL leaves open are fixed
+// the same way as in the CPU restatement: float->int truncates, saturates and
+// maps NaN to 0; int arithmetic wraps; min/max follow GLSL's definition.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define SR_DEV __device__ __forceinline__
+
+namespace sr {
+
+// Error bits written by kernels into the context's device status word.
+enum : uint32_t {
+    ERR_LOOKBACK_TIMEOUT = 1u << 0,  // a decoupled look-back spin gave up
+    ERR_RECORD_RANGE = 1u << 1,      // a curve produced a different record count than counted
+    ERR_CAPACITY = 1u << 2,          // a pre-sized buffer was too small
+    ERR_BAD_INDEX = 1u << 3,         // an index read from memory was out of range
+};
+
+// Polls allowed before a bounded spin gives up (with backoff, ~seconds).
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+SR_DEV float lerp_rn(float a, float b, float t) {
+    // LERP(a,b,t) = a + t*(b-a)   (make_intersection_0.comp:10)
+    return __fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a)));
+}
+SR_DEV float gmin(float x, float y) { return (y < x) ? y : x; }
+SR_DEV float gmax(float x, float y) { return (x < y) ? y : x; }
+SR_DEV int32_t imin(int32_t a, int32_t b) { return b < a ? b : a; }
+SR_DEV int32_t imax(int32_t a, int32_t b) { return a < b ? b : a; }
+SR_DEV int32_t iclamp(int32_t v, int32_t lo, int32_t hi) { return imin(imax(v, lo), hi); }
+SR_DEV int32_t wadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+SR_DEV int32_t wmul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
+SR_DEV int32_t f2i(float x) { return __float2int_rz(x); }  // cvt.rzi.s32.f32: saturates, NaN -> 0
+SR_DEV int32_t fbits(float x) { return __float_as_int(x); }
+SR_DEV float bitsf(int32_t i) { return __int_as_float(i); }
+// float2int_rd (make_intersection_1.comp:76-79)
+SR_DEV int32_t float2int_rd(float x) { return x >= 0.0f ? f2i(x) : f2i(__fsub_rn(x, 1.0f)); }
+
+// PATH_VISIBLE (make_intersection_0.comp:14-20)
+SR_DEV bool path_visible_mask(int32_t m) {
+    bool inv = ((m & 0x11111000) == 0) || ((m & 0x01101011) == 0) || ((m & 0x00011111) == 0) ||
+               ((m & 0x11010110) == 0);
+    return !inv;
+}
+
+// Coordinate of a curve at t: line lerp, quadric 2-level, cubic 3-level.
+SR_DEV float interp(uint32_t type, float t, const float* p) {
+    if (type == 2u) return lerp_rn(p[0], p[1], t);
+    if (type == 3u) {
+        float q0 = lerp_rn(p[0], p[1], t), q1 = lerp_rn(p[1], p[2], t);
+        return lerp_rn(q0, q1, t);
+    }
+    if (type == 4u) {
+        float q0 = lerp_rn(p[0], p[1], t), q1 = lerp_rn(p[1], p[2], t), q2 = lerp_rn(p[2], p[3], t);
+        float l0 = lerp_rn(q0, q1, t), l1 = lerp_rn(q1, q2, t);
+        return lerp_rn(l0, l1, t);
+    }
+    return 0.0f;
+}
+
+SR_DEV void set_error(uint32_t* status, uint32_t bit) {
+    if (status) atomicOr(status, bit);
+}
+
+// ------------------------------------------------------------ memory ops --
+SR_DEV uint64_t ld_acquire_u64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+SR_DEV void st_release_u64(uint64_t* p, uint64_t v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+SR_DEV uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+SR_DEV void st_release_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+SR_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
+SR_DEV uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ------------------------------------------------------- scan geometry --
+// Key layout of a sorted fragment record (64-bit, unsigned order equal to the
+// reference's (path, signed yx) order; see pack_key).
+struct KeyLayout {
+    int32_t F;        // FRAG_SIZE
+    int32_t W, H;     // canvas
+    int32_t Hy;       // number of cell rows: ceil(H / F)
+    uint32_t xbits, rbits, pbits;
+};
+
+// Row rank: cell rows 1..Hy-1 first, then off-canvas/degenerate records,
+// then cell row 0 — the order of the signed 16:16 keys the reference sorts
+// (gen_fragment.comp:180-187 with 0x7FFF biases).
+SR_DEV uint64_t pack_key(const KeyLayout& L, uint32_t path, bool valid, int32_t pos_y, int32_t pos_x) {
+    uint32_t rank, xo;
+    if (!valid) {
+        rank = (uint32_t)(L.Hy - 1);
+        xo = 0;
+    } else {
+        int32_t yy = pos_y / L.F;
+        rank = yy == 0 ? (uint32_t)L.Hy : (uint32_t)(yy - 1);
+        xo = (uint32_t)(pos_x / L.F + 1);
+    }
+    return ((uint64_t)path << (L.rbits + L.xbits)) | ((uint64_t)rank << L.xbits) | (uint64_t)xo;
+}
+
+struct Decoded {
+    uint32_t path;
+    bool valid;
+    int32_t y, x;   // cell origin in pixels (valid records only)
+    int32_t yx;     // the reference's packed key
+};
+
+SR_DEV Decoded unpack_key(const KeyLayout& L, uint64_t k) {
+    Decoded d;
+    uint32_t xo = (uint32_t)(k & ((1ull << L.xbits) - 1));
+    uint32_t rank = (uint32_t)((k >> L.xbits) & ((1ull << L.rbits) - 1));
+    d.path = (uint32_t)(k >> (L.xbits + L.rbits));
+    if (rank == (uint32_t)(L.Hy - 1)) {
+        d.valid = false;
+        d.y = 0x7FFF;
+        d.x = 0x7FFF;
+        d.yx = (int32_t)0xFFFEFFFE;
+    } else {
+        int32_t yy = rank == (uint32_t)L.Hy ? 0 : (int32_t)rank + 1;
+        d.valid = true;
+        d.y = yy * L.F;
+        d.x = ((int32_t)xo - 1) * L.F;
+        d.yx = (int32_t)(((uint32_t)(d.y + 0x7FFF) << 16) | ((uint32_t)(d.x + 0x7FFF) & 0xFFFFu));
+    }
+    return d;
+}
+
+}  // namespace sr

@@ -1,0 +1,295 @@
+// host.cpp — scene sources behind sr.h: the seeded synthetic generator and
+// an .rvg reader with the reference loader's behaviour (host code only).
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/sr.h"
+#include "synth.h"
+
+struct sr_scene_buf {
+    srsynth::Scene s;
+};
+
+namespace {
+thread_local std::string g_host_err;
+}
+
+extern "C" const char* sr_host_last_error(void) { return g_host_err.c_str(); }
+
+extern "C" sr_status sr_synth_scene(const sr_synth_params* p, sr_scene_buf** out) {
+    if (!p || !out) return SR_ERR_INVALID_ARG;
+    if (p->struct_size < sizeof(sr_synth_params)) return SR_ERR_INVALID_ARG;
+    if (p->preset != 0 && p->preset != 1) return SR_ERR_INVALID_ARG;
+    srsynth::Params q;
+    q.preset = p->preset;
+    q.seed = p->seed;
+    q.scene_index = p->scene_index;
+    q.width = p->width;
+    q.height = p->height;
+    q.n_paths = p->n_paths;
+    sr_scene_buf* b = new sr_scene_buf();
+    srsynth::generate(q, b->s);
+    *out = b;
+    return SR_OK;
+}
+
+extern "C" sr_status sr_scene_buf_view(const sr_scene_buf* b, sr_scene_view* v) {
+    if (!b || !v) return SR_ERR_INVALID_ARG;
+    const auto& s = b->s;
+    v->n_points = s.n_points();
+    v->n_curves = s.n_curves();
+    v->n_paths = s.n_paths();
+    v->position = s.pos.data();
+    v->pos_path_idx = s.pos_path.data();
+    v->curve_pos_map = s.curve_pos.data();
+    v->curve_type = s.curve_type.data();
+    v->curve_path_idx = s.curve_path.data();
+    v->fill_rule = s.fill_rule.data();
+    v->fill_info = s.fill_info.data();
+    return SR_OK;
+}
+
+extern "C" void sr_scene_buf_free(sr_scene_buf* b) { delete b; }
+
+extern "C" sr_status sr_scene_buf_size(const sr_scene_buf* b, uint32_t* wh) {
+    if (!b || !wh) return SR_ERR_INVALID_ARG;
+    wh[0] = b->s.width;
+    wh[1] = b->s.height;
+    return SR_OK;
+}
+
+// ------------------------------------------------------------- RVG ------
+// The reference reader (core/vg/rvg.cpp:33-255) works on whitespace tokens;
+// its asserts are compiled out in release builds, so a token it does not
+// expect is simply consumed.  This reader consumes tokens the same way.
+namespace {
+
+struct Tok {
+    std::istream& in;
+    bool next(std::string& t) { return static_cast<bool>(in >> t); }
+};
+
+struct Pt {
+    float x = 0.f, y = 0.f;
+};
+
+// read_point: commas and colons become blanks, then "%f %f"
+Pt parse_point(std::string s) {
+    for (char& ch : s)
+        if (ch == ',' || ch == ':') ch = ' ';
+    Pt p;
+    float a = 0.f, b = 0.f;
+    int got = std::sscanf(s.c_str(), "%f %f", &a, &b);
+    if (got >= 1) p.x = a;
+    if (got >= 2) p.y = b;
+    return p;
+}
+
+struct PathRec {
+    uint32_t first_curve;
+    uint32_t rule = 0;
+    float color[4] = {0.f, 0.f, 0.f, 1.f};
+    float opacity = 0.f;
+};
+
+}  // namespace
+
+extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]) {
+    if (!path || !out) return SR_ERR_INVALID_ARG;
+    std::ifstream fin(path);
+    if (!fin.is_open()) {
+        g_host_err = std::string("cannot open ") + path;
+        return SR_ERR_INVALID_ARG;
+    }
+    Tok tk{fin};
+    std::string t;
+    // header: viewport x,y w,h / window x,y w,h / scene / dyn_identity
+    float vp[4] = {0, 0, 0, 0};
+    tk.next(t);
+    {
+        std::string a, b;
+        tk.next(a);
+        tk.next(b);
+        Pt p0 = parse_point(a), p1 = parse_point(b);
+        vp[0] = p0.x; vp[1] = p0.y; vp[2] = p1.x; vp[3] = p1.y;
+    }
+    tk.next(t);
+    {
+        std::string a, b;
+        tk.next(a);
+        tk.next(b);
+    }
+    tk.next(t);   // scene
+    tk.next(t);   // dyn_identity
+    if (viewport) std::memcpy(viewport, vp, sizeof vp);
+
+    std::vector<Pt> pts;
+    std::vector<uint32_t> curve_first, curve_type;
+    std::vector<PathRec> paths;
+    size_t last_path_points = (size_t)-1;
+
+    auto add_curve = [&](uint32_t type, const Pt* p) {
+        curve_first.push_back((uint32_t)pts.size());
+        curve_type.push_back(type);
+        for (uint32_t k = 0; k < (type & 7u); ++k) pts.push_back(p[k]);
+    };
+
+    while (tk.next(t)) {
+        if (t.size() >= 2 && t[0] == '/' && t[1] == '/') {
+            std::string line;
+            std::getline(fin, line);
+            continue;
+        }
+        if (last_path_points != pts.size()) {
+            last_path_points = pts.size();
+            PathRec r;
+            r.first_curve = (uint32_t)curve_type.size();
+            paths.push_back(r);
+        }
+        PathRec& pr = paths.back();
+        tk.next(t);   // "element"
+        tk.next(t);   // fill rule
+        if (t == "ofill") pr.rule = SR_FILL_EVENODD;
+        else if (t == "nzfill") pr.rule = SR_FILL_NONZERO;
+        else {
+            tk.next(t);
+            continue;
+        }
+        tk.next(t);   // dyn_concrete
+        tk.next(t);
+        tk.next(t);
+        tk.next(t);   // three points, ignored
+        Pt p[4];
+        size_t contour_begin = pts.size();
+        bool closed = false;
+        while (tk.next(t)) {
+            if (t != "fL" && t.size() != 1) break;
+            char cmd = t[0];
+            if (std::string("MmZzLlCcAa").find(cmd) == std::string::npos && t != "fL") break;
+            std::string a, b, c;
+            switch (cmd) {
+                case 'M':
+                    tk.next(a);
+                    p[0] = parse_point(a);
+                    contour_begin = pts.size();
+                    closed = false;
+                    break;
+                case 'L':
+                    tk.next(a);
+                    p[1] = parse_point(a);
+                    add_curve(SR_CURVE_LINE, p);
+                    p[0] = p[1];
+                    break;
+                case 'C':
+                    tk.next(a);
+                    tk.next(b);
+                    tk.next(c);
+                    p[1] = parse_point(a);
+                    p[2] = parse_point(b);
+                    p[3] = parse_point(c);
+                    add_curve(SR_CURVE_CUBIC, p);
+                    p[0] = p[3];
+                    break;
+                case 'Z':
+                    closed = true;
+                    break;
+                default:
+                    if (t == "fL") {
+                        tk.next(a);
+                        p[0] = parse_point(a);
+                    }
+                    break;
+            }
+        }
+        // the last contour, if open, is closed by a straight line (rvg.cpp:211-223)
+        if (!closed && pts.size() > contour_begin) {
+            Pt first = pts[contour_begin], last = pts.back();
+            if (first.x != last.x || first.y != last.y) {
+                Pt q[2] = {last, first};
+                add_curve(SR_CURVE_LINE, q);
+            }
+        }
+        // t now holds "dyn_identity"
+        tk.next(t);   // dyn_paint
+        {
+            std::string o;
+            tk.next(o);
+            pr.opacity = (float)std::strtod(o.c_str(), nullptr);
+        }
+        tk.next(t);
+        if (t == "solid") {
+            tk.next(t);
+            std::string inner;
+            bool rgba = t.compare(0, 4, "rgba") == 0;
+            bool rgb = !rgba && t.compare(0, 3, "rgb") == 0;
+            if (rgba && t.size() >= 6) inner = t.substr(5, t.size() - 6);
+            else if (rgb && t.size() >= 6) inner = t.substr(4, t.size() - 6);   // as rvg.cpp:245
+            if (rgba || rgb) {
+                for (char& ch : inner)
+                    if (ch == ',') ch = ' ';
+                std::istringstream iss(inner);
+                int nc = rgba ? 4 : 3;
+                for (int k = 0; k < nc; ++k) {
+                    float v;
+                    if (!(iss >> v)) break;
+                    pr.color[k] = v;
+                }
+            }
+        }
+    }
+
+    // flatten (scanline_rasterizer.cpp:67-189)
+    sr_scene_buf* bobj = new sr_scene_buf();
+    srsynth::Scene& s = bobj->s;
+    s.width = (uint32_t)vp[2];
+    s.height = (uint32_t)vp[3];
+    const uint32_t n_curves = (uint32_t)curve_type.size();
+    for (uint32_t pi = 0; pi < paths.size(); ++pi) {
+        const PathRec& pr = paths[pi];
+        uint32_t cb = pr.first_curve;
+        uint32_t ce = pi + 1 < paths.size() ? paths[pi + 1].first_curve : n_curves;
+        float col[4] = {pr.color[0], pr.color[1], pr.color[2], pr.color[3] * pr.opacity};
+        uint8_t b8[4];
+        for (int k = 0; k < 4; ++k) {
+            float v = col[k] * 255.0f;
+            if (!(v > 0.0f)) v = 0.0f;
+            if (v > 255.0f) v = 255.0f;
+            b8[k] = (uint8_t)v;
+        }
+        uint32_t c = (uint32_t)b8[0] | ((uint32_t)b8[1] << 8) | ((uint32_t)b8[2] << 16) | ((uint32_t)b8[3] << 24);
+        if (!(c & 0xFF000000u)) c = 0;
+        s.fill_rule.push_back(pr.rule);
+        s.fill_info.push_back(c);
+        for (uint32_t ci = cb; ci < ce; ++ci) {
+            uint32_t pb = curve_first[ci];
+            uint32_t pe = ci + 1 < n_curves ? curve_first[ci + 1] : (uint32_t)pts.size();
+            s.curve_pos.push_back(s.n_points());
+            s.curve_type.push_back(curve_type[ci]);
+            s.curve_path.push_back(pi);
+            for (uint32_t k = pb; k < pe; ++k) {
+                s.pos.push_back(pts[k].x);
+                s.pos.push_back(pts[k].y);
+                s.pos_path.push_back(pi);
+            }
+        }
+    }
+    // paths that received no curve still occupy a slot, like the reference
+    *out = bobj;
+    return SR_OK;
+}
+
+// Pinned host memory for callers that want asynchronous copies.
+#include <cuda_runtime.h>
+extern "C" void* sr_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+extern "C" void sr_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}

@@ -1,0 +1,110 @@
+// kernels.h — launch interface between the host orchestration and the
+// device kernels of the scanline renderer.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sr {
+
+struct Mvp {
+    float m[16];   // rows m0..m3
+};
+
+// Scene + per-frame arrays the geometry kernels read.
+struct GeomArgs {
+    uint32_t n_curves;
+    const uint32_t* curve_type;
+    const uint32_t* curve_pos;
+    const uint32_t* curve_path;
+    const float2* tpos;
+    const int32_t* path_visible;
+    int32_t W, H, F;
+    int32_t pixel_mode;
+    KeyLayout L;
+};
+
+// Optional reference-layout outputs for parity dumps (all NULL in production).
+struct DebugOut {
+    int2* inter;        // [N] (curve, t bits | flags)
+    int32_t* fkey;      // [N] packed yx
+    int32_t* fwn;       // [N] winding change
+    int32_t* fleft;     // [N] centre-sample part (pixel mode)
+};
+
+void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const Mvp& M, float fw,
+                      float fh, float2* tpos, int32_t* path_visible, cudaStream_t st);
+void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, cudaStream_t st);
+void launch_intersect_fragment(const GeomArgs& g, const float* cut_cache, const int32_t* offs, uint64_t* keys,
+                               uint8_t* wnp, const DebugOut& dbg, uint32_t* status, cudaStream_t st);
+
+// ---- scan.cu
+// Exclusive scan of n int32 values into out[0..n] (out[n] = total), single
+// pass with decoupled look-back.  in and out may alias.  tile_status must
+// hold scan_status_words(n) zeroed uint64 words.
+size_t scan_status_words(int64_t n);
+void launch_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, uint64_t* tile_status,
+                               uint32_t* tile_counter, uint32_t* status, cudaStream_t st);
+
+// ---- sort.cu  (onesweep LSD radix sort, 8-bit digits)
+struct SortPlan {
+    int64_t n;
+    uint32_t key_bits;
+    uint32_t passes;
+    uint32_t tiles;
+};
+SortPlan sort_plan(int64_t n, uint32_t key_bits);
+// Device scratch needed by a plan (bytes).
+size_t sort_scratch_bytes(const SortPlan& p);
+// Sorts (keys, values) stably by the low key_bits of the keys.  If
+// vals_in is NULL the values are the identity 0..n-1.  Results end in
+// (keys_out, vals_out); keys_alt/vals_alt are ping-pong buffers of n items.
+void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                     uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch,
+                     uint32_t* status, cudaStream_t st);
+void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                     uint32_t* vals_out, uint32_t* keys_alt, uint32_t* vals_alt, void* scratch,
+                     uint32_t* status, cudaStream_t st);
+
+// ---- winding.cu
+struct WindArgs {
+    int64_t n;                      // N records (host copy)
+    const uint64_t* skeys;          // sorted keys
+    const uint32_t* svals;          // sorted record indices
+    const uint8_t* wnp;             // packed winding bits by record index
+    const uint32_t* fill_rule;      // [P]
+    const uint32_t* fill_info;      // [P]
+    uint32_t n_paths;
+    int32_t W, H, F;
+    int32_t pixel_mode;
+    KeyLayout L;
+    int4* draw;                     // [capacity] draw records
+    int64_t draw_capacity;
+    uint32_t* draw_row;             // [capacity] cell row of each draw record
+    uint32_t* row_count;            // [rows] histogram of draw_row
+    uint64_t* totals;               // [2] merged fragments, spans
+    // parity dumps (NULL in production)
+    int32_t* dbg_wscan;             // [N+1]
+    int32_t* dbg_fflag;             // [N]
+    int32_t* dbg_sflag;             // [N]
+    int32_t* dbg_skey;              // [N]
+};
+size_t winding_status_words(int64_t n);
+void launch_winding_emit(const WindArgs& a, uint64_t* tile_status, uint32_t* tile_counter, uint32_t* status,
+                         cudaStream_t st);
+
+// ---- resolve.cu
+struct ResolveArgs {
+    const int4* draw;
+    const uint32_t* row_sorted_idx;   // draw indices sorted by cell row
+    const int32_t* row_start;         // [rows+1]
+    int32_t W, H, F;
+    int32_t pixel_mode;
+    uint32_t* image;                  // [W*H] RGBA8
+};
+void launch_resolve(const ResolveArgs& a, cudaStream_t st);
+void launch_row_bounds(const uint32_t* srows, int64_t n, int32_t rows, int32_t* row_start, cudaStream_t st);
+
+}  // namespace sr

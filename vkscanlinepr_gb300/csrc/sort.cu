@@ -1,0 +1,320 @@
+// sort.cu — onesweep LSD radix sort (8-bit digits) for 64- and 32-bit keys
+// with 32-bit values.
+//
+// Replaces naive_seg_sort_pairs.comp:26-97, an O(len^2) odd-even
+// transposition sort per path segment.  The fragment key already carries the
+// path in its high bits (see pack_key), so one stable sort of the whole
+// array by key gives the reference's per-path order by (signed yx, index).
+//
+// Per pass, each CTA (dynamic tile id) loads a 4096-key tile, ranks keys by
+// digit with warp __match_any_sync / popc, publishes its per-digit counts,
+// and looks back over earlier tiles' per-digit counts (one thread per digit,
+// bounded spin) to find where its run of each digit starts.  Keys are first
+// scattered into shared memory in digit order, then written out in runs, so
+// global stores stay mostly contiguous.  An upfront kernel histograms every
+// pass's digits in one read of the keys.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sr {
+
+namespace {
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;
+constexpr uint32_t kFlagA = 1u << 30;
+constexpr uint32_t kFlagP = 2u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1u;
+constexpr int kMaxPasses = 8;
+constexpr int kHistBlocks = 608;   // 152 SMs x 4
+
+template <typename K> SR_DEV uint32_t digit_of(K k, uint32_t shift) {
+    return (uint32_t)(k >> shift) & (kRadix - 1);
+}
+
+struct Scratch {
+    uint32_t* hist;       // [passes][256] digit counts, then exclusive offsets
+    uint32_t* lookback;   // [passes][tiles][256]
+    uint32_t* counters;   // [passes] tile counters
+};
+
+Scratch carve(const SortPlan& p, void* base) {
+    Scratch s;
+    char* b = static_cast<char*>(base);
+    s.hist = reinterpret_cast<uint32_t*>(b);
+    b += sizeof(uint32_t) * kMaxPasses * kRadix;
+    s.counters = reinterpret_cast<uint32_t*>(b);
+    b += sizeof(uint32_t) * 64;
+    s.lookback = reinterpret_cast<uint32_t*>(b);
+    return s;
+}
+}  // namespace
+
+SortPlan sort_plan(int64_t n, uint32_t key_bits) {
+    SortPlan p;
+    p.n = n;
+    p.key_bits = key_bits;
+    p.passes = (key_bits + kRadixBits - 1) / kRadixBits;
+    if (p.passes == 0) p.passes = 1;
+    p.tiles = (uint32_t)((n + kTile - 1) / kTile);
+    return p;
+}
+
+size_t sort_scratch_bytes(const SortPlan& p) {
+    return sizeof(uint32_t) * (kMaxPasses * kRadix + 64) +
+           sizeof(uint32_t) * (size_t)p.passes * (size_t)(p.tiles + 1) * kRadix;
+}
+
+// Histogram of every pass's digits (grid-stride; warp-aggregated shared
+// atomics because neighbouring keys usually share their high digits).
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_hist(const K* __restrict__ keys, int64_t n, uint32_t passes,
+                                                   uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kMaxPasses][kRadix];
+    for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kThreads) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t lane = lane_id();
+    int64_t stride = (int64_t)gridDim.x * kThreads;
+    for (int64_t i0 = (int64_t)blockIdx.x * kThreads; i0 < n; i0 += stride) {
+        int64_t i = i0 + threadIdx.x;
+        bool ok = i < n;
+        K k = ok ? keys[i] : (K)0;
+        uint32_t am = __ballot_sync(0xFFFFFFFFu, ok);
+        for (uint32_t p = 0; p < passes; ++p) {
+            uint32_t d = digit_of(k, p * kRadixBits);
+            if (ok) {
+                uint32_t peers = __match_any_sync(am, d);
+                if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&sh[p][d], (uint32_t)__popc(peers));
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < passes * kRadix; i += kThreads) {
+        uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
+// In-place exclusive scan of each pass's 256 digit counts (one CTA per pass).
+__global__ void __launch_bounds__(kRadix) k_hist_scan(uint32_t* hist) {
+    __shared__ uint32_t sw[kRadix / 32];
+    uint32_t* h = hist + blockIdx.x * kRadix;
+    uint32_t v = h[threadIdx.x];
+    uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if ((int)lane >= d) x += t;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kRadix / 32 ? sw[lane] : 0;
+        uint32_t wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, d);
+            if ((int)lane >= d) wi += t;
+        }
+        if (lane < kRadix / 32) sw[lane] = wi - w;
+    }
+    __syncthreads();
+    h[threadIdx.x] = sw[warp] + x - v;
+}
+
+template <typename K> struct OnesweepSmem {
+    uint32_t warp_hist[kWarps][kRadix];
+    uint32_t digit_start[kRadix];   // tile-local exclusive start of each digit
+    uint32_t digit_global[kRadix];  // global base minus digit_start
+    uint32_t scan_tmp[kWarps];
+    uint32_t tile;
+    K keys[kTile];
+    uint32_t vals[kTile];
+};
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ keys_in,
+                                                       const uint32_t* __restrict__ vals_in,
+                                                       K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                       int64_t n, uint32_t shift,
+                                                       const uint32_t* __restrict__ global_off,
+                                                       uint32_t* __restrict__ lookback, uint32_t* counter,
+                                                       uint32_t* status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    OnesweepSmem<K>& S = *reinterpret_cast<OnesweepSmem<K>*>(smem_raw);
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
+    if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t tile = S.tile;
+    const int64_t tbase = (int64_t)tile * kTile;
+    const int64_t wbase = tbase + (int64_t)warp * (32 * kItems);
+
+    // ---- load (warp-striped, coalesced) and rank within the warp
+    K k[kItems];
+    uint32_t v[kItems];
+    uint32_t rank[kItems];
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        int64_t idx = wbase + it * 32 + lane;
+        bool ok = idx < n;
+        k[it] = ok ? keys_in[idx] : (K)0;
+        v[it] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
+    }
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        int64_t idx = wbase + it * 32 + lane;
+        bool ok = idx < n;
+        uint32_t d = ok ? digit_of(k[it], shift) : (uint32_t)kRadix;   // kRadix = out of range
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t before = 0;
+        if (ok && lane == leader) {
+            before = S.warp_hist[warp][d];
+            S.warp_hist[warp][d] = before + (uint32_t)__popc(peers);
+        }
+        before = __shfl_sync(0xFFFFFFFFu, before, leader);
+        rank[it] = before + (uint32_t)__popc(peers & lanemask_lt());
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // ---- per digit: exclusive offsets across warps; tile count; publish
+    const uint32_t d = threadIdx.x;   // kThreads == kRadix
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+        uint32_t t = S.warp_hist[w][d];
+        S.warp_hist[w][d] = cnt;
+        cnt += t;
+    }
+    uint32_t* lb = lookback + (size_t)tile * kRadix;
+    st_release_u32(&lb[d], (tile == 0 ? kFlagP : kFlagA) | cnt);
+
+    // tile-local digit starts: block exclusive scan over the 256 counts
+    uint32_t x = cnt;
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, x, dd);
+        if ((int)lane >= dd) x += t;
+    }
+    if (lane == 31) S.scan_tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kWarps ? S.scan_tmp[lane] : 0;
+        uint32_t wi = w;
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, dd);
+            if ((int)lane >= dd) wi += t;
+        }
+        if (lane < kWarps) S.scan_tmp[lane] = wi - w;
+    }
+    __syncthreads();
+    const uint32_t dstart = S.scan_tmp[warp] + x - cnt;
+    S.digit_start[d] = dstart;
+
+    // ---- look-back for this digit over earlier tiles (bounded)
+    uint32_t excl = 0;
+    if (tile > 0) {
+        int64_t j = (int64_t)tile - 1;
+        uint32_t spins = 0;
+        while (j >= 0) {
+            uint32_t s = ld_acquire_u32(&lookback[(size_t)j * kRadix + d]);
+            uint32_t f = s & ~kCountMask;
+            if (f == 0) {
+                if (++spins > kSpinLimit) {
+                    set_error(status, ERR_LOOKBACK_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            excl += s & kCountMask;
+            if (f == kFlagP) break;
+            --j;
+        }
+        st_release_u32(&lb[d], kFlagP | (excl + cnt));
+    }
+    S.digit_global[d] = global_off[d] + excl - dstart;
+    __syncthreads();
+
+    // ---- scatter into shared memory in digit order
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+        int64_t idx = wbase + it * 32 + lane;
+        if (idx < n) {
+            uint32_t dg = digit_of(k[it], shift);
+            uint32_t pos = S.digit_start[dg] + S.warp_hist[warp][dg] + rank[it];
+            S.keys[pos] = k[it];
+            S.vals[pos] = v[it];
+        }
+    }
+    __syncthreads();
+
+    // ---- write runs to global memory
+    int64_t valid = n - tbase;
+    if (valid > kTile) valid = kTile;
+    for (int j = threadIdx.x; j < valid; j += kThreads) {
+        K kk = S.keys[j];
+        uint32_t dg = digit_of(kk, shift);
+        uint32_t o = S.digit_global[dg] + (uint32_t)j;
+        if ((int64_t)o < n) {
+            keys_out[o] = kk;
+            vals_out[o] = S.vals[j];
+        } else {
+            set_error(status, ERR_BAD_INDEX);
+        }
+    }
+}
+
+template <typename K>
+static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_in, K* keys_out, uint32_t* vals_out,
+                      K* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status, cudaStream_t st) {
+    if (p.n <= 0) return;
+    Scratch s = carve(p, scratch);
+    size_t lb_words = (size_t)p.passes * (size_t)(p.tiles + 1) * kRadix;
+    cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + 64), st);
+    cudaMemsetAsync(s.lookback, 0, sizeof(uint32_t) * lb_words, st);
+    int hb = (int)((p.n + kThreads - 1) / kThreads);
+    if (hb > kHistBlocks) hb = kHistBlocks;
+    k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.passes, s.hist);
+    k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
+    const size_t smem = sizeof(OnesweepSmem<K>);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
+    const K* ksrc = keys_in;
+    const uint32_t* vsrc = vals_in;
+    for (uint32_t pass = 0; pass < p.passes; ++pass) {
+        bool to_out = ((p.passes - 1 - pass) % 2) == 0;
+        K* kdst = to_out ? keys_out : keys_alt;
+        uint32_t* vdst = to_out ? vals_out : vals_alt;
+        k_onesweep<K><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, pass * kRadixBits,
+                                                      s.hist + pass * kRadix,
+                                                      s.lookback + (size_t)pass * (p.tiles + 1) * kRadix,
+                                                      s.counters + pass, status);
+        ksrc = kdst;
+        vsrc = vdst;
+    }
+}
+
+void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                     uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
+                     cudaStream_t st) {
+    sort_impl<uint64_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
+}
+
+void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                     uint32_t* vals_out, uint32_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
+                     cudaStream_t st) {
+    sort_impl<uint32_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
+}
+
+}  // namespace sr

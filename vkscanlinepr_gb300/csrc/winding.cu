@@ -1,0 +1,299 @@
+// winding.cu — one pass over the sorted records that replaces five reference
+// dispatches and two host read-backs:
+//   shuffle_fragment.comp:17-26            gather of winding changes
+//   naive_scan.comp (scanline_rasterizer.cpp:479-506)   winding scan
+//   mark_merged_fragment_and_span.comp:22-93            fragment/span flags
+//   naive_scan.comp over 2N flags (scanline_rasterizer.cpp:545-580)
+//   gen_merged_fragment_and_span.comp:33-103           draw-list emit
+//
+// Each CTA owns 2048 consecutive sorted records.  Chain A (decoupled
+// look-back) gives the exclusive winding prefix of the tile; the flags of
+// each record follow; chain B (a second look-back, packed 31:31-bit counts
+// of merged fragments and spans) gives each record's output slot.  Draw
+// records come out in the reference's order: a record's merged fragment,
+// then the span ending at it.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sr {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kThreads * kItems;
+constexpr uint64_t kFlagA = 1ull << 62;
+constexpr uint64_t kFlagP = 2ull << 62;
+constexpr uint64_t kValMask = (1ull << 62) - 1;
+// chain B value: merged fragments in bits 31..61, spans in bits 0..30
+constexpr int kFragShift = 31;
+constexpr uint64_t kSpanMask = (1ull << 31) - 1;
+
+SR_DEV bool rule_pass(uint32_t rule, int32_t wn) {
+    // mark_merged_fragment_and_span.comp:82
+    return (rule == 0u && wn != 0) || (rule == 1u && (wn & 1) != 0);
+}
+
+SR_DEV int32_t sx2(uint32_t v) { return (int32_t)(v << 30) >> 30; }   // 2-bit two's complement
+
+template <typename T> SR_DEV T warp_incl(T v) {
+    uint32_t lane = lane_id();
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T t = __shfl_up_sync(0xFFFFFFFFu, v, d);
+        if ((int)lane >= d) v = v + t;
+    }
+    return v;
+}
+
+// Look-back over 64-bit tile words; `add` combines values (wrapping).
+template <bool kSigned32>
+SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
+    uint32_t lane = lane_id();
+    uint64_t excl = 0;
+    int64_t look = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (look >= 0) {
+        int64_t j = look - (int64_t)lane;
+        uint64_t s = j >= 0 ? ld_acquire_u64(&tstat[j]) : kFlagP;
+        uint32_t flag = (uint32_t)(s >> 62);
+        uint32_t ready = __ballot_sync(0xFFFFFFFFu, flag != 0);
+        uint32_t pm = __ballot_sync(0xFFFFFFFFu, flag == 2);
+        int firstp = pm ? (__ffs(pm) - 1) : 31;
+        uint32_t need = firstp == 31 ? 0xFFFFFFFFu : ((2u << firstp) - 1u);
+        if ((ready & need) != need) {
+            if (++spins > kSpinLimit) {
+                if (lane == 0) set_error(status, ERR_LOOKBACK_TIMEOUT);
+                break;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        uint64_t v = ((int)lane <= firstp) ? (s & kValMask) : 0ull;
+        if (kSigned32) {
+            uint32_t w = (uint32_t)v;
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) w += __shfl_xor_sync(0xFFFFFFFFu, w, d);
+            excl = (uint64_t)(uint32_t)((uint32_t)excl + w);
+        } else {
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+            excl += v;
+        }
+        if (pm) break;
+        look -= 32;
+    }
+    return excl;
+}
+
+struct Smem {
+    uint32_t tile;
+    int32_t warpA[kThreads / 32];
+    uint64_t warpB[kThreads / 32];
+    int32_t prefixA;
+    uint64_t prefixB;
+    uint64_t keys[kTile + 1];   // keys[0] = predecessor of the tile
+    uint8_t wb[kTile];          // packed winding bits of each record
+};
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uint64_t* __restrict__ tstatA,
+                                                           uint64_t* __restrict__ tstatB, uint32_t* counter,
+                                                           uint32_t* status) {
+    __shared__ Smem S;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t tile = S.tile;
+    const int64_t n = a.n;
+    const int64_t tbase = (int64_t)tile * kTile;
+    const int64_t num_tiles = (n + kTile - 1) / kTile;
+
+    // ---- stage keys (coalesced) and gather winding bits
+    for (int j = threadIdx.x; j < kTile; j += kThreads) {
+        int64_t i = tbase + j;
+        uint64_t k = 0;
+        uint8_t w = 0;
+        if (i < n) {
+            k = a.skeys[i];
+            uint32_t rec = a.svals[i];
+            if (rec < (uint64_t)n) w = a.wnp[rec];
+            else set_error(status, ERR_BAD_INDEX);
+            if ((k >> (a.L.xbits + a.L.rbits)) >= a.n_paths) {
+                set_error(status, ERR_BAD_INDEX);
+                k = 0;
+            }
+        }
+        S.keys[j + 1] = k;
+        S.wb[j] = w;
+    }
+    if (threadIdx.x == 0) {
+        uint64_t k0 = tbase > 0 ? a.skeys[tbase - 1] : 0ull;
+        if ((k0 >> (a.L.xbits + a.L.rbits)) >= a.n_paths) k0 = 0;
+        S.keys[0] = k0;
+    }
+    __syncthreads();
+
+    const int64_t ibase = tbase + (int64_t)threadIdx.x * kItems;
+    int32_t wn[kItems];
+    int32_t wsum = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        int64_t i = ibase + k;
+        int32_t w = 0;
+        if (i < n) w = sx2(S.wb[i - tbase]);
+        wn[k] = w;
+        wsum = wadd(wsum, w);
+    }
+
+    // ---- chain A: winding prefix
+    int32_t inclA = warp_incl<int32_t>(wsum);
+    if (lane == 31) S.warpA[warp] = inclA;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t w = lane < kThreads / 32 ? S.warpA[lane] : 0;
+        int32_t wi = warp_incl<int32_t>(w);
+        if (lane < kThreads / 32) S.warpA[lane] = wadd(wi, -w);
+        int32_t agg = __shfl_sync(0xFFFFFFFFu, wi, kThreads / 32 - 1);
+        if (lane == 0) st_release_u64(&tstatA[tile], (tile == 0 ? kFlagP : kFlagA) | (uint32_t)agg);
+        int32_t excl = 0;
+        if (tile > 0) {
+            excl = (int32_t)(uint32_t)lookback<true>(tstatA, tile, status);
+            if (lane == 0) st_release_u64(&tstatA[tile], kFlagP | (uint32_t)wadd(excl, agg));
+        }
+        if (lane == 0) {
+            S.prefixA = excl;
+            if (tile == num_tiles - 1 && a.dbg_wscan) a.dbg_wscan[n] = wadd(excl, agg);
+        }
+    }
+    __syncthreads();
+    int32_t wrun = wadd(wadd(S.prefixA, S.warpA[warp]), wadd(inclA, -wsum));
+
+    // ---- flags
+    uint32_t ff[kItems], sf[kItems];
+    uint64_t bsum = 0;
+    const int32_t F = a.F;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        int64_t i = ibase + k;
+        int32_t wscan = wrun;
+        wrun = wadd(wrun, wn[k]);
+        ff[k] = 0;
+        sf[k] = 0;
+        if (i >= n) continue;
+        int jl = (int)(i - tbase);
+        uint64_t k1 = S.keys[jl + 1];
+        Decoded d1 = unpack_key(a.L, k1);
+        bool on = !(d1.x < 0 || d1.y < 0 || d1.x >= a.W || d1.y >= a.H);
+        uint32_t rule = a.fill_rule[d1.path];
+        if (i == 0) {
+            ff[k] = on ? 1u : 0u;
+        } else {
+            uint64_t k0 = S.keys[jl];
+            Decoded d0 = unpack_key(a.L, k0);
+            if (on && (d0.path != d1.path || d0.yx != d1.yx)) ff[k] = 1u;
+            if (d0.y == d1.y && wadd(d0.x, F) < d1.x && d0.path == d1.path && rule_pass(rule, wscan)) sf[k] = 1u;
+        }
+        if (a.pixel_mode && ff[k]) {
+            // centre sample of the merged cell: scan at its first record plus
+            // the left-of-centre changes of the cell's pieces
+            int32_t wc = wscan;
+            int64_t j = i;
+            for (;;) {
+                uint64_t kj;
+                int32_t lj;
+                int64_t jt = j - tbase;
+                if (jt < kTile) {
+                    kj = S.keys[jt + 1];
+                    lj = sx2((uint32_t)S.wb[jt] >> 2);
+                } else {
+                    kj = a.skeys[j];
+                    uint32_t rec = a.svals[j];
+                    lj = rec < (uint64_t)n ? sx2((uint32_t)a.wnp[rec] >> 2) : 0;
+                }
+                if (kj != k1) break;
+                wc = wadd(wc, lj);
+                if (++j >= n) break;
+            }
+            if (!rule_pass(rule, wc)) ff[k] = 0u;
+        }
+        if (a.dbg_wscan) {
+            a.dbg_wscan[i] = wscan;
+            a.dbg_fflag[i] = (int32_t)ff[k];
+            a.dbg_sflag[i] = (int32_t)sf[k];
+            a.dbg_skey[i] = d1.yx;
+        }
+        bsum += ((uint64_t)ff[k] << kFragShift) | (uint64_t)sf[k];
+    }
+
+    // ---- chain B: output slots
+    uint64_t inclB = warp_incl<uint64_t>(bsum);
+    if (lane == 31) S.warpB[warp] = inclB;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = lane < kThreads / 32 ? S.warpB[lane] : 0ull;
+        uint64_t wi = warp_incl<uint64_t>(w);
+        if (lane < kThreads / 32) S.warpB[lane] = wi - w;
+        uint64_t agg = __shfl_sync(0xFFFFFFFFu, wi, kThreads / 32 - 1);
+        if (lane == 0) st_release_u64(&tstatB[tile], (tile == 0 ? kFlagP : kFlagA) | agg);
+        uint64_t excl = 0;
+        if (tile > 0) {
+            excl = lookback<false>(tstatB, tile, status);
+            if (lane == 0) st_release_u64(&tstatB[tile], kFlagP | (excl + agg));
+        }
+        if (lane == 0) {
+            S.prefixB = excl;
+            if (tile == num_tiles - 1) {
+                uint64_t tot = excl + agg;
+                a.totals[0] = tot >> kFragShift;
+                a.totals[1] = tot & kSpanMask;
+            }
+        }
+    }
+    __syncthreads();
+    uint64_t brun = S.prefixB + S.warpB[warp] + (inclB - bsum);
+
+    // ---- emit draw records (gen_merged_fragment_and_span.comp:155-196)
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        int64_t i = ibase + k;
+        uint64_t fb = brun >> kFragShift, sb = brun & kSpanMask;
+        brun += ((uint64_t)ff[k] << kFragShift) | (uint64_t)sf[k];
+        if (i >= n || !(ff[k] | sf[k])) continue;
+        int jl = (int)(i - tbase);
+        Decoded d1 = unpack_key(a.L, S.keys[jl + 1]);
+        int32_t info = (int32_t)a.fill_info[d1.path];
+        int64_t o = (int64_t)(fb + sb);
+        if (ff[k]) {
+            if (o < a.draw_capacity) {
+                a.draw[o] = make_int4((int32_t)((uint32_t)d1.y << 16) | d1.x, F, info, (int32_t)(fb + 1));
+                a.draw_row[o] = (uint32_t)(d1.y / F);
+            } else {
+                set_error(status, ERR_CAPACITY);
+            }
+            ++o;
+        }
+        if (sf[k]) {
+            Decoded d0 = unpack_key(a.L, S.keys[jl]);
+            int32_t x0 = imax(0, wadd(d0.x, F));
+            if (o < a.draw_capacity) {
+                a.draw[o] = make_int4((int32_t)((uint32_t)d0.y << 16) | x0, d1.x - x0, info, 0);
+                a.draw_row[o] = (uint32_t)(d0.y / F);
+            } else {
+                set_error(status, ERR_CAPACITY);
+            }
+        }
+    }
+}
+
+size_t winding_status_words(int64_t n) { return 2 * (size_t)((n + kTile - 1) / kTile + 1); }
+
+void launch_winding_emit(const WindArgs& a, uint64_t* tile_status, uint32_t* tile_counter, uint32_t* status,
+                         cudaStream_t st) {
+    if (a.n <= 0) return;
+    int64_t tiles = (a.n + kTile - 1) / kTile;
+    uint64_t* sA = tile_status;
+    uint64_t* sB = tile_status + (tiles + 1);
+    k_winding_emit<<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
+}
+
+}  // namespace sr
