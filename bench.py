@@ -1,0 +1,357 @@
+#!/usr/bin/env python
+"""Benchmark: 4096x4096 frames of 20,000 mixed paths (seed 1), pixel mode.
+
+One step renders one frame of the scene (curves -> intersections -> sort ->
+winding -> spans/fragments -> RGBA8) on one GB300.  Prints ONE JSON line.
+
+  value       frames/s with the scene resident in HBM, CUDA events on the
+              render stream around each frame, L2 flushed (256 MiB memset)
+              between timed frames.
+  e2e         frames/s through the C ABI with host buffers: every step copies
+              the scene from pinned host memory (sr_load_scene) and reads the
+              RGBA8 frame back into pinned host memory (sr_render).
+  roofline    the dominant stage's algorithmic bytes / its CUDA-event time
+              against the measured HBM copy bandwidth.
+  cpu_baseline  the C++ oracle (the CPU restatement of the reference shaders)
+              rendering the same frame with every host thread.
+
+--impl reference times that CPU restatement as the reference arm (the
+reference itself is a Windows/Vulkan program with no CPU path).
+Under torchrun (N>1) every rank renders its own replica of the frame
+("replicas only"; no collective on the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    # name: (preset, seed, width, height, paths)
+    "frame4096": (1, 1, 4096, 4096, 20000),
+    "frame1024": (0, 0, 1024, 1024, 500),
+    "mixed2048": (1, 1, 2048, 2048, 5000),
+}
+L2_FLUSH_BYTES = 256 << 20
+STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
+               "row_sort", "resolve"]
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="frame4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of each stage's kernel from the committed ncu
+    summary (lines 'traffic <stage> <bytes> <records>'), or {}."""
+    p = os.path.join(REPO, "profiles", "traffic.md")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            parts = line.strip().strip("|").split()
+            if len(parts) == 4 and parts[0] == "traffic":
+                out[parts[1]] = (float(parts[2]), float(parts[3]))
+    return out
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile(prefix="clk", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.tmp.name) as f:
+            for line in f:
+                cols = [c.strip() for c in line.split(",")]
+                if len(cols) < 7:
+                    continue
+                try:
+                    sm.append(float(cols[0]))
+                    mx.append(float(cols[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, cols[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.tmp.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def stage_bytes(st, n_curves, n_points, W, H):
+    """Algorithmic bytes per stage for one frame."""
+    N = st["n_intersections"]
+    O = st["n_draw_records"]
+    passes = st["sort_passes"]
+    rows_bits = max(1, int(np.ceil(np.log2(H + 1))))
+    row_passes = (rows_bits + 7) // 8
+    return {
+        "transform": n_points * (8 + 4 + 8),
+        "count": n_curves * (12 + 32 + 20 + 4),
+        "offset_scan": n_curves * 8,
+        "chains": n_curves * (12 + 80 + 32) + N * 4,
+        "merge": n_curves * (8 + 80) + N * (4 + 8),
+        "fragment": N * (8 + 9) + n_curves * 0,
+        "sort": N * 8 + passes * N * 2 * (8 + 4),
+        "winding_emit": N * (8 + 4 + 1) + O * (16 + 4),
+        "row_sort": O * 4 + row_passes * O * 2 * (4 + 4),
+        "resolve": O * (4 + 16) + W * H * 4,
+    }
+
+
+def run_cpu_baseline(scene_oracle, W, H, budget_s=20.0):
+    import oracle
+    threads = oracle.hw_threads()
+    times = []
+    img = None
+    t_all = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        f = oracle.Frame(scene_oracle, width=W, height=H, mode=oracle.MODE_PIXEL, threads=threads)
+        times.append(time.perf_counter() - t0)
+        if img is None:
+            img = f.get("image")
+        del f
+        if time.perf_counter() - t_all > budget_s * 0.5 or len(times) >= 5:
+            break
+    v = len(times) / sum(times)
+    return {"value": round(v, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": "%d full frame(s) of the same scene by the oracle (C++ restatement, %d threads)"
+                      % (len(times), threads)}, img
+
+
+def oracle_scene(preset, seed, W, H, P):
+    import oracle
+    return oracle.synth(preset, seed, width=W, height=H, n_paths=P)
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    wl = WORKLOADS[args.workload]
+    preset, seed, W, H, P = wl
+    workload_desc = "%dx%d frame, %d paths (preset %d, seed %d), pixel mode, 1 sample/px" % (W, H, P, preset, seed)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        import oracle
+        oracle.build()
+        sc = oracle_scene(preset, seed, W, H, P)
+        threads = oracle.hw_threads()
+        for _ in range(args.warmup):
+            oracle.Frame(sc, mode=oracle.MODE_PIXEL, threads=threads)
+        t = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            oracle.Frame(sc, mode=oracle.MODE_PIXEL, threads=threads)
+            t.append(time.perf_counter() - t0)
+        v = len(t) / sum(t)
+        line = {"metric": "frames/s (%s)" % args.workload, "value": round(v, 4), "unit": "frames/s",
+                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(1000 * sum(t) / len(t), 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": workload_desc, "l2": "n/a (CPU)"},
+                "cpu_baseline": {"value": round(v, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                                 "sample": "one full frame per step (C++ restatement of the reference "
+                                           "shaders, %d threads)" % threads},
+                "e2e": {"value": round(v, 4), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    import torch
+    import vkscanlinepr_gb300 as sr
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    sr.lib()
+    stream = torch.cuda.current_stream()
+    sptr = ctypes_stream(stream)
+
+    scene = sr.synth_scene(preset, seed, width=W, height=H, n_paths=P)
+    r = sr.ScanlineVGRasterizer(mode=sr.MODE_PIXEL, device=local, profile=True)
+    r.initialize(None, W, H)
+    r.loadVG(scene)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    clk = ClockSampler(local)
+    clk.start()
+    for _ in range(max(args.warmup, 3)):
+        r.render_device(stream=sptr)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms, stage_acc, launches = [], {k: 0.0 for k in STAGE_NAMES}, 0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0.record(stream)
+        r.render_device(stream=sptr)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        st = r.stats()
+        launches += st["kernel_launches"]
+        for k in STAGE_NAMES:
+            stage_acc[k] += st["stage_ms"][k]
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1000.0)
+    st = r.stats()
+
+    # ---- end to end through the C ABI with pinned host buffers
+    arrs = scene.arrays()
+    pinned = {}
+    h2d = 0
+    for k, a in arrs.items():
+        pb = sr.PinnedBuffer(max(a.nbytes, 4))
+        view = pb.array[:a.nbytes].view(a.dtype)
+        view[:] = a
+        pinned[k] = (pb, view)
+        h2d += a.nbytes
+    pscene = sr.VGContainer.from_arrays(W, H, *[pinned[k][1] for k in
+                                                ("position", "pos_path_idx", "curve_pos_map", "curve_type",
+                                                 "curve_path_idx", "fill_rule", "fill_info")])
+    out_pb = sr.PinnedBuffer(W * H * 4)
+    out_img = out_pb.array.reshape(H, W, 4)
+    e2e_steps = max(3, min(args.steps, 10))
+    r.loadVG(pscene)
+    r.render(out=out_img, stream=sptr)
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        r.loadVG(pscene)
+        r.render(out=out_img, stream=sptr)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": round(world * e2e_steps / e2e_s, 4), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(W * H * 4)}
+    gpu_img = out_img.copy()
+
+    # ---- roofline of the dominant stage
+    peak, peak_kind = measured_peaks()
+    sb = stage_bytes(st, scene.n_curves, scene.n_points, W, H)
+    stage_ms = {k: stage_acc[k] / args.steps for k in STAGE_NAMES}
+    dom = max(stage_ms, key=lambda k: stage_ms[k])
+    stages = {}
+    for k in STAGE_NAMES:
+        ms = stage_ms[k]
+        stages[k] = {"ms": round(ms, 4), "algo_bytes": int(sb[k]),
+                     "gbs": round(sb[k] / (ms * 1e6), 1) if ms > 0 else None,
+                     "frac": round(sb[k] / (ms * 1e6) / peak, 4) if ms > 0 else None}
+    traffic = None
+    tr = profile_traffic()
+    if dom in tr and tr[dom][1] > 0:
+        traffic = int(tr[dom][0] / tr[dom][1] * st["n_intersections"])
+    achieved = sb[dom] / (stage_ms[dom] * 1e6)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic}
+
+    line = {"metric": "frames/s (4096x4096, 20000 paths, 1 spp, bit-exact)" if args.workload == "frame4096"
+            else "frames/s (%s)" % args.workload,
+            "value": round(value, 4), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_desc, "width": W, "height": H, "paths": P,
+                       "n_intersections": int(st["n_intersections"]), "n_draw_records": int(st["n_draw_records"]),
+                       "sort_key_bits": int(st["key_bits"]), "sort_passes": int(st["sort_passes"]),
+                       "l2": "flushed between timed frames (256 MiB memset)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "samples_per_s": round(value * W * H, 1),
+            "roofline": roofline, "stages": stages, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": int(launches)}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        so = oracle_scene(preset, seed, W, H, P)
+        cpu, ref_img = run_cpu_baseline(so, W, H)
+        line["cpu_baseline"] = cpu
+        line["bit_exact"] = bool(np.array_equal(ref_img, gpu_img))
+    r.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -96,6 +96,8 @@ typedef struct sr_options {
 /* Keep every intermediate stage buffer after sr_render so that
  * sr_debug_dump can read it (parity testing; costs extra device writes). */
 #define SR_FLAG_KEEP_STAGES 0x1u
+/* Record a CUDA event around every stage of sr_render (see sr_stats). */
+#define SR_FLAG_PROFILE 0x2u
 
 typedef struct sr_ctx sr_ctx;
 
@@ -134,6 +136,12 @@ typedef struct sr_stats {
     uint64_t n_spans;
     uint32_t key_bits;         /* bits of the sort key                   */
     uint32_t sort_passes;      /* radix passes run                       */
+    uint32_t kernel_launches;  /* kernels this library launched for the frame */
+    uint32_t reserved;
+    /* with SR_FLAG_PROFILE: device time of each stage (CUDA events on the
+     * render stream): transform, count, offset scan, crossing chains,
+     * record merge, fragments, sort, winding+emit, row sort, resolve */
+    float stage_ms[12];
 } sr_stats;
 sr_status sr_get_stats(const sr_ctx* ctx, sr_stats* out);
 

@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(HERE, "libsr.so")
 MODE_REFERENCE = 0
 MODE_PIXEL = 1
 FLAG_KEEP_STAGES = 0x1
+FLAG_PROFILE = 0x2
 
 LINE, QUADRIC, CUBIC = 0x02, 0x03, 0x04
 NON_ZERO, EVEN_ODD = 0, 1
@@ -63,7 +64,12 @@ class Options(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("n_intersections", ctypes.c_uint64), ("n_draw_records", ctypes.c_uint64),
                 ("n_merged_fragments", ctypes.c_uint64), ("n_spans", ctypes.c_uint64),
-                ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32)]
+                ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32),
+                ("kernel_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("stage_ms", ctypes.c_float * 12)]
+
+STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
+               "row_sort", "resolve"]
 
 
 class SynthParams(ctypes.Structure):
@@ -282,9 +288,9 @@ class ScanlineVGRasterizer:
     """Headless drop-in for the reference's ScanlineVGRasterizer
     (core/scanline/scanline_rasterizer.h:31-49)."""
 
-    def __init__(self, mode=MODE_PIXEL, device=0, keep_stages=False):
+    def __init__(self, mode=MODE_PIXEL, device=0, keep_stages=False, profile=False):
         self.mode, self.device = mode, device
-        self.flags = FLAG_KEEP_STAGES if keep_stages else 0
+        self.flags = (FLAG_KEEP_STAGES if keep_stages else 0) | (FLAG_PROFILE if profile else 0)
         self._ctx = None
         self._scene = None
         self.width = self.height = 0
@@ -323,7 +329,9 @@ class ScanlineVGRasterizer:
     def stats(self):
         s = Stats()
         _check(lib().sr_get_stats(self._ctx, ctypes.byref(s)))
-        return {k: getattr(s, k) for k, _ in Stats._fields_}
+        d = {k: getattr(s, k) for k, _ in Stats._fields_ if k not in ("stage_ms", "reserved")}
+        d["stage_ms"] = dict(zip(STAGE_NAMES, [float(x) for x in s.stage_ms]))
+        return d
 
     def dump(self, stage):
         L = lib()

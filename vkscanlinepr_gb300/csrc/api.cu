@@ -7,6 +7,7 @@
 //   onesweep sort -> winding/mark/emit -> [read O] -> row sort -> resolve
 // on the caller's stream, with device buffers that only grow.
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -81,10 +82,23 @@ enum Ctl : int {
     CTL_STATUS = 0,
     CTL_SCAN_COUNTER = 1,
     CTL_WIND_COUNTER = 2,
+    CTL_BUCKETS = 4,   // 4 chain-bucket counters
     CTL_WORDS = 16,
 };
 
+std::atomic<uint64_t> g_launches{0};
+
 }  // namespace
+
+namespace sr {
+void count_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace sr
+
+enum Stage : int {
+    ST_TRANSFORM = 0, ST_COUNT, ST_SCAN, ST_CHAINS, ST_MERGE, ST_FRAGMENT, ST_SORT, ST_WINDING, ST_ROWSORT,
+    ST_RESOLVE, ST_COUNT_ALL
+};
 
 struct sr_ctx {
     int device = 0;
@@ -96,25 +110,40 @@ struct sr_ctx {
     uint32_t V = 0, C = 0, P = 0;
     DevBuf pos, pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info;
     // frame
-    DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status;
+    DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, cbuf, rec;
+    int sm_count = 148;
     DevBuf keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status;
     DevBuf draw, draw_row, totals;
     DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, image;
-    DevBuf d_inter, d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
+    DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
     // pinned host scalars
     int32_t* h_n = nullptr;        // [2] N, status
     uint64_t* h_tot = nullptr;     // [3] frags, spans, status
     sr_stats stats{};
     int64_t last_N = 0, last_O = 0;
     bool stages_valid = false;
+    // profiling: a start/end event per stage
+    cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
+    bool ev_pending = false;
+    cudaStream_t cur_stream = nullptr;
+
+    void mark(int stage, bool end) {
+        if (!(flags & SR_FLAG_PROFILE)) return;
+        cudaEvent_t& e = ev[2 * stage + (end ? 1 : 0)];
+        if (!e) cudaEventCreate(&e);
+        cudaEventRecord(e, cur_stream);
+    }
 
     ~sr_ctx() {
         DevBuf* all[] = {&pos, &pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info,
-                         &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status, &keys, &keys_alt,
+                         &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status, &pieces, &chain_lists,
+                         &cbuf, &rec, &keys, &keys_alt,
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row,
                          &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start,
-                         &image, &d_inter, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
+                         &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
         for (DevBuf* b : all) release(*b);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
         if (h_n) cudaFreeHost(h_n);
         if (h_tot) cudaFreeHost(h_tot);
     }
@@ -151,6 +180,9 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     CUDA_TRY(ensure(c->offs, sizeof(int32_t) * ((size_t)C + 1)));
     CUDA_TRY(ensure(c->ctl, sizeof(uint32_t) * CTL_WORDS));
     CUDA_TRY(ensure(c->scan_status, sizeof(uint64_t) * scan_status_words(C)));
+    CUDA_TRY(ensure(c->pieces, piece_table_bytes(std::max<uint32_t>(C, 1))));
+    const uint32_t list_cap = chain_list_capacity(std::max<uint32_t>(C, 1));
+    CUDA_TRY(ensure(c->chain_lists, sizeof(uint32_t) * 4 * (size_t)list_cap));
     uint32_t* ctl = c->ctl.as<uint32_t>();
     uint32_t* status = ctl + CTL_STATUS;
 
@@ -158,9 +190,13 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     CUDA_TRY(cudaMemsetAsync(c->path_visible.p, 0, sizeof(int32_t) * std::max<uint32_t>(P, 1), st));
     CUDA_TRY(cudaMemsetAsync(c->scan_status.p, 0, sizeof(uint64_t) * scan_status_words(C), st));
 
+    c->cur_stream = st;
+    const uint64_t launches0 = launches_so_far();
     // K1 transform (transform_pos.comp)
+    c->mark(ST_TRANSFORM, false);
     launch_transform(c->pos.as<float2>(), c->pos_path.as<uint32_t>(), V, c->mvp, (float)c->W, (float)c->H,
                      c->tpos.as<float2>(), c->path_visible.as<int32_t>(), st);
+    c->mark(ST_TRANSFORM, true);
     GeomArgs g;
     g.n_curves = C;
     g.curve_type = c->curve_type.as<uint32_t>();
@@ -174,9 +210,18 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     g.pixel_mode = c->mode == SR_MODE_PIXEL;
     g.L = c->layout();
     // K2 count pass + K3 offset scan (make_intersection_0.comp, naive_scan.comp)
-    launch_count(g, c->cut.as<float>(), c->count.as<int32_t>(), st);
+    ChainWork cw;
+    cw.pieces = c->pieces.as<uint4>();
+    cw.chain_lists = c->chain_lists.as<uint32_t>();
+    cw.list_cap = list_cap;
+    cw.bucket_count = ctl + CTL_BUCKETS;
+    c->mark(ST_COUNT, false);
+    launch_count(g, c->cut.as<float>(), c->count.as<int32_t>(), cw, status, st);
+    c->mark(ST_COUNT, true);
+    c->mark(ST_SCAN, false);
     launch_exclusive_scan_i32(c->count.as<int32_t>(), c->offs.as<int32_t>(), C, c->scan_status.as<uint64_t>(),
                               ctl + CTL_SCAN_COUNTER, status, st);
+    c->mark(ST_SCAN, true);
     CUDA_TRY(cudaGetLastError());
     // read back N, as the reference does (scanline_rasterizer.cpp:355-356)
     CUDA_TRY(cudaMemcpyAsync(&c->h_n[0], c->offs.as<int32_t>() + C, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -191,15 +236,16 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     c->last_N = N;
     const size_t n1 = (size_t)std::max<int64_t>(N, 1);
 
+    CUDA_TRY(ensure(c->cbuf, sizeof(int32_t) * n1));
+    CUDA_TRY(ensure(c->rec, sizeof(int2) * n1));
     CUDA_TRY(ensure(c->keys, sizeof(uint64_t) * n1));
     CUDA_TRY(ensure(c->keys_alt, sizeof(uint64_t) * n1));
     CUDA_TRY(ensure(c->skeys, sizeof(uint64_t) * n1));
     CUDA_TRY(ensure(c->wnp, n1));
     CUDA_TRY(ensure(c->svals, sizeof(uint32_t) * n1));
     CUDA_TRY(ensure(c->vals_alt, sizeof(uint32_t) * n1));
-    DebugOut dbg{nullptr, nullptr, nullptr, nullptr};
+    DebugOut dbg{nullptr, nullptr, nullptr};
     if (keep) {
-        CUDA_TRY(ensure(c->d_inter, sizeof(int2) * n1));
         CUDA_TRY(ensure(c->d_fkey, sizeof(int32_t) * n1));
         CUDA_TRY(ensure(c->d_fwn, sizeof(int32_t) * n1));
         CUDA_TRY(ensure(c->d_fleft, sizeof(int32_t) * n1));
@@ -207,15 +253,22 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
         CUDA_TRY(ensure(c->d_fflag, sizeof(int32_t) * n1));
         CUDA_TRY(ensure(c->d_sflag, sizeof(int32_t) * n1));
         CUDA_TRY(ensure(c->d_skey, sizeof(int32_t) * n1));
-        dbg.inter = c->d_inter.as<int2>();
         dbg.fkey = c->d_fkey.as<int32_t>();
         dbg.fwn = c->d_fwn.as<int32_t>();
         dbg.fleft = c->d_fleft.as<int32_t>();
         CUDA_TRY(cudaMemsetAsync(c->d_wscan.p, 0, sizeof(int32_t) * (n1 + 1), st));
     }
-    // K4+K5 intersections and fragments
-    launch_intersect_fragment(g, c->cut.as<float>(), c->offs.as<int32_t>(), c->keys.as<uint64_t>(),
-                              c->wnp.as<uint8_t>(), dbg, status, st);
+    // K4 intersections: crossing chains, then the per-curve merge
+    c->mark(ST_CHAINS, false);
+    launch_chains(g, c->offs.as<int32_t>(), cw, c->cbuf.as<int32_t>(), c->sm_count, st);
+    c->mark(ST_CHAINS, true);
+    c->mark(ST_MERGE, false);
+    launch_merge(g, c->offs.as<int32_t>(), cw, c->cbuf.as<int32_t>(), c->rec.as<int2>(), status, st);
+    c->mark(ST_MERGE, true);
+    // K5 fragments and sort keys
+    c->mark(ST_FRAGMENT, false);
+    launch_fragment(g, c->rec.as<int2>(), N, c->keys.as<uint64_t>(), c->wnp.as<uint8_t>(), dbg, st);
+    c->mark(ST_FRAGMENT, true);
     CUDA_TRY(cudaGetLastError());
 
     // K6 sort by (path, row rank, x)
@@ -223,8 +276,10 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     uint32_t key_bits = L.pbits + L.rbits + L.xbits;
     SortPlan sp = sort_plan(N, key_bits);
     CUDA_TRY(ensure(c->sort_scratch, sort_scratch_bytes(sp)));
+    c->mark(ST_SORT, false);
     launch_sort_u64(sp, c->keys.as<uint64_t>(), nullptr, c->skeys.as<uint64_t>(), c->svals.as<uint32_t>(),
                     c->keys_alt.as<uint64_t>(), c->vals_alt.as<uint32_t>(), c->sort_scratch.p, status, st);
+    c->mark(ST_SORT, true);
     CUDA_TRY(cudaGetLastError());
 
     // K7..K9 winding scan, flags and draw-list emit
@@ -257,7 +312,9 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     wa.dbg_fflag = keep ? c->d_fflag.as<int32_t>() : nullptr;
     wa.dbg_sflag = keep ? c->d_sflag.as<int32_t>() : nullptr;
     wa.dbg_skey = keep ? c->d_skey.as<int32_t>() : nullptr;
+    c->mark(ST_WINDING, false);
     launch_winding_emit(wa, c->wind_status.as<uint64_t>(), ctl + CTL_WIND_COUNTER, status, st);
+    c->mark(ST_WINDING, true);
     CUDA_TRY(cudaGetLastError());
     // read back the draw-list size (scanline_rasterizer.cpp:578-580)
     CUDA_TRY(cudaMemcpyAsync(c->h_tot, c->totals.p, sizeof(uint64_t) * 2, cudaMemcpyDeviceToHost, st));
@@ -286,9 +343,11 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     CUDA_TRY(ensure(c->row_start, sizeof(int32_t) * ((size_t)rows + 1)));
     SortPlan rp = sort_plan(O, bits_for((uint64_t)rows));
     CUDA_TRY(ensure(c->row_sort_scratch, sort_scratch_bytes(rp)));
+    c->mark(ST_ROWSORT, false);
     launch_sort_u32(rp, c->draw_row.as<uint32_t>(), nullptr, c->rkeys.as<uint32_t>(), c->rvals.as<uint32_t>(),
                     c->rkeys_alt.as<uint32_t>(), c->rvals_alt.as<uint32_t>(), c->row_sort_scratch.p, status, st);
     launch_row_bounds(c->rkeys.as<uint32_t>(), O, rows, c->row_start.as<int32_t>(), st);
+    c->mark(ST_ROWSORT, true);
     ResolveArgs ra;
     ra.draw = c->draw.as<int4>();
     ra.row_sorted_idx = c->rvals.as<uint32_t>();
@@ -298,8 +357,12 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     ra.F = c->F;
     ra.pixel_mode = g.pixel_mode;
     ra.image = c->image.as<uint32_t>();
+    c->mark(ST_RESOLVE, false);
     launch_resolve(ra, st);
+    c->mark(ST_RESOLVE, true);
     CUDA_TRY(cudaGetLastError());
+    c->stats.kernel_launches = (uint32_t)(launches_so_far() - launches0);
+    c->ev_pending = (c->flags & SR_FLAG_PROFILE) != 0;
     c->stages_valid = keep;
     return SR_OK;
 }
@@ -327,6 +390,8 @@ sr_status sr_create(uint32_t width, uint32_t height, const sr_options* opt, sr_c
     CUDA_TRY(cudaSetDevice(o.device));
     sr_ctx* c = new sr_ctx();
     c->device = o.device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, o.device);
+    if (c->sm_count <= 0) c->sm_count = 148;
     c->W = (int32_t)width;
     c->H = (int32_t)height;
     c->mode = o.mode;
@@ -421,8 +486,18 @@ sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) 
     return SR_OK;
 }
 
-sr_status sr_get_stats(const sr_ctx* c, sr_stats* out) {
-    if (!c || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+sr_status sr_get_stats(const sr_ctx* cc, sr_stats* out) {
+    if (!cc || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    sr_ctx* c = const_cast<sr_ctx*>(cc);
+    if (c->ev_pending) {
+        CUDA_TRY(cudaEventSynchronize(c->ev[2 * ST_RESOLVE + 1]));
+        for (int s = 0; s < ST_COUNT_ALL; ++s) {
+            float ms = 0.f;
+            if (c->ev[2 * s] && c->ev[2 * s + 1]) CUDA_TRY(cudaEventElapsedTime(&ms, c->ev[2 * s], c->ev[2 * s + 1]));
+            c->stats.stage_ms[s] = ms;
+        }
+        c->ev_pending = false;
+    }
     *out = c->stats;
     return SR_OK;
 }
@@ -439,7 +514,7 @@ sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
         case SR_STAGE_CUTPOINTS: src = c->cut.p; need = 20 * (size_t)c->C; need_stages = false; break;
         case SR_STAGE_CURVE_COUNT: src = c->count.p; need = 4 * (size_t)c->C; need_stages = false; break;
         case SR_STAGE_CURVE_OFFSET: src = c->offs.p; need = 4 * ((size_t)c->C + 1); need_stages = false; break;
-        case SR_STAGE_INTERSECTION: src = c->d_inter.p; need = 8 * N; break;
+        case SR_STAGE_INTERSECTION: src = c->rec.p; need = 8 * N; need_stages = false; break;
         case SR_STAGE_FRAG_KEY: src = c->d_fkey.p; need = 4 * N; break;
         case SR_STAGE_FRAG_WINDING: src = c->d_fwn.p; need = 4 * N; break;
         case SR_STAGE_FRAG_LEFT: src = c->d_fleft.p; need = 4 * N; break;

@@ -118,330 +118,462 @@ SR_DEV int32_t cut_range(int32_t size, int32_t F, int32_t& b, int32_t& e) {
     return imax((e - b) / F + 1, 0);
 }
 
-// ---------------------------------------------------------------- K2 ----
-// make_intersection_0.comp:226-411.  One thread per curve: path cull,
-// monotonic cut points (cached, 5 floats per curve) and the number of
-// intersection records the curve will emit.
-__global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restrict__ cut_cache,
-                                               int32_t* __restrict__ count) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.n_curves) return;
-    uint32_t type = g.curve_type[c];
-    CurvePts P;
-    load_curve(g.tpos, g.curve_pos[c], type, P);
-    bool vis = path_visible_mask(g.path_visible[g.curve_path[c]]);
-    const int32_t F = g.F;
-    uint32_t n = 0;
-    float q[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    if (vis) {
-#pragma unroll
-        for (int ax = 0; ax < 2; ++ax) {
-            const float* p = ax == 0 ? P.x : P.y;
-            if (type == 4u) {
-                float r0 = 0.0f, r1 = 0.0f;
-                float a = __fadd_rn(__fmul_rn(3.0f, __fsub_rn(p[1], p[2])), __fsub_rn(p[3], p[0]));
-                float b = __fmul_rn(2.0f, __fadd_rn(__fsub_rn(p[0], p[1]), __fsub_rn(p[2], p[1])));
-                solve_quad(a, b, __fsub_rn(p[1], p[0]), r0, r1);
-                if (r0 > 0.0f && r0 < 1.0f) q[n++] = r0;
-                if (r1 > 0.0f && r1 < 1.0f && r1 != r0) q[n++] = r1;
-            } else if (type == 3u) {
-                float den = __fadd_rn(__fsub_rn(p[0], p[1]), __fsub_rn(p[2], p[1]));
-                if (den != 0.0f) {
-                    float r0 = __fdiv_rn(__fsub_rn(p[0], p[1]), den);
-                    if (r0 > 0.0f && r0 < 1.0f) q[n++] = r0;
-                }
-            }
-        }
-        // insertion network of make_intersection_0.comp:315-359, including
-        // its `t2 = q3` (the 4th cut is never moved)
-        float q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
-        if (n >= 2) {
-            float t1 = q1, t0 = q0;
-            if (t1 < t0) { q1 = t0; q0 = t1; }
-        }
-        if (n >= 3) {
-            float t2 = q2, t1 = q1;
-            if (t2 < t1) {
-                q2 = t1;
-                float t0 = q0;
-                if (t2 < t0) { q1 = t0; q0 = t2; } else { q1 = t2; }
-            }
-        }
-        if (n >= 4) {
-            float t3 = q3, t2 = q3;
-            if (t3 < t2) {
-                q3 = t2;
-                float t1 = q1;
-                if (t3 < t1) {
-                    q2 = t1;
-                    float t0 = q0;
-                    if (t3 < t0) { q1 = t0; q0 = t3; } else { q1 = t3; }
-                } else {
-                    q2 = t3;
-                }
-            }
-        }
-        q[0] = q0; q[1] = q1; q[2] = q2; q[3] = q3;
-    }
-    float* cc = cut_cache + 5 * (size_t)c;
-    cc[0] = q[0];
-    cc[1] = q[1];
-    cc[2] = q[2];
-    cc[3] = q[3];
-    cc[4] = __uint_as_float(n);
-    if (vis) q[n++] = 1.0f;
-    float x0 = P.x[0], y0 = P.y[0];
-    const float fF = (float)F;
-    int32_t pc = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        float t1 = q[i];
-        float x1 = interp(type, t1, P.x), y1 = interp(type, t1, P.y);
-        int32_t xb, xe, yb, ye;
-        // get_xy_begin_end (make_intersection_0.comp:167-183)
-        if (x0 <= x1) {
-            xb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(x0, fF)), fF)), F);
-            xe = f2i(__fmul_rn(floorf(__fdiv_rn(x1, fF)), fF));
-        } else {
-            xb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(x1, fF)), fF)), F);
-            xe = f2i(__fmul_rn(floorf(__fdiv_rn(x0, fF)), fF));
-        }
-        if (y0 <= y1) {
-            yb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(y0, fF)), fF)), F);
-            ye = f2i(__fmul_rn(floorf(__fdiv_rn(y1, fF)), fF));
-        } else {
-            yb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(y1, fF)), fF)), F);
-            ye = f2i(__fmul_rn(floorf(__fdiv_rn(y0, fF)), fF));
-        }
-        int32_t nx = cut_range(g.W, F, xb, xe);
-        int32_t ny = cut_range(g.H, F, yb, ye);
-        pc = wadd(pc, wadd(1, wadd(nx, ny)));
-        x0 = x1;
-        y0 = y1;
-    }
-    count[c] = pc;
+
+// Pieces of a curve: at most 4 monotonic cuts + the end at t = 1.
+constexpr int kMaxPieces = 5;
+
+// Piece record layout in the output: [t0][x crossings][y crossings], the
+// crossing values of each side solved by one chain (k_chains), then merged
+// in t order (k_merge).  PieceInfo packs what the chains and the merge need.
+SR_DEV uint32_t pack_n(int32_t nx, bool xneg, int32_t ny, bool yneg) {
+    return (uint32_t)nx | (xneg ? 0x8000u : 0u) | ((uint32_t)ny << 16) | (yneg ? 0x80000000u : 0u);
+}
+SR_DEV int32_t piece_nx(uint32_t n) { return (int32_t)(n & 0x7FFFu); }
+SR_DEV int32_t piece_ny(uint32_t n) { return (int32_t)((n >> 16) & 0x7FFFu); }
+
+// Chain buckets by length, longest first, so that the longest dependency
+// chains start in the first wave of k_chains.
+SR_DEV uint32_t chain_bucket(int32_t len) {
+    return len >= 1024 ? 0u : (len >= 256 ? 1u : (len >= 32 ? 2u : 3u));
 }
 
-// ---------------------------------------------------------- K4 + K5 -----
-// Fragment of one record (gen_fragment.comp:100-200) given its piece
-// [t0, t1) on curve P.  Returns the 64-bit sort key, the winding change and
-// (pixel mode) the centre-sample part of the change.
-struct FragOut {
-    uint64_t key;
-    int32_t yx;
-    int32_t wn;
-    int32_t left;
+// get_xy_begin_end_delta + udpate_cut_range for one axis
+// (make_intersection_1.comp:150-213): number of grid crossings, first
+// grid line and step.
+SR_DEV int32_t axis_range_rd(float a0, float a1, int32_t size, int32_t F, float& start, bool& neg) {
+    const float invF = 1.0f / (float)F;   // x / F == x * (1/F) exactly for F in {1, 2}
+    int32_t b, e;
+    if (a0 <= a1) {
+        b = wadd(wmul(float2int_rd(__fmul_rn(a0, invF)), F), F);
+        e = wmul(float2int_rd(__fmul_rn(a1, invF)), F);
+        neg = false;
+    } else {
+        b = wadd(wmul(float2int_rd(__fmul_rn(a1, invF)), F), F);
+        e = wmul(float2int_rd(__fmul_rn(a0, invF)), F);
+        neg = true;
+    }
+    int32_t n = cut_range(size, F, b, e);
+    start = (float)(neg ? e : b);
+    return n;
+}
+
+// ---------------------------------------------------------------- K2 ----
+// make_intersection_0.comp:226-411.  One thread per curve: path cull,
+// monotonic cut points (cached, 5 floats per curve), the number of records
+// the curve emits (the reference's count), and the set-up of each piece's
+// x and y crossing chains, which are appended to length buckets.
+__global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restrict__ cut_cache,
+                                               int32_t* __restrict__ count, uint4* __restrict__ pieces,
+                                               uint32_t* __restrict__ chain_lists, uint32_t list_cap,
+                                               uint32_t* __restrict__ bucket_count, uint32_t* __restrict__ status) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = c < g.n_curves;
+    uint32_t my_chains[2 * kMaxPieces];
+    uint32_t my_bucket[2 * kMaxPieces];
+    int n_chains = 0;
+    if (active) {
+        uint32_t type = g.curve_type[c];
+        CurvePts P;
+        load_curve(g.tpos, g.curve_pos[c], type, P);
+        bool vis = path_visible_mask(g.path_visible[g.curve_path[c]]);
+        const int32_t F = g.F;
+        uint32_t n = 0;
+        float q[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        if (vis) {
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                const float* p = ax == 0 ? P.x : P.y;
+                if (type == 4u) {
+                    float r0 = 0.0f, r1 = 0.0f;
+                    float a = __fadd_rn(__fmul_rn(3.0f, __fsub_rn(p[1], p[2])), __fsub_rn(p[3], p[0]));
+                    float b = __fmul_rn(2.0f, __fadd_rn(__fsub_rn(p[0], p[1]), __fsub_rn(p[2], p[1])));
+                    solve_quad(a, b, __fsub_rn(p[1], p[0]), r0, r1);
+                    if (r0 > 0.0f && r0 < 1.0f) q[n++] = r0;
+                    if (r1 > 0.0f && r1 < 1.0f && r1 != r0) q[n++] = r1;
+                } else if (type == 3u) {
+                    float den = __fadd_rn(__fsub_rn(p[0], p[1]), __fsub_rn(p[2], p[1]));
+                    if (den != 0.0f) {
+                        float r0 = __fdiv_rn(__fsub_rn(p[0], p[1]), den);
+                        if (r0 > 0.0f && r0 < 1.0f) q[n++] = r0;
+                    }
+                }
+            }
+            // insertion network of make_intersection_0.comp:315-359, including
+            // its `t2 = q3` (the 4th cut is never moved)
+            float q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+            if (n >= 2) {
+                float t1 = q1, t0 = q0;
+                if (t1 < t0) { q1 = t0; q0 = t1; }
+            }
+            if (n >= 3) {
+                float t2 = q2, t1 = q1;
+                if (t2 < t1) {
+                    q2 = t1;
+                    float t0 = q0;
+                    if (t2 < t0) { q1 = t0; q0 = t2; } else { q1 = t2; }
+                }
+            }
+            if (n >= 4) {
+                float t3 = q3, t2 = q3;
+                if (t3 < t2) {
+                    q3 = t2;
+                    float t1 = q1;
+                    if (t3 < t1) {
+                        q2 = t1;
+                        float t0 = q0;
+                        if (t3 < t0) { q1 = t0; q0 = t3; } else { q1 = t3; }
+                    } else {
+                        q2 = t3;
+                    }
+                }
+            }
+            q[0] = q0; q[1] = q1; q[2] = q2; q[3] = q3;
+        }
+        float* cc = cut_cache + 5 * (size_t)c;
+        cc[0] = q[0];
+        cc[1] = q[1];
+        cc[2] = q[2];
+        cc[3] = q[3];
+        cc[4] = __uint_as_float(n);
+        if (vis) q[n++] = 1.0f;
+        float x0 = P.x[0], y0 = P.y[0];
+        const float fF = (float)F;
+        int32_t pc = 0, walk = 0;
+        uint4* pt = pieces + (size_t)c * kMaxPieces;
+#pragma unroll
+        for (uint32_t i = 0; i < (uint32_t)kMaxPieces; ++i) {
+            if (i >= n) break;
+            float t1 = q[i];
+            float x1 = interp(type, t1, P.x), y1 = interp(type, t1, P.y);
+            // count: get_xy_begin_end (make_intersection_0.comp:167-183)
+            int32_t xb, xe, yb, ye;
+            if (x0 <= x1) {
+                xb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(x0, fF)), fF)), F);
+                xe = f2i(__fmul_rn(floorf(__fdiv_rn(x1, fF)), fF));
+            } else {
+                xb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(x1, fF)), fF)), F);
+                xe = f2i(__fmul_rn(floorf(__fdiv_rn(x0, fF)), fF));
+            }
+            if (y0 <= y1) {
+                yb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(y0, fF)), fF)), F);
+                ye = f2i(__fmul_rn(floorf(__fdiv_rn(y1, fF)), fF));
+            } else {
+                yb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(y1, fF)), fF)), F);
+                ye = f2i(__fmul_rn(floorf(__fdiv_rn(y0, fF)), fF));
+            }
+            int32_t nxc = cut_range(g.W, F, xb, xe);
+            int32_t nyc = cut_range(g.H, F, yb, ye);
+            pc = wadd(pc, wadd(1, wadd(nxc, nyc)));
+            // chain set-up: the intersection pass's own range formulas
+            float sx, sy;
+            bool xneg, yneg;
+            int32_t nx = axis_range_rd(x0, x1, g.W, F, sx, xneg);
+            int32_t ny = axis_range_rd(y0, y1, g.H, F, sy, yneg);
+            int32_t tb = fbits(t1) & ~3;
+            tb |= (floorf(x1) == x1) ? 2 : 3;   // make_intersection_1.comp:271-276
+            pt[i] = make_uint4(pack_n(nx, xneg, ny, yneg), (uint32_t)tb, __float_as_uint(sx), __float_as_uint(sy));
+            if (nx > 0) {
+                my_chains[n_chains] = (c << 4) | (i << 1) | 0u;
+                my_bucket[n_chains++] = chain_bucket(nx);
+            }
+            if (ny > 0) {
+                my_chains[n_chains] = (c << 4) | (i << 1) | 1u;
+                my_bucket[n_chains++] = chain_bucket(ny);
+            }
+            walk += 1 + nx + ny;
+            x0 = x1;
+            y0 = y1;
+        }
+        count[c] = pc;
+        if (walk != pc) set_error(status, ERR_RECORD_RANGE);
+    }
+    // append chains to their buckets (warp-aggregated per bucket)
+    const uint32_t lane = lane_id();
+    for (int k = 0; k < 2 * kMaxPieces; ++k) {
+        bool has = k < n_chains;
+        if (!__any_sync(0xFFFFFFFFu, has)) break;
+        uint32_t b = has ? my_bucket[k] : 4u;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
+        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t base = 0;
+        if (has && lane == leader) base = atomicAdd(&bucket_count[b], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (has) {
+            uint32_t slot = base + (uint32_t)__popc(peers & lanemask_lt());
+            if (slot < list_cap) chain_lists[(size_t)b * list_cap + slot] = my_chains[k];
+            else set_error(status, ERR_CAPACITY);
+        }
+    }
+}
+
+// ------------------------------------------------------------ chains -----
+// One crossing chain: the successive roots of one coordinate of one piece
+// at the grid lines start, start+d, ... (make_intersection_1.comp:377-440).
+// Each solve starts from the previous root of the same side (flag bits
+// included), so a chain is sequential but chains are independent.
+struct AxisPoly {
+    float p0, p1, p2, p3;
+    float d01, d12, d23;
 };
 
-SR_DEV FragOut make_fragment(const GeomArgs& g, uint32_t path, float t0, float t1, float pfx, float pfy,
-                             float plx, float ply) {
-    FragOut o;
-    o.yx = (int32_t)0xFFFEFFFE;
-    o.wn = 0;
-    o.left = 0;
+template <int kType> SR_DEV float eval_axis(const AxisPoly& a, float t) {
+    if (kType == 2) return __fadd_rn(a.p0, __fmul_rn(t, a.d01));
+    float q0 = __fadd_rn(a.p0, __fmul_rn(t, a.d01));
+    float q1 = __fadd_rn(a.p1, __fmul_rn(t, a.d12));
+    if (kType == 3) return __fadd_rn(q0, __fmul_rn(t, __fsub_rn(q1, q0)));
+    float q2 = __fadd_rn(a.p2, __fmul_rn(t, a.d23));
+    float l0 = __fadd_rn(q0, __fmul_rn(t, __fsub_rn(q1, q0)));
+    float l1 = __fadd_rn(q1, __fmul_rn(t, __fsub_rn(q2, q1)));
+    return __fadd_rn(l0, __fmul_rn(t, __fsub_rn(l1, l0)));
+}
+
+SR_DEV bool same_sign(float a, float c, float b) {
+    return (fbits(__fsub_rn(a, c)) ^ fbits(__fsub_rn(b, c))) >= 0;
+}
+
+// 24-step bisection of the reference (make_intersection_1.comp:402-434).
+// kSpec evaluates both possible next midpoints with the current one, so
+// two steps cost one dependent curve evaluation; the values and decisions
+// are exactly those of the one-step loop.
+template <int kType, bool kSpec>
+SR_DEV float bisect(const AxisPoly& a, float c, float t_min, float t_max) {
+    float ta = t_min, tb = t_max;
+    float vt0 = eval_axis<kType>(a, ta);
+    float t_solve = ta;
+    if (vt0 == c) return t_solve;
+    float last = 0.0f;
+    if (kSpec) {
+#pragma unroll 2
+        for (int j = 0; j < 12; ++j) {
+            float tm = __fmul_rn(__fadd_rn(ta, tb), 0.5f);
+            float mL = __fmul_rn(__fadd_rn(ta, tm), 0.5f);
+            float mR = __fmul_rn(__fadd_rn(tm, tb), 0.5f);
+            float v = eval_axis<kType>(a, tm);
+            float vL = eval_axis<kType>(a, mL);
+            float vR = eval_axis<kType>(a, mR);
+            bool r1 = same_sign(v, c, vt0);
+            float ta1 = r1 ? tm : ta, tb1 = r1 ? tb : tm, vt1 = r1 ? v : vt0;
+            float m2 = r1 ? mR : mL, v2 = r1 ? vR : vL;
+            bool r2 = same_sign(v2, c, vt1);
+            ta = r2 ? m2 : ta1;
+            tb = r2 ? tb1 : m2;
+            vt0 = r2 ? v2 : vt1;
+            t_solve = m2;
+            last = v2;
+        }
+    } else {
+#pragma unroll 4
+        for (int j = 0; j < 24; ++j) {
+            float tm = __fmul_rn(__fadd_rn(ta, tb), 0.5f);
+            float v = eval_axis<kType>(a, tm);
+            t_solve = tm;
+            last = v;
+            if (same_sign(v, c, vt0)) {
+                ta = tm;
+                vt0 = v;
+            } else {
+                tb = tm;
+            }
+        }
+    }
+    if (fabsf(__fsub_rn(last, c)) > 1.0f) t_solve = t_min;
+    return t_solve;
+}
+
+template <int kType, bool kSpec>
+SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t_lo, float t_hi, int side,
+                      int32_t* __restrict__ out) {
+    float lo = t_lo;
+    float inv = 0.0f;
+    if (kType == 2) {
+        float d = __fsub_rn(a.p1, a.p0);
+        inv = (d != 0.0f) ? __fdiv_rn(1.0f, d) : 0.0f;
+    }
+    for (int32_t k = 0; k < len; ++k) {
+        float c = x;
+        x = __fadd_rn(x, dx);
+        float t;
+        if (kType == 2) t = gmin(gmax(__fmul_rn(__fsub_rn(c, a.p0), inv), lo), t_hi);
+        else t = bisect<kType, kSpec>(a, c, lo, t_hi);
+        int32_t ob = (fbits(t) & ~3) | side;
+        out[k] = ob;
+        lo = bitsf(ob);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t* __restrict__ offs,
+                                                const uint4* __restrict__ pieces,
+                                                const uint32_t* __restrict__ chain_lists, uint32_t list_cap,
+                                                const uint32_t* __restrict__ bucket_count,
+                                                int32_t* __restrict__ cbuf) {
+    uint32_t nb[4];
+    uint32_t total = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        nb[b] = imin((int32_t)bucket_count[b], (int32_t)list_cap);
+        total += nb[b];
+    }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += stride) {
+        uint32_t b = 0, r = it;
+        while (b < 3 && r >= nb[b]) { r -= nb[b]; ++b; }
+        uint32_t item = chain_lists[(size_t)b * list_cap + r];
+        uint32_t c = item >> 4, piece = (item >> 1) & 7u;
+        int side = (int)(item & 1u);
+        uint32_t type = g.curve_type[c];
+        const uint4* pt = pieces + (size_t)c * kMaxPieces;
+        int64_t base = offs[c];
+        for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
+        uint4 me = pt[piece];
+        int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
+        base += 1 + (side ? nx : 0);
+        int32_t len = side ? ny : nx;
+        bool neg = side ? (me.x & 0x80000000u) != 0 : (me.x & 0x8000u) != 0;
+        float x = __uint_as_float(side ? me.w : me.z);
+        float dx = neg ? -(float)g.F : (float)g.F;
+        float t_lo = piece == 0 ? 0.0f : __uint_as_float(pt[piece - 1].y);
+        float t_hi = __uint_as_float(me.y);
+        const float2* cp = g.tpos + g.curve_pos[c];
+        AxisPoly a;
+        uint32_t np = type & 7u;
+        float p[4];
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+            float2 v = k < np ? cp[k] : make_float2(0.0f, 0.0f);
+            p[k] = side ? v.y : v.x;
+        }
+        a.p0 = p[0]; a.p1 = p[1]; a.p2 = p[2]; a.p3 = p[3];
+        a.d01 = __fsub_rn(p[1], p[0]);
+        a.d12 = __fsub_rn(p[2], p[1]);
+        a.d23 = __fsub_rn(p[3], p[2]);
+        int32_t* out = cbuf + base;
+        const bool spec = b < 3;
+        if (type == 2u) run_chain<2, false>(a, len, x, dx, t_lo, t_hi, side, out);
+        else if (type == 3u) {
+            if (spec) run_chain<3, true>(a, len, x, dx, t_lo, t_hi, side, out);
+            else run_chain<3, false>(a, len, x, dx, t_lo, t_hi, side, out);
+        } else {
+            if (spec) run_chain<4, true>(a, len, x, dx, t_lo, t_hi, side, out);
+            else run_chain<4, false>(a, len, x, dx, t_lo, t_hi, side, out);
+        }
+    }
+}
+
+// ------------------------------------------------------------- merge -----
+// The record order of make_intersection_1.comp:310-441: per piece, the
+// start t0 and the two chains merged by `next_tx <= next_ty`, an exhausted
+// side counting as 2.0 (with its side bit); a record whose t (flag bits
+// masked) equals the previous one ORs the flags into both
+// (make_intersection_1.comp:361-375).
+__global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* __restrict__ offs,
+                                               const uint4* __restrict__ pieces, const int32_t* __restrict__ cbuf,
+                                               int2* __restrict__ rec, uint32_t* __restrict__ status) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= g.n_curves) return;
+    int64_t pc = offs[c];
+    const int64_t end = offs[c + 1];
+    if (pc >= end) return;
+    const uint4* pt = pieces + (size_t)c * kMaxPieces;
+    const int32_t minus_one = fbits(-1.0f);
+    const int32_t ex_x = fbits(2.0f), ex_y = fbits(2.0f) | 1;
+    int32_t t0 = 0;   // bits of 0.0f
+    for (int i = 0; i < kMaxPieces && pc < end; ++i) {
+        uint4 me = pt[i];
+        int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
+        const int32_t* X = cbuf + pc + 1;
+        const int32_t* Y = X + nx;
+        // heads: A = x side, B = y side (make_intersection_1.comp:321-359)
+        int32_t ia = 0, ib = 0;
+        // both sides cross: A = x chain, B = [t0, y chain]; no x crossing:
+        // A empty, B = [t0, y chain]; no y crossing: A = [t0, x chain], B empty
+        const bool a_has_t0 = (nx > 0 && ny == 0);
+        const int32_t lenA = nx + (a_has_t0 ? 1 : 0);
+        const int32_t lenB = a_has_t0 ? 0 : ny + 1;
+        int32_t n_loop = nx + ny + 1;
+        if (pc + n_loop > end) {
+            set_error(status, ERR_RECORD_RANGE);
+            return;
+        }
+        int32_t last = minus_one;
+        for (int32_t k = 0; k < n_loop; ++k) {
+            int32_t av = ex_x, bv = ex_y;
+            if (ia < lenA) av = a_has_t0 ? (ia == 0 ? t0 : X[ia - 1]) : X[ia];
+            if (ib < lenB) bv = ib == 0 ? t0 : Y[ib - 1];
+            int32_t out;
+            if (bitsf(av) <= bitsf(bv)) {
+                out = av;
+                ++ia;
+            } else {
+                out = bv;
+                ++ib;
+            }
+            if ((out & ~3) == (last & ~3)) {
+                out |= last;
+                rec[pc - 1] = make_int2((int32_t)c, out);
+            }
+            rec[pc] = make_int2((int32_t)c, out);
+            last = out;
+            ++pc;
+        }
+        t0 = (int32_t)me.y;
+    }
+    if (pc != end) set_error(status, ERR_RECORD_RANGE);
+}
+
+// ---------------------------------------------------------- fragment -----
+// gen_fragment.comp:90-245, one thread per record: the piece between this
+// record's t and the next record's t (t = 1 when the next record belongs to
+// another curve), its cell, the 64-bit sort key, the winding change across
+// the sample row and (pixel mode) the part of it left of the cell centre.
+__global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* __restrict__ rec, int64_t n,
+                                                  uint64_t* __restrict__ keys, uint8_t* __restrict__ wnp,
+                                                  DebugOut dbg) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int2 r0 = rec[i];
+    int2 r1 = (i + 1 != n) ? rec[i + 1] : make_int2(-1, 0x3f800000);
+    float t0 = gmax(bitsf(r0.y & ~3), 0.0f);
+    float t1 = gmax(bitsf(r1.y & ~3), 0.0f);
+    uint32_t c = (uint32_t)r0.x;
+    uint32_t path = g.curve_path[c];
+    if (r0.x != r1.x) t1 = 1.0f;
+    int32_t yx = (int32_t)0xFFFEFFFE, wn = 0, left = 0;
     bool valid = false;
     int32_t pos_x = 0, pos_y = 0;
     if (t0 < t1) {
+        uint32_t type = g.curve_type[c];
+        CurvePts P;
+        load_curve(g.tpos, g.curve_pos[c], type, P);
+        float pfx = interp(type, t0, P.x), pfy = interp(type, t0, P.y);
+        float plx = interp(type, t1, P.x), ply = interp(type, t1, P.y);
         const int32_t F = g.F;
-        const float fF = (float)F;
-        int32_t rx = wmul(float2int_rd(__fdiv_rn(__fmul_rn(__fadd_rn(pfx, plx), 0.5f), fF)), F);
-        int32_t ry = wmul(float2int_rd(__fdiv_rn(__fmul_rn(__fadd_rn(pfy, ply), 0.5f), fF)), F);
+        const float invF = 1.0f / (float)F;   // exact: F is 1 or 2
+        int32_t rx = wmul(float2int_rd(__fmul_rn(__fmul_rn(__fadd_rn(pfx, plx), 0.5f), invF)), F);
+        int32_t ry = wmul(float2int_rd(__fmul_rn(__fmul_rn(__fadd_rn(pfy, ply), 0.5f), invF)), F);
         pos_x = imin(imax(rx, -F), wadd(g.W & (int32_t)0xFFFFFFFE, F));
         pos_y = imin(imax(ry, -F), wadd(g.H & (int32_t)0xFFFFFFFE, F));
         if ((uint32_t)ry < (uint32_t)g.H) {
             valid = true;
-            o.yx = (int32_t)(((uint32_t)wadd(pos_y, 0x7FFF) << 16) | ((uint32_t)wadd(pos_x, 0x7FFF) & 0xFFFFu));
+            yx = (int32_t)(((uint32_t)wadd(pos_y, 0x7FFF) << 16) | ((uint32_t)wadd(pos_x, 0x7FFF) & 0xFFFFu));
         }
         // winding sample row cell_y + FRAG_SIZE/2 (gen_fragment.comp:188-199)
-        float wn_y = __fadd_rn((float)pos_y, __fmul_rn(0.5f, fF));
-        if (pfy == ply) o.wn = 0;
-        else if (pfy < wn_y && wn_y <= ply) o.wn = -1;
-        else if (ply < wn_y && wn_y <= pfy) o.wn = 1;
-        if (g.pixel_mode && o.wn != 0) {
+        float wn_y = __fadd_rn((float)pos_y, __fmul_rn(0.5f, (float)F));
+        if (pfy == ply) wn = 0;
+        else if (pfy < wn_y && wn_y <= ply) wn = -1;
+        else if (ply < wn_y && wn_y <= pfy) wn = 1;
+        if (g.pixel_mode && wn != 0) {
             float dyv = __fsub_rn(ply, pfy);
             float tc = __fdiv_rn(__fsub_rn(wn_y, pfy), dyv);
             float xc = __fadd_rn(pfx, __fmul_rn(tc, __fsub_rn(plx, pfx)));
-            if (xc < __fadd_rn((float)pos_x, 0.5f)) o.left = o.wn;
+            if (xc < __fadd_rn((float)pos_x, 0.5f)) left = wn;
         }
     }
-    o.key = pack_key(g.L, path, valid, pos_y, pos_x);
-    return o;
-}
-
-// make_intersection_1.comp:217-447 fused with gen_fragment.comp:90-245.
-// One thread per curve walks each monotonic piece across the FRAG_SIZE grid
-// in t order, emitting the reference's intersection records; the fragment
-// of record k is built when record k+1's t is known (the last record of a
-// curve ends at t = 1).  Writes the sort key and packed winding bits of
-// every record; debug pointers, when set, receive the reference layouts.
-__global__ void __launch_bounds__(128) k_intersect_fragment(const GeomArgs g, const float* __restrict__ cut_cache,
-                                                            const int32_t* __restrict__ offs,
-                                                            uint64_t* __restrict__ keys,
-                                                            uint8_t* __restrict__ wnp, DebugOut dbg,
-                                                            uint32_t* __restrict__ status) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.n_curves) return;
-    const int32_t F = g.F;
-    uint32_t type = g.curve_type[c];
-    uint32_t path = g.curve_path[c];
-    CurvePts P;
-    load_curve(g.tpos, g.curve_pos[c], type, P);
-    bool vis = path_visible_mask(g.path_visible[path]);
-    const float* cc = cut_cache + 5 * (size_t)c;
-    float q[5] = {cc[0], cc[1], cc[2], cc[3], 0.0f};
-    uint32_t n = __float_as_uint(cc[4]);
-    if (n > 4) n = 4;
-    if (vis) q[n++] = 1.0f;
-    int64_t pc = offs[c];
-    const int64_t end = offs[c + 1];
-    if (pc >= end) return;
-
-    float t0_ms = 0.0f;
-    float x0m = P.x[0], y0m = P.y[0];
-    const int32_t minus_one = fbits(-1.0f);
-    // pending record: emitted, fragment not yet built
-    bool have_prev = false;
-    float prev_t = 0.0f, prev_x = 0.0f, prev_y = 0.0f;
-    const float fF = (float)F;
-
-    for (uint32_t i = 0; i < n; ++i) {
-        float t1_ms = q[i];
-        float x1m = interp(type, t1_ms, P.x), y1m = interp(type, t1_ms, P.y);
-        int32_t tb = fbits(t1_ms) & ~3;
-        tb |= (floorf(x1m) == x1m) ? 2 : 3;   // make_intersection_1.comp:271-276
-        t1_ms = bitsf(tb);
-        int32_t xb, xe, yb, ye;
-        float dx, dy;
-        // get_xy_begin_end_delta (make_intersection_1.comp:150-170)
-        if (x0m <= x1m) {
-            xb = wadd(wmul(float2int_rd(__fdiv_rn(x0m, fF)), F), F);
-            xe = wmul(float2int_rd(__fdiv_rn(x1m, fF)), F);
-            dx = fF;
-        } else {
-            xb = wadd(wmul(float2int_rd(__fdiv_rn(x1m, fF)), F), F);
-            xe = wmul(float2int_rd(__fdiv_rn(x0m, fF)), F);
-            dx = -fF;
-        }
-        if (y0m <= y1m) {
-            yb = wadd(wmul(float2int_rd(__fdiv_rn(y0m, fF)), F), F);
-            ye = wmul(float2int_rd(__fdiv_rn(y1m, fF)), F);
-            dy = fF;
-        } else {
-            yb = wadd(wmul(float2int_rd(__fdiv_rn(y1m, fF)), F), F);
-            ye = wmul(float2int_rd(__fdiv_rn(y0m, fF)), F);
-            dy = -fF;
-        }
-        int32_t nx = cut_range(g.W, F, xb, xe);
-        int32_t ny = cut_range(g.H, F, yb, ye);
-        int32_t n_loop = nx + ny + 1;
-        float x = (float)(dx < 0.0f ? xe : xb);
-        float y = (float)(dy < 0.0f ? ye : yb);
-        float tnx = t0_ms, tny = t0_ms;
-        int32_t last = minus_one;
-        for (int32_t it = -1; it < n_loop; ++it) {
-            float t_solve = 0.0f, cval = 0.0f, t_min;
-            int side = 0;
-            if (it == -1) {
-                t_min = tnx;
-                if (nx == 0) { side = 0; t_solve = 2.0f; }
-                else if (ny == 0) { side = 1; t_solve = 2.0f; }
-                else { side = 0; --nx; cval = x; x = __fadd_rn(x, dx); }
-            } else if (tnx <= tny) {
-                t_min = tnx;
-                side = 0;
-                if (nx > 0) { --nx; cval = x; x = __fadd_rn(x, dx); }
-                else t_solve = 2.0f;
-            } else {
-                t_min = tny;
-                side = 1;
-                if (ny > 0) { --ny; cval = y; y = __fadd_rn(y, dy); }
-                else t_solve = 2.0f;
-            }
-            if (it >= 0) {
-                // emit record (make_intersection_1.comp:361-375)
-                int32_t out = fbits(t_min);
-                if ((out & ~3) == (last & ~3)) {
-                    out |= last;
-                    if (dbg.inter) dbg.inter[pc - 1] = make_int2((int32_t)c, out);
-                }
-                if (pc >= end) {
-                    set_error(status, ERR_RECORD_RANGE);
-                    return;
-                }
-                if (dbg.inter) dbg.inter[pc] = make_int2((int32_t)c, out);
-                last = out;
-                float tcur = bitsf(out & ~3);
-                tcur = gmax(tcur, 0.0f);
-                float cx = interp(type, tcur, P.x), cy = interp(type, tcur, P.y);
-                if (have_prev) {
-                    FragOut fo = make_fragment(g, path, prev_t, tcur, prev_x, prev_y, cx, cy);
-                    size_t k = (size_t)(pc - 1);
-                    keys[k] = fo.key;
-                    wnp[k] = (uint8_t)((fo.wn & 3) | ((fo.left & 3) << 2));
-                    if (dbg.fkey) {
-                        dbg.fkey[k] = fo.yx;
-                        dbg.fwn[k] = fo.wn;
-                        dbg.fleft[k] = fo.left;
-                    }
-                }
-                have_prev = true;
-                prev_t = tcur;
-                prev_x = cx;
-                prev_y = cy;
-                ++pc;
-            }
-            if (t_solve < 2.0f) {
-                const float* cv = side == 0 ? P.x : P.y;
-                if (type == 2u) {
-                    float a = __fsub_rn(cv[1], cv[0]);
-                    a = (a != 0.0f) ? __fdiv_rn(1.0f, a) : 0.0f;
-                    t_solve = gmin(gmax(__fmul_rn(__fsub_rn(cval, cv[0]), a), t_min), t1_ms);
-                } else {
-                    float ta = t_min, tb1 = t1_ms;
-                    float vt0 = interp(type, ta, cv);
-                    t_solve = ta;
-                    if (vt0 != cval) {
-                        float raw_t0 = ta, last_vtm = 0.0f;
-#pragma unroll 4
-                        for (int j = 0; j < 24; ++j) {
-                            float tm = __fmul_rn(__fadd_rn(ta, tb1), 0.5f);
-                            float vtm = interp(type, tm, cv);
-                            t_solve = tm;
-                            last_vtm = vtm;
-                            if ((fbits(__fsub_rn(vtm, cval)) ^ fbits(__fsub_rn(vt0, cval))) >= 0) {
-                                ta = tm;
-                                vt0 = vtm;
-                            } else {
-                                tb1 = tm;
-                            }
-                        }
-                        if (fabsf(__fsub_rn(last_vtm, cval)) > 1.0f) t_solve = raw_t0;
-                    }
-                }
-            }
-            int32_t nb = (fbits(t_solve) & ~3) | side;
-            if (side == 0) tnx = bitsf(nb);
-            else tny = bitsf(nb);
-        }
-        t0_ms = t1_ms;
-        x0m = x1m;
-        y0m = y1m;
-    }
-    if (pc != end) {
-        set_error(status, ERR_RECORD_RANGE);
-        return;
-    }
-    if (have_prev) {
-        // last record of the curve: its piece ends at t = 1
-        float cx = interp(type, 1.0f, P.x), cy = interp(type, 1.0f, P.y);
-        FragOut fo = make_fragment(g, path, prev_t, 1.0f, prev_x, prev_y, cx, cy);
-        size_t k = (size_t)(end - 1);
-        keys[k] = fo.key;
-        wnp[k] = (uint8_t)((fo.wn & 3) | ((fo.left & 3) << 2));
-        if (dbg.fkey) {
-            dbg.fkey[k] = fo.yx;
-            dbg.fwn[k] = fo.wn;
-            dbg.fleft[k] = fo.left;
-        }
+    keys[i] = pack_key(g.L, path, valid, pos_y, pos_x);
+    wnp[i] = (uint8_t)((wn & 3) | ((left & 3) << 2));
+    if (dbg.fkey) {
+        dbg.fkey[i] = yx;
+        dbg.fwn[i] = wn;
+        dbg.fleft[i] = left;
     }
 }
 
@@ -449,18 +581,40 @@ __global__ void __launch_bounds__(128) k_intersect_fragment(const GeomArgs g, co
 void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const Mvp& M, float fw,
                       float fh, float2* tpos, int32_t* path_visible, cudaStream_t st) {
     if (n_points == 0) return;
+    count_launches(1);
     k_transform<<<(n_points + 255) / 256, 256, 0, st>>>(pos, pos_path, n_points, M, fw, fh, tpos, path_visible);
 }
 
-void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, cudaStream_t st) {
+size_t piece_table_bytes(uint32_t n_curves) { return sizeof(uint4) * kMaxPieces * (size_t)n_curves; }
+uint32_t chain_list_capacity(uint32_t n_curves) { return 2u * kMaxPieces * n_curves; }
+
+void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const ChainWork& w, uint32_t* status,
+                  cudaStream_t st) {
     if (g.n_curves == 0) return;
-    k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count);
+    count_launches(1);
+    k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count, w.pieces, w.chain_lists, w.list_cap,
+                                                      w.bucket_count, status);
 }
 
-void launch_intersect_fragment(const GeomArgs& g, const float* cut_cache, const int32_t* offs, uint64_t* keys,
-                               uint8_t* wnp, const DebugOut& dbg, uint32_t* status, cudaStream_t st) {
+void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
+                   cudaStream_t st) {
     if (g.n_curves == 0) return;
-    k_intersect_fragment<<<(g.n_curves + 127) / 128, 128, 0, st>>>(g, cut_cache, offs, keys, wnp, dbg, status);
+    count_launches(1);
+    k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.chain_lists, w.list_cap, w.bucket_count, cbuf);
+}
+
+void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, const int32_t* cbuf, int2* rec,
+                  uint32_t* status, cudaStream_t st) {
+    if (g.n_curves == 0) return;
+    count_launches(1);
+    k_merge<<<(g.n_curves + 127) / 128, 128, 0, st>>>(g, offs, w.pieces, cbuf, rec, status);
+}
+
+void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n, uint64_t* keys, uint8_t* wnp,
+                     const DebugOut& dbg, cudaStream_t st) {
+    if (n <= 0) return;
+    count_launches(1);
+    k_fragment<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rec, n, keys, wnp, dbg);
 }
 
 }  // namespace sr

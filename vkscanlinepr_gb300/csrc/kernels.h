@@ -9,6 +9,10 @@
 
 namespace sr {
 
+// Number of kernels this library has launched in this process.
+void count_launches(uint32_t n);
+uint64_t launches_so_far();
+
 struct Mvp {
     float m[16];   // rows m0..m3
 };
@@ -28,17 +32,34 @@ struct GeomArgs {
 
 // Optional reference-layout outputs for parity dumps (all NULL in production).
 struct DebugOut {
-    int2* inter;        // [N] (curve, t bits | flags)
     int32_t* fkey;      // [N] packed yx
     int32_t* fwn;       // [N] winding change
     int32_t* fleft;     // [N] centre-sample part (pixel mode)
 };
 
+// Crossing-chain work of the intersection stage.
+struct ChainWork {
+    uint4* pieces;            // [n_curves][5] per-piece chain set-up
+    uint32_t* chain_lists;    // [4][list_cap] chain ids by length bucket
+    uint32_t list_cap;
+    uint32_t* bucket_count;   // [4] zeroed before the count pass
+};
+size_t piece_table_bytes(uint32_t n_curves);
+uint32_t chain_list_capacity(uint32_t n_curves);
+
 void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const Mvp& M, float fw,
                       float fh, float2* tpos, int32_t* path_visible, cudaStream_t st);
-void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, cudaStream_t st);
-void launch_intersect_fragment(const GeomArgs& g, const float* cut_cache, const int32_t* offs, uint64_t* keys,
-                               uint8_t* wnp, const DebugOut& dbg, uint32_t* status, cudaStream_t st);
+void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const ChainWork& w, uint32_t* status,
+                  cudaStream_t st);
+// Crossing chains (longest first) then the per-curve merge into the
+// reference's intersection records rec[N] (curve, t bits | flags).
+void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
+                   cudaStream_t st);
+void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, const int32_t* cbuf, int2* rec,
+                  uint32_t* status, cudaStream_t st);
+// One fragment per record: sort key + packed winding bits.
+void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n, uint64_t* keys, uint8_t* wnp,
+                     const DebugOut& dbg, cudaStream_t st);
 
 // ---- scan.cu
 // Exclusive scan of n int32 values into out[0..n] (out[n] = total), single

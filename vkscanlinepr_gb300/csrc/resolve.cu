@@ -119,6 +119,7 @@ void launch_resolve(const ResolveArgs& a, cudaStream_t st) {
         cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = smem;
     }
+    count_launches(1);
     k_resolve<<<rows, kResolveThreads, smem, st>>>(a);
 }
 
@@ -126,6 +127,7 @@ void launch_row_bounds(const uint32_t* srows, int64_t n, int32_t rows, int32_t* 
     int64_t work = n + 1;
     int blocks = (int)((work + 255) / 256);
     if (blocks > 1216) blocks = 1216;
+    count_launches(1);
     k_row_bounds<<<blocks, 256, 0, st>>>(srows, n, rows, row_start);
 }
 

@@ -143,6 +143,7 @@ void launch_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, uint6
         return;
     }
     int64_t tiles = (n + kTile - 1) / kTile;
+    count_launches(1);
     k_scan_i32<<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, tile_status, tile_counter, status);
 }
 

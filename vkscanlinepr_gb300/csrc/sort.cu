@@ -282,7 +282,9 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
     cudaMemsetAsync(s.lookback, 0, sizeof(uint32_t) * lb_words, st);
     int hb = (int)((p.n + kThreads - 1) / kThreads);
     if (hb > kHistBlocks) hb = kHistBlocks;
+    count_launches(1);
     k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.passes, s.hist);
+    count_launches(1);
     k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
     const size_t smem = sizeof(OnesweepSmem<K>);
     static bool attr_set = false;
@@ -296,6 +298,7 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
         bool to_out = ((p.passes - 1 - pass) % 2) == 0;
         K* kdst = to_out ? keys_out : keys_alt;
         uint32_t* vdst = to_out ? vals_out : vals_alt;
+        count_launches(1);
         k_onesweep<K><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, pass * kRadixBits,
                                                       s.hist + pass * kRadix,
                                                       s.lookback + (size_t)pass * (p.tiles + 1) * kRadix,

@@ -293,6 +293,7 @@ void launch_winding_emit(const WindArgs& a, uint64_t* tile_status, uint32_t* til
     int64_t tiles = (a.n + kTile - 1) / kTile;
     uint64_t* sA = tile_status;
     uint64_t* sB = tile_status + (tiles + 1);
+    count_launches(1);
     k_winding_emit<<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
 }
 
