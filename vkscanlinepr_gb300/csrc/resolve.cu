@@ -28,99 +28,186 @@ __global__ void k_row_bounds(const uint32_t* __restrict__ srows, int64_t n, int3
     }
 }
 
-// Integer source-over of one RGBA8 pixel, two channels per 32-bit lane:
-// c' = (s*a + d*(255-a) + 127) / 255 for R, G, B and, with s = 255, for A.
-// x/255 for 0 <= x <= 65152 is (x + 1 + (x >> 8)) >> 8 (checked exhaustively
-// by the CPU tests).
-struct BlendSrc {
-    uint32_t ia;       // 255 - a
-    uint32_t pre_rb;   // s_r*a + 127 | (s_b*a + 127) << 16
-    uint32_t pre_ga;   // s_g*a + 127 | (255*a + 127) << 16
+// ----------------------------------------------------------- pixel mode --
+// Source-over in path order over opaque white: for R, G, B
+//   c' = floor((s*a + c*(255-a) + 127) / 255) = round((s*a + c*(255-a)) / 255),
+// computed on the FMA pipe: u = c*ia + s*a is an exact float (<= 65025),
+// and fma(u, 1/255, 1.5*2^23) - 1.5*2^23 rounds u/255 to the nearest
+// integer exactly for every reachable u (checked exhaustively by the CPU
+// tests).  Alpha stays 255: (255*a + 255*(255-a) + 127) / 255 = 255.
+constexpr float kRound = 12582912.0f;   // 1.5 * 2^23
+constexpr int kK = 8;                   // pixels per lane; a warp owns 32*kK
+constexpr int kSeg = 32 * kK;
+constexpr int kChunk = 512;
+
+struct PixRec {
+    int32_t x0, x1;     // [x0, x1) clipped to >= 0
+    float ia;           // 255 - a
+    float sr, sg, sb;   // s*a per channel
 };
 
-SR_DEV BlendSrc blend_src(uint32_t c) {
-    uint32_t a = c >> 24;
-    BlendSrc b;
-    b.ia = 255u - a;
-    b.pre_rb = (c & 0x00FF00FFu) * a + 0x007F007Fu;
-    b.pre_ga = (((c >> 8) & 0xFFu) | (255u << 16)) * a + 0x007F007Fu;
-    return b;
+SR_DEV void blend3(float& r, float& g, float& b, const PixRec& q) {
+    const float inv = 1.0f / 255.0f;
+    float ur = __fmaf_rn(r, q.ia, q.sr), ug = __fmaf_rn(g, q.ia, q.sg), ub = __fmaf_rn(b, q.ia, q.sb);
+    r = __fsub_rn(__fmaf_rn(ur, inv, kRound), kRound);
+    g = __fsub_rn(__fmaf_rn(ug, inv, kRound), kRound);
+    b = __fsub_rn(__fmaf_rn(ub, inv, kRound), kRound);
 }
 
-SR_DEV uint32_t blend_px(uint32_t d, const BlendSrc& s) {
-    uint32_t rb = (d & 0x00FF00FFu) * s.ia + s.pre_rb;
-    uint32_t ga = ((d >> 8) & 0x00FF00FFu) * s.ia + s.pre_ga;
-    rb = ((rb + 0x00010001u + ((rb >> 8) & 0x00FF00FFu)) >> 8) & 0x00FF00FFu;
-    ga = ((ga + 0x00010001u + ((ga >> 8) & 0x00FF00FFu)) >> 8) & 0x00FF00FFu;
-    return rb | (ga << 8);
-}
-
-constexpr int kResolveThreads = 256;
-constexpr int kChunk = 256;
-
-__global__ void __launch_bounds__(kResolveThreads) k_resolve(const ResolveArgs a) {
-    extern __shared__ __align__(16) uint32_t rowbuf[];   // [F][W]
-    __shared__ int32_t s_x[kChunk], s_w[kChunk];
-    __shared__ uint32_t s_c[kChunk];
-    const int32_t r = blockIdx.x;
-    const int32_t W = a.W, F = a.F;
-    const int32_t y0 = r * F;
-    const int32_t nrows = imin(F, a.H - y0);
-    const int tid = threadIdx.x;
-    for (int32_t p = tid; p < nrows * W; p += kResolveThreads) rowbuf[p] = 0xFFFFFFFFu;
-    const int32_t beg = a.row_start[r], end = a.row_start[r + 1];
-    __syncthreads();
-    for (int32_t c0 = beg; c0 < end; c0 += kChunk) {
-        if (c0 + tid < end) {
-            int4 d = a.draw[a.row_sorted_idx[c0 + tid]];
-            s_x[tid] = d.x & 0xFFFF;
-            s_w[tid] = d.y;
-            s_c[tid] = (uint32_t)d.z;
-        }
-        __syncthreads();
-        const int32_t cnt = imin(kChunk, end - c0);
-        for (int32_t q = 0; q < cnt; ++q) {
-            int32_t xa = imax(s_x[q], 0);
-            int32_t xb = imin(wadd(s_x[q], s_w[q]), W);
-            uint32_t col = s_c[q];
-            int32_t p0 = xa + ((tid - xa) & (kResolveThreads - 1));
-            if (p0 >= xb) continue;
-            if (a.pixel_mode) {
-                BlendSrc bs = blend_src(col);
-                for (int32_t p = p0; p < xb; p += kResolveThreads) {
-                    for (int32_t rr = 0; rr < nrows; ++rr) {
-                        uint32_t* px = &rowbuf[rr * W + p];
-                        *px = blend_px(*px, bs);
+__global__ void __launch_bounds__(512) k_resolve_pixel(const ResolveArgs a) {
+    __shared__ PixRec sq[kChunk];
+    const int32_t row = blockIdx.x;
+    const int32_t W = a.W;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const int32_t beg = a.row_start[row], end = a.row_start[row + 1];
+    uint32_t* out = a.image + (size_t)row * W;
+    for (int32_t group = 0; group < W; group += nw * kSeg) {
+        const int32_t seg = group + warp * kSeg;
+        float r[kK], g[kK], b[kK];
+#pragma unroll
+        for (int j = 0; j < kK; ++j) r[j] = g[j] = b[j] = 255.0f;
+        for (int32_t c0 = beg; c0 < end; c0 += kChunk) {
+            const int32_t cnt = imin(kChunk, end - c0);
+            __syncthreads();
+            for (int q = tid; q < cnt; q += blockDim.x) {
+                int4 d = a.draw[a.row_sorted_idx[c0 + q]];
+                PixRec pr;
+                int32_t x = d.x & 0xFFFF;
+                pr.x0 = x;
+                pr.x1 = wadd(x, d.y);
+                uint32_t col = (uint32_t)d.z, al = col >> 24;
+                pr.ia = (float)(255u - al);
+                pr.sr = (float)((col & 0xFFu) * al);
+                pr.sg = (float)(((col >> 8) & 0xFFu) * al);
+                pr.sb = (float)(((col >> 16) & 0xFFu) * al);
+                sq[q] = pr;
+            }
+            __syncthreads();
+            if (seg >= W) continue;
+            for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
+                const int32_t qi = g0 + lane;
+                bool ov = false;
+                if (qi < cnt) ov = sq[qi].x0 < seg + kSeg && sq[qi].x1 > seg;
+                uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
+                while (m) {
+                    const int q = g0 + __ffs(m) - 1;
+                    m &= m - 1;
+                    const PixRec pr = sq[q];
+                    if (pr.x1 - pr.x0 == 1) {
+                        // one pixel: a uniform branch on its register slot
+                        const int32_t off = pr.x0 - seg;
+                        const int j = off >> 5;
+                        if (lane == (off & 31)) {
+                            switch (j) {
+                                case 0: blend3(r[0], g[0], b[0], pr); break;
+                                case 1: blend3(r[1], g[1], b[1], pr); break;
+                                case 2: blend3(r[2], g[2], b[2], pr); break;
+                                case 3: blend3(r[3], g[3], b[3], pr); break;
+                                case 4: blend3(r[4], g[4], b[4], pr); break;
+                                case 5: blend3(r[5], g[5], b[5], pr); break;
+                                case 6: blend3(r[6], g[6], b[6], pr); break;
+                                default: blend3(r[7], g[7], b[7], pr); break;
+                            }
+                        }
+                    } else if (pr.x0 <= seg && pr.x1 >= seg + kSeg) {
+#pragma unroll
+                        for (int j = 0; j < kK; ++j) blend3(r[j], g[j], b[j], pr);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < kK; ++j) {
+                            int32_t p = seg + lane + 32 * j;
+                            if (p >= pr.x0 && p < pr.x1) blend3(r[j], g[j], b[j], pr);
+                        }
                     }
                 }
-            } else {
-                for (int32_t p = p0; p < xb; p += kResolveThreads)
-                    for (int32_t rr = 0; rr < nrows; ++rr) rowbuf[rr * W + p] = col;
             }
         }
-        __syncthreads();
+        if (seg < W) {
+#pragma unroll
+            for (int j = 0; j < kK; ++j) {
+                int32_t p = seg + lane + 32 * j;
+                if (p < W) {
+                    uint32_t v = (uint32_t)__float2int_rn(r[j]) | ((uint32_t)__float2int_rn(g[j]) << 8) |
+                                 ((uint32_t)__float2int_rn(b[j]) << 16) | 0xFF000000u;
+                    out[p] = v;
+                }
+            }
+        }
     }
-    uint32_t* out = a.image + (size_t)y0 * W;
-    if ((W & 3) == 0) {
-        const uint4* src = reinterpret_cast<const uint4*>(rowbuf);
-        uint4* dst = reinterpret_cast<uint4*>(out);
-        for (int32_t p = tid; p < nrows * W / 4; p += kResolveThreads) dst[p] = src[p];
-    } else {
-        for (int32_t p = tid; p < nrows * W; p += kResolveThreads) out[p] = rowbuf[p];
+}
+
+// ------------------------------------------------------- reference mode --
+// Overwrite in draw order (blending off), 2-pixel cell rows: each lane
+// keeps kK pixels of both rows of its warp's segment.
+struct RefRec {
+    int32_t x0, x1;
+    uint32_t col;
+};
+
+__global__ void __launch_bounds__(512) k_resolve_ref(const ResolveArgs a) {
+    __shared__ RefRec sq[kChunk];
+    const int32_t cell = blockIdx.x;
+    const int32_t W = a.W;
+    const int32_t y0 = cell * a.F;
+    const int32_t nrows = imin(a.F, a.H - y0);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    const int32_t beg = a.row_start[cell], end = a.row_start[cell + 1];
+    for (int32_t group = 0; group < W; group += nw * kSeg) {
+        const int32_t seg = group + warp * kSeg;
+        uint32_t px[kK];
+#pragma unroll
+        for (int j = 0; j < kK; ++j) px[j] = 0xFFFFFFFFu;
+        for (int32_t c0 = beg; c0 < end; c0 += kChunk) {
+            const int32_t cnt = imin(kChunk, end - c0);
+            __syncthreads();
+            for (int q = tid; q < cnt; q += blockDim.x) {
+                int4 d = a.draw[a.row_sorted_idx[c0 + q]];
+                RefRec rr;
+                rr.x0 = d.x & 0xFFFF;
+                rr.x1 = wadd(rr.x0, d.y);
+                rr.col = (uint32_t)d.z;
+                sq[q] = rr;
+            }
+            __syncthreads();
+            if (seg >= W) continue;
+            for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
+                const int32_t qi = g0 + lane;
+                bool ov = false;
+                if (qi < cnt) ov = sq[qi].x0 < seg + kSeg && sq[qi].x1 > seg;
+                uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
+                while (m) {
+                    const int q = g0 + __ffs(m) - 1;
+                    m &= m - 1;
+                    const RefRec rr = sq[q];
+#pragma unroll
+                    for (int j = 0; j < kK; ++j) {
+                        int32_t p = seg + lane + 32 * j;
+                        if (p >= rr.x0 && p < rr.x1) px[j] = rr.col;
+                    }
+                }
+            }
+        }
+        if (seg < W) {
+            for (int32_t rr = 0; rr < nrows; ++rr) {
+                uint32_t* out = a.image + (size_t)(y0 + rr) * W;
+#pragma unroll
+                for (int j = 0; j < kK; ++j) {
+                    int32_t p = seg + lane + 32 * j;
+                    if (p < W) out[p] = px[j];
+                }
+            }
+        }
     }
 }
 
 void launch_resolve(const ResolveArgs& a, cudaStream_t st) {
     int32_t rows = (a.H + a.F - 1) / a.F;
     if (rows <= 0) return;
-    size_t smem = (size_t)a.F * a.W * sizeof(uint32_t);
-    static size_t attr = 0;
-    if (smem > 48 * 1024 && smem > attr) {
-        cudaFuncSetAttribute(k_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = smem;
-    }
+    int warps = (a.W + kSeg - 1) / kSeg;
+    if (warps > 16) warps = 16;
     count_launches(1);
-    k_resolve<<<rows, kResolveThreads, smem, st>>>(a);
+    if (a.pixel_mode) k_resolve_pixel<<<rows, 32 * warps, 0, st>>>(a);
+    else k_resolve_ref<<<rows, 32 * warps, 0, st>>>(a);
 }
 
 void launch_row_bounds(const uint32_t* srows, int64_t n, int32_t rows, int32_t* row_start, cudaStream_t st) {
