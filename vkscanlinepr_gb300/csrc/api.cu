@@ -83,6 +83,7 @@ enum Ctl : int {
     CTL_SCAN_COUNTER = 1,
     CTL_WIND_COUNTER = 2,
     CTL_BUCKETS = 4,   // 4 chain-bucket counters
+    CTL_LONG = 8,      // long-piece counter
     CTL_WORDS = 16,
 };
 
@@ -110,7 +111,7 @@ struct sr_ctx {
     uint32_t V = 0, C = 0, P = 0;
     DevBuf pos, pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info;
     // frame
-    DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, cbuf, rec;
+    DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, long_list, cbuf, rec;
     int sm_count = 148;
     DevBuf keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status;
     DevBuf draw, draw_row, totals;
@@ -137,6 +138,7 @@ struct sr_ctx {
     ~sr_ctx() {
         DevBuf* all[] = {&pos, &pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info,
                          &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status, &pieces, &chain_lists,
+                         &long_list,
                          &cbuf, &rec, &keys, &keys_alt,
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row,
                          &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start,
@@ -183,6 +185,7 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     CUDA_TRY(ensure(c->pieces, piece_table_bytes(std::max<uint32_t>(C, 1))));
     const uint32_t list_cap = chain_list_capacity(std::max<uint32_t>(C, 1));
     CUDA_TRY(ensure(c->chain_lists, sizeof(uint32_t) * 4 * (size_t)list_cap));
+    CUDA_TRY(ensure(c->long_list, sizeof(uint32_t) * (size_t)list_cap));
     uint32_t* ctl = c->ctl.as<uint32_t>();
     uint32_t* status = ctl + CTL_STATUS;
 
@@ -215,6 +218,8 @@ static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
     cw.chain_lists = c->chain_lists.as<uint32_t>();
     cw.list_cap = list_cap;
     cw.bucket_count = ctl + CTL_BUCKETS;
+    cw.long_list = c->long_list.as<uint32_t>();
+    cw.long_count = ctl + CTL_LONG;
     c->mark(ST_COUNT, false);
     launch_count(g, c->cut.as<float>(), c->count.as<int32_t>(), cw, status, st);
     c->mark(ST_COUNT, true);

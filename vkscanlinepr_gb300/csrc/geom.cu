@@ -121,6 +121,8 @@ SR_DEV int32_t cut_range(int32_t size, int32_t F, int32_t& b, int32_t& e) {
 
 // Pieces of a curve: at most 4 monotonic cuts + the end at t = 1.
 constexpr int kMaxPieces = 5;
+// Pieces with at least this many records are merged by a whole CTA.
+constexpr int32_t kLongPiece = 64;
 
 // Piece record layout in the output: [t0][x crossings][y crossings], the
 // crossing values of each side solved by one chain (k_chains), then merged
@@ -165,12 +167,14 @@ SR_DEV int32_t axis_range_rd(float a0, float a1, int32_t size, int32_t F, float&
 __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restrict__ cut_cache,
                                                int32_t* __restrict__ count, uint4* __restrict__ pieces,
                                                uint32_t* __restrict__ chain_lists, uint32_t list_cap,
-                                               uint32_t* __restrict__ bucket_count, uint32_t* __restrict__ status) {
+                                               uint32_t* __restrict__ bucket_count, uint32_t* __restrict__ long_list,
+                                               uint32_t* __restrict__ long_count, uint32_t* __restrict__ status) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = c < g.n_curves;
     uint32_t my_chains[2 * kMaxPieces];
     uint32_t my_bucket[2 * kMaxPieces];
     int n_chains = 0;
+    uint32_t long_mask = 0;   // pieces merged by k_merge_long
     if (active) {
         uint32_t type = g.curve_type[c];
         CurvePts P;
@@ -281,14 +285,30 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
                 my_bucket[n_chains++] = chain_bucket(ny);
             }
             walk += 1 + nx + ny;
+            if (1 + nx + ny >= kLongPiece) long_mask |= 1u << i;
             x0 = x1;
             y0 = y1;
         }
         count[c] = pc;
         if (walk != pc) set_error(status, ERR_RECORD_RANGE);
     }
-    // append chains to their buckets (warp-aggregated per bucket)
+    // append long pieces (warp-aggregated)
     const uint32_t lane = lane_id();
+    for (int i = 0; i < kMaxPieces; ++i) {
+        bool has = (long_mask >> i) & 1u;
+        uint32_t m = __ballot_sync(0xFFFFFFFFu, has);
+        if (!m) continue;
+        uint32_t leader = (uint32_t)(__ffs(m) - 1);
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(long_count, (uint32_t)__popc(m));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (has) {
+            uint32_t slot = base + (uint32_t)__popc(m & lanemask_lt());
+            if (slot < list_cap) long_list[slot] = (c << 3) | (uint32_t)i;
+            else set_error(status, ERR_CAPACITY);
+        }
+    }
+    // append chains to their buckets (warp-aggregated per bucket)
     for (int k = 0; k < 2 * kMaxPieces; ++k) {
         bool has = k < n_chains;
         if (!__any_sync(0xFFFFFFFFu, has)) break;
@@ -327,9 +347,10 @@ template <int kType> SR_DEV float eval_axis(const AxisPoly& a, float t) {
     return __fadd_rn(l0, __fmul_rn(t, __fsub_rn(l1, l0)));
 }
 
-SR_DEV bool same_sign(float a, float c, float b) {
-    return (fbits(__fsub_rn(a, c)) ^ fbits(__fsub_rn(b, c))) >= 0;
-}
+// (bits(a - c) ^ bits(b - c)) >= 0 of make_intersection_1.comp:421: for
+// finite values a - c is negative exactly when a < c (x - x is +0), so the
+// test is a pair of compares.
+SR_DEV bool same_sign(float a, float c, float b) { return (a < c) == (b < c); }
 
 // 24-step bisection of the reference (make_intersection_1.comp:402-434).
 // kSpec evaluates both possible next midpoints with the current one, so
@@ -494,6 +515,11 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
             set_error(status, ERR_RECORD_RANGE);
             return;
         }
+        if (n_loop >= kLongPiece) {   // k_merge_long
+            pc += n_loop;
+            t0 = (int32_t)me.y;
+            continue;
+        }
         int32_t last = minus_one;
         for (int32_t k = 0; k < n_loop; ++k) {
             int32_t av = ex_x, bv = ex_y;
@@ -518,6 +544,92 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
         t0 = (int32_t)me.y;
     }
     if (pc != end) set_error(status, ERR_RECORD_RANGE);
+}
+
+// Merge of one long piece by a CTA.  The chains are non-decreasing (each
+// root is solved from the previous one, flag bits included); only the
+// piece start t0 may exceed the first roots by less than 4 ulp, so the
+// sequential merge is: the x roots <= t0, then t0, then the stable merge
+// (x first on ties) of the remaining x roots with the y roots.  Each
+// element's slot is its index plus a binary-search rank in the other
+// chain.  The flag-OR of equal t values is then applied per element:
+// record k of a run [s, e] of equal masked t ends as OR(v_s .. v_min(k+1,e)).
+SR_DEV int32_t count_le(const int32_t* a, int32_t n, float v) {   // elements <= v
+    int32_t lo = 0, hi = n;
+    while (lo < hi) {
+        int32_t mid = (lo + hi) >> 1;
+        if (bitsf(a[mid]) <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+SR_DEV int32_t count_lt(const int32_t* a, int32_t n, float v) {   // elements < v
+    int32_t lo = 0, hi = n;
+    while (lo < hi) {
+        int32_t mid = (lo + hi) >> 1;
+        if (bitsf(a[mid]) < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_merge_long(const GeomArgs g, const int32_t* __restrict__ offs,
+                                                    const uint4* __restrict__ pieces,
+                                                    const uint32_t* __restrict__ long_list, uint32_t list_cap,
+                                                    const uint32_t* __restrict__ long_count,
+                                                    int32_t* __restrict__ cbuf, int2* __restrict__ rec) {
+    __shared__ int32_t s_i0;
+    const uint32_t n_long = imin((int32_t)*long_count, (int32_t)list_cap);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (uint32_t item = blockIdx.x; item < n_long; item += gridDim.x) {
+        const uint32_t c = long_list[item] >> 3, piece = long_list[item] & 7u;
+        const uint4* pt = pieces + (size_t)c * kMaxPieces;
+        int64_t base = offs[c];
+        for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
+        const int32_t nx = piece_nx(pt[piece].x), ny = piece_ny(pt[piece].x);
+        const int32_t L = 1 + nx + ny;
+        const int32_t t0 = piece == 0 ? 0 : (int32_t)pt[piece - 1].y;
+        const int32_t* X = cbuf + base + 1;
+        const int32_t* Y = X + nx;
+        int2* R = rec + base;
+        if (nx == 0 || ny == 0) {
+            const int32_t* S = nx == 0 ? Y : X;
+            for (int32_t k = tid; k < L; k += nt) R[k] = make_int2((int32_t)c, k == 0 ? t0 : S[k - 1]);
+        } else {
+            if (tid == 0) s_i0 = count_le(X, nx, bitsf(t0));
+            __syncthreads();
+            const int32_t i0 = s_i0;
+            for (int32_t i = tid; i < nx; i += nt) {
+                int32_t v = X[i];
+                int32_t pos = i < i0 ? i : i0 + 1 + (i - i0) + count_lt(Y, ny, bitsf(v));
+                R[pos] = make_int2((int32_t)c, v);
+            }
+            if (tid == 0) R[i0] = make_int2((int32_t)c, t0);
+            for (int32_t j = tid; j < ny; j += nt) {
+                int32_t v = Y[j];
+                int32_t pos = i0 + 1 + j + count_le(X + i0, nx - i0, bitsf(v));
+                R[pos] = make_int2((int32_t)c, v);
+            }
+        }
+        __syncthreads();
+        int32_t* T = cbuf + base;   // the chains are consumed: reuse as scratch
+        for (int32_t k = tid; k < L; k += nt) {
+            int32_t v = R[k].y, acc = v;
+            for (int32_t s = k - 1; s >= 0; --s) {
+                int32_t u = R[s].y;
+                if ((u & ~3) != (v & ~3)) break;
+                acc |= u;
+            }
+            if (k + 1 < L) {
+                int32_t u = R[k + 1].y;
+                if ((u & ~3) == (v & ~3)) acc |= u;
+            }
+            T[k] = acc;
+        }
+        __syncthreads();
+        for (int32_t k = tid; k < L; k += nt) R[k].y = T[k];
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------- fragment -----
@@ -585,6 +697,17 @@ void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_po
     k_transform<<<(n_points + 255) / 256, 256, 0, st>>>(pos, pos_path, n_points, M, fw, fh, tpos, path_visible);
 }
 
+static int sm_count_hint() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n * 8;
+}
+
 size_t piece_table_bytes(uint32_t n_curves) { return sizeof(uint4) * kMaxPieces * (size_t)n_curves; }
 uint32_t chain_list_capacity(uint32_t n_curves) { return 2u * kMaxPieces * n_curves; }
 
@@ -593,7 +716,7 @@ void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const Cha
     if (g.n_curves == 0) return;
     count_launches(1);
     k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count, w.pieces, w.chain_lists, w.list_cap,
-                                                      w.bucket_count, status);
+                                                      w.bucket_count, w.long_list, w.long_count, status);
 }
 
 void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
@@ -603,11 +726,13 @@ void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, i
     k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.chain_lists, w.list_cap, w.bucket_count, cbuf);
 }
 
-void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, const int32_t* cbuf, int2* rec,
+void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
                   uint32_t* status, cudaStream_t st) {
     if (g.n_curves == 0) return;
-    count_launches(1);
+    count_launches(2);
     k_merge<<<(g.n_curves + 127) / 128, 128, 0, st>>>(g, offs, w.pieces, cbuf, rec, status);
+    k_merge_long<<<sm_count_hint(), 256, 0, st>>>(g, offs, w.pieces, w.long_list, w.list_cap, w.long_count,
+                                                  cbuf, rec);
 }
 
 void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n, uint64_t* keys, uint8_t* wnp,

@@ -43,6 +43,8 @@ struct ChainWork {
     uint32_t* chain_lists;    // [4][list_cap] chain ids by length bucket
     uint32_t list_cap;
     uint32_t* bucket_count;   // [4] zeroed before the count pass
+    uint32_t* long_list;      // [list_cap] (curve << 3 | piece) of long pieces
+    uint32_t* long_count;     // [1] zeroed before the count pass
 };
 size_t piece_table_bytes(uint32_t n_curves);
 uint32_t chain_list_capacity(uint32_t n_curves);
@@ -55,7 +57,7 @@ void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const Cha
 // reference's intersection records rec[N] (curve, t bits | flags).
 void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
                    cudaStream_t st);
-void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, const int32_t* cbuf, int2* rec,
+void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
                   uint32_t* status, cudaStream_t st);
 // One fragment per record: sort key + packed winding bits.
 void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n, uint64_t* keys, uint8_t* wnp,
