@@ -128,6 +128,16 @@ sr_status sr_set_mvp(sr_ctx* ctx, const float m[16]);
  * into the context's own device framebuffer only. */
 sr_status sr_render(sr_ctx* ctx, void* rgba_out, int out_is_device, void* stream);
 
+/* Paints a caller-given draw list: n records of 4 int32 (packed yx, width,
+ * RGBA8 colour, fragment index) in host memory, as produced by the emit
+ * stage (gen_merged_fragment_and_span.comp:170,195).  This is the
+ * reference's MOCK_DATA path (scanline_rasterizer.cpp:251-281, :808-818),
+ * which skips the compute passes and draws a draw list read from a CSV.
+ * Output as for sr_render; records whose row lies outside the canvas are
+ * skipped. */
+sr_status sr_render_draw_list(sr_ctx* ctx, const int32_t* records, int64_t n, void* rgba_out, int out_is_device,
+                              void* stream);
+
 /* Per-frame counters of the last sr_render. */
 typedef struct sr_stats {
     uint64_t n_intersections;  /* N: intersection records (n_fragments)  */
@@ -173,6 +183,15 @@ sr_status sr_debug_dump(sr_ctx* ctx, int stage, void* dst, size_t* bytes);
 
 /* Replaces the destructor of ScanlineVGRasterizer. */
 void sr_destroy(sr_ctx* ctx);
+
+/* Exclusive scan of n int32 values in device memory: d_out[0..n] with
+ * d_out[n] = the total (n+1 outputs; d_in and d_out may be the same
+ * buffer), wrapping on overflow.  Replaces the reference's standalone scan
+ * kernel workdir/shaders/common/naive_scan.comp:27-73 (one workgroup,
+ * 1023-element batches) with a single-pass decoupled look-back scan.
+ * Asynchronous on `stream`; its look-back scratch comes from
+ * cudaMallocAsync/cudaFreeAsync on the same stream.  0 <= n < 2^31. */
+sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* sr_last_error(void);

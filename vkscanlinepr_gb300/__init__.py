@@ -84,7 +84,7 @@ class SynthParams(ctypes.Structure):
 # every symbol include/sr.h declares
 EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stats", "sr_debug_dump",
            "sr_destroy", "sr_last_error", "sr_synth_scene", "sr_rvg_load", "sr_scene_buf_view",
-           "sr_scene_buf_free"]
+           "sr_scene_buf_free", "sr_exclusive_scan_i32", "sr_render_draw_list"]
 
 _lib = None
 
@@ -123,6 +123,8 @@ def lib():
     L.sr_host_alloc.restype = vp
     L.sr_host_free.argtypes = [vp]
     L.sr_host_free.restype = None
+    L.sr_exclusive_scan_i32.argtypes = [vp, vp, ctypes.c_int64, vp]
+    L.sr_render_draw_list.argtypes = [vp, vp, ctypes.c_int64, vp, ctypes.c_int, vp]
     _lib = L
     return L
 
@@ -264,6 +266,11 @@ def load_rvg(path):
         L.sr_scene_buf_free(h)
 
 
+def exclusive_scan_i32(d_in, d_out, n, stream=None):
+    """Exclusive scan of n int32 at device address d_in into d_out[0..n]."""
+    _check(lib().sr_exclusive_scan_i32(d_in, d_out, int(n), stream))
+
+
 class PinnedBuffer:
     """Page-locked host buffer (cudaMallocHost) viewed as a numpy array."""
 
@@ -319,6 +326,15 @@ class ScanlineVGRasterizer:
             out = np.empty((self.height, self.width, 4), np.uint8)
         ptr = out.ctypes.data if isinstance(out, np.ndarray) else out
         _check(lib().sr_render(self._ctx, ptr, 0, stream))
+        return out
+
+    def render_draw_list(self, records, out=None, stream=None):
+        """Paints an (n, 4) int32 draw list (the reference's MOCK_DATA path)."""
+        rec = np.ascontiguousarray(records, np.int32).reshape(-1, 4)
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.uint8)
+        _check(lib().sr_render_draw_list(self._ctx, rec.ctypes.data if rec.size else None, rec.shape[0],
+                                         out.ctypes.data, 0, stream))
         return out
 
     def render_device(self, dev_ptr=None, stream=None):

@@ -491,6 +491,62 @@ sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) 
     return SR_OK;
 }
 
+sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void* rgba_out, int out_is_device,
+                              void* stream) {
+    if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
+    if (n < 0 || n >= (1ll << 30) || (n > 0 && !records)) return fail(SR_ERR_INVALID_ARG, "bad draw list");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaSetDevice(c->device));
+    const int32_t rows = (c->H + c->F - 1) / c->F;
+    const size_t n1 = (size_t)std::max<int64_t>(n, 1);
+    std::vector<uint32_t> row((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t y = records[4 * i] >> 16;
+        row[(size_t)i] = (y < 0 || y >= c->H) ? (uint32_t)rows : (uint32_t)(y / c->F);
+    }
+    CUDA_TRY(ensure(c->draw, sizeof(int4) * n1));
+    CUDA_TRY(ensure(c->draw_row, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(c->ctl, sizeof(uint32_t) * CTL_WORDS));
+    CUDA_TRY(ensure(c->rkeys, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(c->rvals, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(c->rkeys_alt, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(c->rvals_alt, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(c->row_start, sizeof(int32_t) * ((size_t)rows + 1)));
+    CUDA_TRY(cudaMemsetAsync(c->ctl.p, 0, sizeof(uint32_t) * CTL_WORDS, st));
+    if (n) {
+        CUDA_TRY(cudaMemcpyAsync(c->draw.p, records, sizeof(int4) * (size_t)n, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(c->draw_row.p, row.data(), sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+    }
+    sr::SortPlan rp = sr::sort_plan(n, bits_for((uint64_t)rows));
+    CUDA_TRY(ensure(c->row_sort_scratch, sr::sort_scratch_bytes(rp)));
+    uint32_t* status = c->ctl.as<uint32_t>() + CTL_STATUS;
+    sr::launch_sort_u32(rp, c->draw_row.as<uint32_t>(), nullptr, c->rkeys.as<uint32_t>(), c->rvals.as<uint32_t>(),
+                        c->rkeys_alt.as<uint32_t>(), c->rvals_alt.as<uint32_t>(), c->row_sort_scratch.p, status, st);
+    sr::launch_row_bounds(c->rkeys.as<uint32_t>(), n, rows, c->row_start.as<int32_t>(), st);
+    sr::ResolveArgs ra;
+    ra.draw = c->draw.as<int4>();
+    ra.row_sorted_idx = c->rvals.as<uint32_t>();
+    ra.row_start = c->row_start.as<int32_t>();
+    ra.W = c->W;
+    ra.H = c->H;
+    ra.F = c->F;
+    ra.pixel_mode = c->mode == SR_MODE_PIXEL;
+    ra.image = c->image.as<uint32_t>();
+    sr::launch_resolve(ra, st);
+    CUDA_TRY(cudaGetLastError());
+    c->last_O = n;
+    if (rgba_out) {
+        CUDA_TRY(cudaMemcpyAsync(rgba_out, c->image.p, (size_t)c->W * c->H * 4,
+                                 out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    }
+    if (!out_is_device || !rgba_out) {
+        CUDA_TRY(cudaMemcpyAsync(&c->h_n[1], status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return check_status_word((uint32_t)c->h_n[1]);
+    }
+    return SR_OK;
+}
+
 sr_status sr_get_stats(const sr_ctx* cc, sr_stats* out) {
     if (!cc || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     sr_ctx* c = const_cast<sr_ctx*>(cc);
@@ -543,6 +599,31 @@ sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
     CUDA_TRY(cudaSetDevice(c->device));
     if (need) CUDA_TRY(cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost));
     *bytes = need;
+    return SR_OK;
+}
+
+sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream) {
+    if (n < 0 || n >= (1ll << 31)) return fail(SR_ERR_INVALID_ARG, "scan length %lld out of range", (long long)n);
+    if (!d_out || (n > 0 && !d_in)) return fail(SR_ERR_INVALID_ARG, "NULL device pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(int32_t), st));
+        return SR_OK;
+    }
+    // tile words, then the tile counter and the status word
+    const size_t words = sr::scan_status_words(n) + 2;
+    void* scratch = nullptr;
+    CUDA_TRY(cudaMallocAsync(&scratch, words * sizeof(uint64_t), st));
+    uint64_t* tiles = static_cast<uint64_t*>(scratch);
+    uint32_t* tail = reinterpret_cast<uint32_t*>(tiles + words - 2);
+    cudaError_t e = cudaMemsetAsync(scratch, 0, words * sizeof(uint64_t), st);
+    if (e == cudaSuccess) {
+        sr::launch_exclusive_scan_i32(d_in, d_out, n, tiles, tail, tail + 1, st);
+        e = cudaGetLastError();
+    }
+    cudaError_t f = cudaFreeAsync(scratch, st);
+    CUDA_TRY(e);
+    CUDA_TRY(f);
     return SR_OK;
 }
 
