@@ -225,7 +225,14 @@ sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]);
 
 /* Points `view` at the arrays of `buf` (valid until sr_scene_buf_free). */
 sr_status sr_scene_buf_view(const sr_scene_buf* buf, sr_scene_view* view);
+/* Canvas size the scene was made for: wh[0] = width, wh[1] = height. */
+sr_status sr_scene_buf_size(const sr_scene_buf* buf, uint32_t wh[2]);
 void sr_scene_buf_free(sr_scene_buf* buf);
+
+/* Page-locked host memory (cudaMallocHost) for full-bandwidth copies of
+ * scenes and frames; NULL on failure. */
+void* sr_host_alloc(size_t bytes);
+void sr_host_free(void* p);
 
 #ifdef __cplusplus
 }
