@@ -193,6 +193,27 @@ void sr_destroy(sr_ctx* ctx);
  * cudaMallocAsync/cudaFreeAsync on the same stream.  0 <= n < 2^31. */
 sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
 
+/* The same scan for callers that cannot allocate device memory: a host that
+ * gives all device memory to its own allocator or runs under a hard memory
+ * budget forbids third-party allocations, and a frame loop with a fixed
+ * latency budget cannot risk an allocation call that may wait on the device.
+ * This entry point calls no cudaMalloc, cudaFree or other allocating routine.
+ * It has no counterpart in the reference.
+ *
+ * Its look-back scratch is a fixed array of SR_NOALLOC_SCAN_SCRATCH_BYTES
+ * compiled into the library: every GPU that loads the library holds it until
+ * the process exits.  n is limited to SR_NOALLOC_SCAN_MAX_N; larger n is
+ * rejected with SR_ERR_INVALID_ARG.  The first call on a device looks up the
+ * array's device address (with that device current); make that first call
+ * before any stream capture.  Every call uses the same array and clears the
+ * part it needs, so calls that overlap on the GPU (on different streams, or
+ * from different threads) race: serialise them on one stream.  Inputs,
+ * outputs and results are as for sr_exclusive_scan_i32; asynchronous on
+ * `stream`. */
+#define SR_NOALLOC_SCAN_MAX_N (1ll << 24)
+#define SR_NOALLOC_SCAN_SCRATCH_BYTES (4104u * 8u)
+sr_status sr_exclusive_scan_i32_noalloc(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* sr_last_error(void);
 

@@ -84,7 +84,8 @@ class SynthParams(ctypes.Structure):
 # every symbol include/sr.h declares
 EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stats", "sr_debug_dump",
            "sr_destroy", "sr_last_error", "sr_synth_scene", "sr_rvg_load", "sr_scene_buf_view",
-           "sr_scene_buf_free", "sr_exclusive_scan_i32", "sr_render_draw_list"]
+           "sr_scene_buf_free", "sr_exclusive_scan_i32", "sr_render_draw_list",
+           "sr_exclusive_scan_i32_noalloc"]
 
 _lib = None
 
@@ -125,6 +126,7 @@ def lib():
     L.sr_host_free.restype = None
     L.sr_exclusive_scan_i32.argtypes = [vp, vp, ctypes.c_int64, vp]
     L.sr_render_draw_list.argtypes = [vp, vp, ctypes.c_int64, vp, ctypes.c_int, vp]
+    L.sr_exclusive_scan_i32_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp]
     _lib = L
     return L
 
@@ -269,6 +271,16 @@ def load_rvg(path):
 def exclusive_scan_i32(d_in, d_out, n, stream=None):
     """Exclusive scan of n int32 at device address d_in into d_out[0..n]."""
     _check(lib().sr_exclusive_scan_i32(d_in, d_out, int(n), stream))
+
+
+NOALLOC_SCAN_MAX_N = 1 << 24
+
+
+def exclusive_scan_i32_noalloc(d_in, d_out, n, stream=None):
+    """The exclusive scan for callers that cannot allocate device memory:
+    its scratch is a fixed array inside the library (n <= NOALLOC_SCAN_MAX_N;
+    calls that overlap on the GPU race)."""
+    _check(lib().sr_exclusive_scan_i32_noalloc(d_in, d_out, int(n), stream))
 
 
 class PinnedBuffer:

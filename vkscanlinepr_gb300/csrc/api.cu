@@ -92,6 +92,7 @@ std::atomic<uint64_t> g_launches{0};
 }  // namespace
 
 namespace sr {
+sr_status report_error(sr_status s, const char* msg) { return fail(s, "%s", msg); }
 void count_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace sr
