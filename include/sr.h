@@ -218,6 +218,56 @@ sr_status sr_exclusive_scan_i32_noalloc(const int32_t* d_in, int32_t* d_out, int
 const char* sr_last_error(void);
 
 /* ------------------------------------------------------------------ */
+/* Batches: many uneven scenes in one frame (no reference counterpart; */
+/* the reference renders one scene per VGRasterizer).                  */
+/* ------------------------------------------------------------------ */
+
+/* A set of scenes rendered together: their curves go through every stage
+ * in the same launches (one scene table gives each kernel its scene's
+ * canvas), so small scenes share the GPU instead of each paying the launch
+ * and read-back costs of a frame.  Each scene's image is bit-identical to
+ * the same scene rendered alone with sr_render. */
+typedef struct sr_batch sr_batch;
+
+typedef struct sr_synth_params sr_synth_params;
+
+typedef struct sr_batch_render_opts {
+    uint32_t struct_size;
+    uint32_t use_graph;          /* capture the frame as a CUDA graph and replay it
+                                    (needs record_capacity >= 0) */
+    int64_t  record_capacity;    /* < 0: size exactly (one host wait for the
+                                    record count, as the reference does);
+                                    >= 0: pre-sized, no mid-frame wait */
+    uint32_t refit_on_overflow;  /* on overflow, rerun with exact sizing */
+    uint32_t reserved;
+} sr_batch_render_opts;
+
+typedef struct sr_batch_stats {
+    sr_stats frame;              /* counters of the last frame (all scenes) */
+    uint32_t n_scenes, n_paths, n_curves;
+    uint32_t overflows;          /* pre-sized frames whose records did not fit */
+    uint32_t refits;             /* of those, rerun with exact sizing */
+    uint32_t graph_captured;
+    int64_t  record_capacity;    /* capacity of the last frame */
+} sr_batch_stats;
+
+sr_status sr_batch_create(const sr_options* opt, sr_batch** out);
+/* Appends a scene (copied; resident on the device after sr_batch_commit).
+ * mvp may be NULL (identity). */
+sr_status sr_batch_add_scene(sr_batch* b, uint32_t width, uint32_t height, const sr_scene_view* scene,
+                             const float* mvp, uint32_t* index);
+/* Appends `count` synthetic scenes, scene_index p->scene_index + i. */
+sr_status sr_batch_add_synth(sr_batch* b, const sr_synth_params* p, uint32_t count, uint32_t* first_index);
+sr_status sr_batch_commit(sr_batch* b);
+sr_status sr_batch_set_mvp(sr_batch* b, uint32_t index, const float m[16]);
+sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* opts, void* stream);
+sr_status sr_batch_get_image(sr_batch* b, uint32_t index, void* rgba_out, int out_is_device, void* stream);
+sr_status sr_batch_info(const sr_batch* b, uint32_t index, uint32_t* width, uint32_t* height);
+sr_status sr_batch_get_stats(const sr_batch* b, sr_batch_stats* out);
+sr_status sr_batch_clear(sr_batch* b);
+void sr_batch_destroy(sr_batch* b);
+
+/* ------------------------------------------------------------------ */
 /* Scene sources: synthetic generator and RVG loader (host only).      */
 /* ------------------------------------------------------------------ */
 
@@ -226,16 +276,18 @@ typedef struct sr_scene_buf sr_scene_buf;
 
 /* Synthetic scene parameters.  preset 0: closed star paths of cubics;
  * preset 1: mixed cubic/quadric/line paths with even-odd paths,
- * figure-eights and full-canvas backgrounds.  Fields left 0 take the
- * preset's default. */
-typedef struct sr_synth_params {
+ * figure-eights and full-canvas backgrounds; preset 2: scene `scene_index`
+ * of a batch of uneven scenes (square side uniform over 256..2048, path
+ * count lognormal with median 200, paths as preset 1).  Fields left 0 take
+ * the preset's default. */
+struct sr_synth_params {
     uint32_t struct_size;
     int32_t  preset;
     uint64_t seed;
     uint32_t scene_index;   /* independent stream per scene of a batch */
     uint32_t width, height;
     uint32_t n_paths;
-} sr_synth_params;
+};
 
 sr_status sr_synth_scene(const sr_synth_params* p, sr_scene_buf** out);
 

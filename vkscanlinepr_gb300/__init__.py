@@ -72,6 +72,12 @@ STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment
                "row_sort", "resolve"]
 
 
+class BatchRenderOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("use_graph", ctypes.c_uint32),
+                ("record_capacity", ctypes.c_int64), ("refit_on_overflow", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
 class SynthParams(ctypes.Structure):
     _fields_ = [
         ("struct_size", ctypes.c_uint32), ("preset", ctypes.c_int32),
@@ -81,11 +87,19 @@ class SynthParams(ctypes.Structure):
     ]
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = [("frame", Stats), ("n_scenes", ctypes.c_uint32), ("n_paths", ctypes.c_uint32),
+                ("n_curves", ctypes.c_uint32), ("overflows", ctypes.c_uint32), ("refits", ctypes.c_uint32),
+                ("graph_captured", ctypes.c_uint32), ("record_capacity", ctypes.c_int64)]
+
+
 # every symbol include/sr.h declares
 EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stats", "sr_debug_dump",
            "sr_destroy", "sr_last_error", "sr_synth_scene", "sr_rvg_load", "sr_scene_buf_view",
            "sr_scene_buf_free", "sr_exclusive_scan_i32", "sr_render_draw_list",
-           "sr_exclusive_scan_i32_noalloc"]
+           "sr_exclusive_scan_i32_noalloc", "sr_batch_create", "sr_batch_add_scene", "sr_batch_add_synth",
+           "sr_batch_commit", "sr_batch_set_mvp", "sr_batch_render", "sr_batch_get_image", "sr_batch_info",
+           "sr_batch_get_stats", "sr_batch_clear", "sr_batch_destroy"]
 
 _lib = None
 
@@ -127,6 +141,21 @@ def lib():
     L.sr_exclusive_scan_i32.argtypes = [vp, vp, ctypes.c_int64, vp]
     L.sr_render_draw_list.argtypes = [vp, vp, ctypes.c_int64, vp, ctypes.c_int, vp]
     L.sr_exclusive_scan_i32_noalloc.argtypes = [vp, vp, ctypes.c_int64, vp]
+    L.sr_batch_create.argtypes = [ctypes.POINTER(Options), ctypes.POINTER(vp)]
+    L.sr_batch_add_scene.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(SceneView), vp,
+                                     ctypes.POINTER(ctypes.c_uint32)]
+    L.sr_batch_add_synth.argtypes = [vp, ctypes.POINTER(SynthParams), ctypes.c_uint32,
+                                     ctypes.POINTER(ctypes.c_uint32)]
+    L.sr_batch_commit.argtypes = [vp]
+    L.sr_batch_set_mvp.argtypes = [vp, ctypes.c_uint32, vp]
+    L.sr_batch_render.argtypes = [vp, ctypes.POINTER(BatchRenderOpts), vp]
+    L.sr_batch_get_image.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_int, vp]
+    L.sr_batch_info.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
+                                ctypes.POINTER(ctypes.c_uint32)]
+    L.sr_batch_get_stats.argtypes = [vp, ctypes.POINTER(BatchStats)]
+    L.sr_batch_clear.argtypes = [vp]
+    L.sr_batch_destroy.argtypes = [vp]
+    L.sr_batch_destroy.restype = None
     _lib = L
     return L
 
@@ -382,6 +411,86 @@ class ScanlineVGRasterizer:
         if self._ctx:
             lib().sr_destroy(self._ctx)
             self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SceneBatch:
+    """Many uneven scenes rendered in the same launches (sr_batch_*).
+
+    Each scene's image is bit-identical to rendering it alone.  render() can
+    size the record buffers exactly (one host wait, as the reference does) or
+    take a record capacity and enqueue the whole frame without waiting
+    (optionally as a replayed CUDA graph); an overflow is detected on the
+    device and, with refit=True, the frame reruns with exact sizing."""
+
+    def __init__(self, mode=MODE_PIXEL, device=0, profile=False):
+        o = Options(ctypes.sizeof(Options), mode, device, FLAG_PROFILE if profile else 0)
+        h = ctypes.c_void_p()
+        _check(lib().sr_batch_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self.mode = mode
+        self._keep = []
+
+    def add_scene(self, container, width=None, height=None, mvp=None):
+        w = container.width if width is None else width
+        h = container.height if height is None else height
+        v = container.view()
+        m = None if mvp is None else np.ascontiguousarray(mvp, np.float32).reshape(16)
+        idx = ctypes.c_uint32()
+        _check(lib().sr_batch_add_scene(self._h, int(w), int(h), ctypes.byref(v),
+                                        m.ctypes.data if m is not None else None, ctypes.byref(idx)))
+        return idx.value
+
+    def add_synth(self, preset, seed, count, scene_index=0, width=0, height=0, n_paths=0):
+        p = SynthParams(ctypes.sizeof(SynthParams), preset, seed, scene_index, width, height, n_paths)
+        first = ctypes.c_uint32()
+        _check(lib().sr_batch_add_synth(self._h, ctypes.byref(p), int(count), ctypes.byref(first)))
+        return first.value
+
+    def commit(self):
+        _check(lib().sr_batch_commit(self._h))
+
+    def set_mvp(self, index, m):
+        a = np.ascontiguousarray(m, np.float32).reshape(16)
+        _check(lib().sr_batch_set_mvp(self._h, int(index), a.ctypes.data))
+
+    def render(self, capacity=-1, graph=False, refit=True, stream=None):
+        o = BatchRenderOpts(ctypes.sizeof(BatchRenderOpts), 1 if graph else 0, int(capacity), 1 if refit else 0, 0)
+        _check(lib().sr_batch_render(self._h, ctypes.byref(o), stream))
+
+    def size(self, index):
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(lib().sr_batch_info(self._h, int(index), ctypes.byref(w), ctypes.byref(h)))
+        return w.value, h.value
+
+    def image(self, index, out=None, stream=None):
+        w, h = self.size(index)
+        if out is None:
+            out = np.empty((h, w, 4), np.uint8)
+        _check(lib().sr_batch_get_image(self._h, int(index), out.ctypes.data, 0, stream))
+        return out
+
+    def stats(self):
+        s = BatchStats()
+        _check(lib().sr_batch_get_stats(self._h, ctypes.byref(s)))
+        f = s.frame
+        d = {k: getattr(s, k) for k, _ in BatchStats._fields_ if k != "frame"}
+        d.update({k: getattr(f, k) for k, _ in Stats._fields_ if k not in ("stage_ms", "reserved")})
+        d["stage_ms"] = dict(zip(STAGE_NAMES, [float(x) for x in f.stage_ms]))
+        return d
+
+    def clear(self):
+        _check(lib().sr_batch_clear(self._h))
+
+    def close(self):
+        if self._h:
+            lib().sr_batch_destroy(self._h)
+            self._h = None
 
     def __del__(self):
         try:

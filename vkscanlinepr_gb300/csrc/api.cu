@@ -1,21 +1,30 @@
-// api.cu — context, device memory and per-frame sequencing behind sr.h.
+// api.cu — device state, per-frame sequencing and the C ABI of sr.h.
 //
 // ScanlineVGRasterizer::drawFrame (scanline_rasterizer.cpp:282-696) submits
 // eleven compute dispatches with three blocking host read-backs, then draws
-// the list through the graphics queue.  Here one frame is:
-//   transform -> count -> offset scan -> [read N] -> intersect+fragment ->
-//   onesweep sort -> winding/mark/emit -> [read O] -> row sort -> resolve
-// on the caller's stream, with device buffers that only grow.
+// the list through the graphics queue.  Here a frame of a set of scenes is
+//   transform -> count -> chain order -> offset scan -> [read N] ->
+//   chains -> merge -> fragments -> sort -> winding/mark/emit ->
+//   row sort -> resolve
+// on the caller's stream.  The read of N is the only mid-frame host wait,
+// and only when the record buffers are sized exactly; with a given record
+// capacity (learned sizing, or the previous frame's count) the frame
+// enqueues without waiting, an overflow is detected on the device, and the
+// frame can be captured as a CUDA graph.  A single-scene context is a
+// one-scene batch.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sr.h"
 #include "kernels.h"
+#include "synth.h"
 
 namespace {
 
@@ -40,6 +49,12 @@ sr_status fail(sr_status s, const char* fmt, ...) {
             return fail(st_, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, \
                         __LINE__);                                                            \
         }                                                                                     \
+    } while (0)
+
+#define SR_TRY(expr)                      \
+    do {                                  \
+        sr_status s_ = (expr);            \
+        if (s_ != SR_OK) return s_;       \
     } while (0)
 
 struct DevBuf {
@@ -82,8 +97,10 @@ enum Ctl : int {
     CTL_STATUS = 0,
     CTL_SCAN_COUNTER = 1,
     CTL_WIND_COUNTER = 2,
-    CTL_BUCKETS = 4,   // 4 chain-bucket counters
+    CTL_NDRAW = 3,     // merged fragments + spans of the frame
+    CTL_CHAINS = 4,    // chain counter
     CTL_LONG = 8,      // long-piece counter
+    CTL_QUEUE = 9,     // chain work-queue counter
     CTL_WORDS = 16,
 };
 
@@ -102,276 +119,527 @@ enum Stage : int {
     ST_RESOLVE, ST_COUNT_ALL
 };
 
-struct sr_ctx {
-    int device = 0;
-    int32_t W = 0, H = 0, mode = 0, F = 2;
+static sr_status check_status_word(uint32_t s) {
+    if (s == 0) return SR_OK;
+    if (s & sr::ERR_LOOKBACK_TIMEOUT) return fail(SR_ERR_TIMEOUT, "device look-back wait timed out (status 0x%x)", s);
+    if (s & sr::ERR_CAPACITY) return fail(SR_ERR_OVERFLOW_REFIT, "record capacity exceeded (status 0x%x)", s);
+    return fail(SR_ERR_INTERNAL, "device consistency check failed (status 0x%x)", s);
+}
+
+// Host copy of a set of scenes, concatenated in the flattened layout.
+struct HostScenes {
+    std::vector<float> pos;
+    std::vector<uint32_t> pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info, path_scene;
+    std::vector<sr::SceneInfo> info;
+
+    void clear() { *this = HostScenes(); }
+    uint32_t n_points() const { return (uint32_t)pos_path.size(); }
+    uint32_t n_curves() const { return (uint32_t)curve_type.size(); }
+    uint32_t n_paths() const { return (uint32_t)fill_rule.size(); }
+};
+
+static const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+// Validates a caller's scene (the checks of sr_load_scene).
+static sr_status validate_scene(const sr_scene_view* s) {
+    const uint32_t V = s->n_points, C = s->n_curves, P = s->n_paths;
+    if ((V && (!s->position || !s->pos_path_idx)) ||
+        (C && (!s->curve_pos_map || !s->curve_type || !s->curve_path_idx)) || (P && (!s->fill_rule || !s->fill_info)))
+        return fail(SR_ERR_INVALID_ARG, "scene array missing");
+    if (C > (1u << 27) || V > (1u << 29) || P > (1u << 26)) return fail(SR_ERR_INVALID_ARG, "scene too large");
+    for (uint32_t i = 0; i < C; ++i) {
+        uint32_t t = s->curve_type[i];
+        if (t != SR_CURVE_LINE && t != SR_CURVE_QUADRIC && t != SR_CURVE_CUBIC)
+            return fail(SR_ERR_INVALID_ARG, "curve %u: unsupported type 0x%x", i, t);
+        if ((uint64_t)s->curve_pos_map[i] + (t & 7u) > V)
+            return fail(SR_ERR_INVALID_ARG, "curve %u: control points out of range", i);
+        if (s->curve_path_idx[i] >= P) return fail(SR_ERR_INVALID_ARG, "curve %u: path index out of range", i);
+        if (i > 0 && s->curve_path_idx[i] < s->curve_path_idx[i - 1])
+            return fail(SR_ERR_INVALID_ARG, "curves must be grouped by path in path order");
+    }
+    for (uint32_t i = 0; i < V; ++i) {
+        if (s->pos_path_idx[i] >= P) return fail(SR_ERR_INVALID_ARG, "point %u: path index out of range", i);
+        if (!std::isfinite(s->position[2 * (size_t)i]) || !std::isfinite(s->position[2 * (size_t)i + 1]))
+            return fail(SR_ERR_INVALID_ARG, "point %u: coordinate is not finite", i);
+    }
+    for (uint32_t i = 0; i < P; ++i)
+        if (s->fill_rule[i] > 1u) return fail(SR_ERR_INVALID_ARG, "path %u: fill rule %u", i, s->fill_rule[i]);
+    return SR_OK;
+}
+
+// Appends one validated scene to a host set.
+static void append_scene(HostScenes& h, uint32_t w, uint32_t hgt, const sr_scene_view* s, const float* mvp) {
+    const uint32_t pb = h.n_paths(), vb = h.n_points();
+    sr::SceneInfo si{};
+    si.W = (int32_t)w;
+    si.H = (int32_t)hgt;
+    si.path_begin = pb;
+    si.path_end = pb + s->n_paths;
+    std::memcpy(si.mvp, mvp ? mvp : kIdentity, sizeof si.mvp);
+    const uint32_t sidx = (uint32_t)h.info.size();
+    h.info.push_back(si);
+    if (s->n_points) h.pos.insert(h.pos.end(), s->position, s->position + 2 * (size_t)s->n_points);
+    for (uint32_t i = 0; i < s->n_points; ++i) h.pos_path.push_back(s->pos_path_idx[i] + pb);
+    for (uint32_t i = 0; i < s->n_curves; ++i) {
+        h.curve_pos.push_back(s->curve_pos_map[i] + vb);
+        h.curve_type.push_back(s->curve_type[i]);
+        h.curve_path.push_back(s->curve_path_idx[i] + pb);
+    }
+    if (s->n_paths) {
+        h.fill_rule.insert(h.fill_rule.end(), s->fill_rule, s->fill_rule + s->n_paths);
+        h.fill_info.insert(h.fill_info.end(), s->fill_info, s->fill_info + s->n_paths);
+        h.path_scene.insert(h.path_scene.end(), s->n_paths, sidx);
+    }
+}
+
+// --------------------------------------------------------------------------
+// The device pipeline of one set of scenes.
+struct Pipeline {
+    int device = 0, sm_count = 148;
+    int32_t mode = SR_MODE_PIXEL, F = 1;
     uint32_t flags = 0;
-    sr::Mvp mvp;
     bool loaded = false;
-    // scene
-    uint32_t V = 0, C = 0, P = 0;
-    DevBuf pos, pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info;
+    // scenes
+    uint32_t S = 0, V = 0, C = 0, P = 0;
+    int32_t Wmax = 1, Hmax = 1;
+    uint32_t total_rows = 0, res_ctas = 0;
+    uint64_t total_pixels = 0;
+    std::vector<sr::SceneInfo> info;
+    std::vector<uint32_t> cta_base;
+    DevBuf pos, pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info, path_scene, scenes_d, cta_base_d;
     // frame
-    DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, long_list, cbuf, rec;
-    int sm_count = 148;
-    DevBuf keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status;
-    DevBuf draw, draw_row, totals;
+    DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, chain_sort_scratch, long_list;
+    DevBuf cbuf, rec, keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status, draw, draw_row, totals;
     DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, image;
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
-    // pinned host scalars
-    int32_t* h_n = nullptr;        // [2] N, status
-    uint64_t* h_tot = nullptr;     // [3] frags, spans, status
+    // host scalars (pinned): N, status; fragments, spans
+    uint32_t* h_u32 = nullptr;
+    uint64_t* h_u64 = nullptr;
+    // results
     sr_stats stats{};
-    int64_t last_N = 0, last_O = 0;
+    int64_t last_N = 0, last_O = 0, last_cap = 0;
     bool stages_valid = false;
-    // profiling: a start/end event per stage
+    // profiling
     cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
-    bool ev_pending = false;
-    cudaStream_t cur_stream = nullptr;
+    bool ev_pending = false, capturing = false;
+    cudaStream_t cur = nullptr;
 
-    void mark(int stage, bool end) {
-        if (!(flags & SR_FLAG_PROFILE)) return;
-        cudaEvent_t& e = ev[2 * stage + (end ? 1 : 0)];
-        if (!e) cudaEventCreate(&e);
-        cudaEventRecord(e, cur_stream);
-    }
-
-    ~sr_ctx() {
-        DevBuf* all[] = {&pos, &pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info,
-                         &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status, &pieces, &chain_lists,
-                         &long_list,
-                         &cbuf, &rec, &keys, &keys_alt,
-                         &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row,
-                         &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start,
-                         &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
+    ~Pipeline() {
+        DevBuf* all[] = {&pos, &pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info, &path_scene,
+                         &scenes_d, &cta_base_d, &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status,
+                         &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf, &rec, &keys, &keys_alt,
+                         &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
+                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &image, &d_fkey,
+                         &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
-        if (h_n) cudaFreeHost(h_n);
-        if (h_tot) cudaFreeHost(h_tot);
+        if (h_u32) cudaFreeHost(h_u32);
+        if (h_u64) cudaFreeHost(h_u64);
+    }
+
+    sr_status init(int dev, int32_t m, uint32_t fl) {
+        device = dev;
+        mode = m;
+        F = m == SR_MODE_PIXEL ? 1 : 2;
+        flags = fl;
+        CUDA_TRY(cudaSetDevice(dev));
+        cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (sm_count <= 0) sm_count = 148;
+        CUDA_TRY(cudaMallocHost(&h_u32, sizeof(uint32_t) * 8));
+        CUDA_TRY(cudaMallocHost(&h_u64, sizeof(uint64_t) * 4));
+        CUDA_TRY(ensure(ctl, sizeof(uint32_t) * CTL_WORDS));
+        return SR_OK;
+    }
+
+    void mark(int stage, bool end) {
+        if (!(flags & SR_FLAG_PROFILE) || capturing) return;
+        cudaEvent_t& e = ev[2 * stage + (end ? 1 : 0)];
+        if (!e) cudaEventCreate(&e);
+        cudaEventRecord(e, cur);
     }
 
     sr::KeyLayout layout() const {
         sr::KeyLayout L;
         L.F = F;
-        L.W = W;
-        L.H = H;
-        L.Hy = (H + F - 1) / F;
-        L.xbits = bits_for((uint64_t)((W & ~1) / F + 2));
+        L.W = Wmax;
+        L.H = Hmax;
+        L.Hy = (Hmax + F - 1) / F;
+        L.xbits = bits_for((uint64_t)((Wmax & ~1) / F + 2));
         L.rbits = bits_for((uint64_t)L.Hy);
         L.pbits = bits_for(P > 0 ? (uint64_t)(P - 1) : 0);
         return L;
     }
+
+    sr::SceneTable table() const { return sr::SceneTable{scenes_d.as<sr::SceneInfo>(), path_scene.as<uint32_t>(), S}; }
+
+    // Places the scenes' rows and framebuffers and uploads the scene table.
+    sr_status upload_table() {
+        total_rows = 0;
+        total_pixels = 0;
+        res_ctas = 0;
+        Wmax = 1;
+        Hmax = 1;
+        cta_base.assign(S + 1, 0);
+        for (uint32_t s = 0; s < S; ++s) {
+            sr::SceneInfo& si = info[s];
+            si.rows = (uint32_t)((si.H + F - 1) / F);
+            si.row_base = total_rows;
+            si.image_off = total_pixels;
+            total_rows += si.rows;
+            total_pixels += (uint64_t)si.W * (uint64_t)si.H;
+            Wmax = std::max(Wmax, si.W);
+            Hmax = std::max(Hmax, si.H);
+            cta_base[s] = res_ctas;
+            uint32_t rpc = sr::resolve_rows_per_cta(si.W);
+            res_ctas += (si.rows + rpc - 1) / rpc;
+        }
+        cta_base[S] = res_ctas;
+        CUDA_TRY(ensure(scenes_d, sizeof(sr::SceneInfo) * std::max<uint32_t>(S, 1)));
+        CUDA_TRY(ensure(cta_base_d, sizeof(uint32_t) * (S + 1)));
+        CUDA_TRY(ensure(image, 4 * std::max<uint64_t>(total_pixels, 1)));
+        if (S) CUDA_TRY(cudaMemcpy(scenes_d.p, info.data(), sizeof(sr::SceneInfo) * S, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(cta_base_d.p, cta_base.data(), sizeof(uint32_t) * (S + 1), cudaMemcpyHostToDevice));
+        return SR_OK;
+    }
+
+    sr_status upload(const HostScenes& h) {
+        CUDA_TRY(cudaSetDevice(device));
+        S = (uint32_t)h.info.size();
+        V = h.n_points();
+        C = h.n_curves();
+        P = h.n_paths();
+        if (C > (1u << 27) || V > (1u << 29) || P > (1u << 26)) return fail(SR_ERR_INVALID_ARG, "scene set too large");
+        info = h.info;
+        CUDA_TRY(ensure(pos, sizeof(float) * 2 * (size_t)std::max<uint32_t>(V, 1)));
+        CUDA_TRY(ensure(pos_path, sizeof(uint32_t) * std::max<uint32_t>(V, 1)));
+        CUDA_TRY(ensure(curve_pos, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(curve_type, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(curve_path, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(fill_rule, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        CUDA_TRY(ensure(fill_info, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        CUDA_TRY(ensure(path_scene, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        auto up = [](DevBuf& d, const void* src, size_t bytes) -> cudaError_t {
+            return bytes ? cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+        };
+        CUDA_TRY(up(pos, h.pos.data(), sizeof(float) * h.pos.size()));
+        CUDA_TRY(up(pos_path, h.pos_path.data(), sizeof(uint32_t) * V));
+        CUDA_TRY(up(curve_pos, h.curve_pos.data(), sizeof(uint32_t) * C));
+        CUDA_TRY(up(curve_type, h.curve_type.data(), sizeof(uint32_t) * C));
+        CUDA_TRY(up(curve_path, h.curve_path.data(), sizeof(uint32_t) * C));
+        CUDA_TRY(up(fill_rule, h.fill_rule.data(), sizeof(uint32_t) * P));
+        CUDA_TRY(up(fill_info, h.fill_info.data(), sizeof(uint32_t) * P));
+        CUDA_TRY(up(path_scene, h.path_scene.data(), sizeof(uint32_t) * P));
+        SR_TRY(upload_table());
+        loaded = true;
+        stages_valid = false;
+        return SR_OK;
+    }
+
+    sr::GeomArgs geom(int64_t cap) const {
+        sr::GeomArgs g;
+        g.n_curves = C;
+        g.curve_type = curve_type.as<uint32_t>();
+        g.curve_pos = curve_pos.as<uint32_t>();
+        g.curve_path = curve_path.as<uint32_t>();
+        g.tpos = tpos.as<float2>();
+        g.path_visible = path_visible.as<int32_t>();
+        g.W = Wmax;
+        g.H = Hmax;
+        g.F = F;
+        g.pixel_mode = mode == SR_MODE_PIXEL;
+        g.L = layout();
+        g.st = table();
+        g.rec_cap = cap;
+        return g;
+    }
+
+    uint32_t list_cap() const { return sr::chain_list_capacity(std::max<uint32_t>(C, 1)); }
+
+    sr::ChainWork chain_work() const {
+        sr::ChainWork cw;
+        uint32_t* ctlp = ctl.as<uint32_t>();
+        uint32_t* cl = chain_lists.as<uint32_t>();
+        const uint32_t lc = list_cap();
+        cw.pieces = pieces.as<uint4>();
+        cw.chain_items = cl;
+        cw.chain_keys = cl + lc;
+        cw.sorted_items = cl + 2 * (size_t)lc;
+        cw.sorted_keys = cl + 3 * (size_t)lc;
+        cw.list_cap = lc;
+        cw.chain_count = ctlp + CTL_CHAINS;
+        cw.chain_queue = ctlp + CTL_QUEUE;
+        cw.long_list = long_list.as<uint32_t>();
+        cw.long_count = ctlp + CTL_LONG;
+        return cw;
+    }
+
+    // Buffers of the stages before the record count is known.
+    sr_status prepare_front() {
+        CUDA_TRY(ensure(tpos, sizeof(float2) * std::max<uint32_t>(V, 1)));
+        CUDA_TRY(ensure(path_visible, sizeof(int32_t) * std::max<uint32_t>(P, 1)));
+        CUDA_TRY(ensure(cut, sizeof(float) * 5 * (size_t)std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(count, sizeof(int32_t) * ((size_t)C + 1)));
+        CUDA_TRY(ensure(offs, sizeof(int32_t) * ((size_t)C + 1)));
+        CUDA_TRY(ensure(scan_status, sizeof(uint64_t) * sr::scan_status_words(C)));
+        CUDA_TRY(ensure(pieces, sr::piece_table_bytes(std::max<uint32_t>(C, 1))));
+        const uint32_t lc = list_cap();
+        CUDA_TRY(ensure(chain_lists, sizeof(uint32_t) * 6 * (size_t)lc));
+        CUDA_TRY(ensure(long_list, sizeof(uint32_t) * (size_t)lc));
+        sr::SortPlan cp = sr::sort_plan(lc, sr::chain_key_bits(), ctl.as<uint32_t>() + CTL_CHAINS);
+        CUDA_TRY(ensure(chain_sort_scratch, sr::sort_scratch_bytes(cp)));
+        CUDA_TRY(ensure(totals, sizeof(uint64_t) * 4));
+        CUDA_TRY(ensure(row_start, sizeof(int32_t) * ((size_t)total_rows + 1)));
+        return SR_OK;
+    }
+
+    // Buffers of the stages after the count, for `cap` records.
+    sr_status reserve(int64_t cap) {
+        const size_t n1 = (size_t)std::max<int64_t>(cap, 1);
+        CUDA_TRY(ensure(cbuf, sizeof(int32_t) * n1));
+        CUDA_TRY(ensure(rec, sizeof(int2) * n1));
+        CUDA_TRY(ensure(keys, sizeof(uint64_t) * n1));
+        CUDA_TRY(ensure(keys_alt, sizeof(uint64_t) * n1));
+        CUDA_TRY(ensure(skeys, sizeof(uint64_t) * n1));
+        CUDA_TRY(ensure(wnp, n1));
+        CUDA_TRY(ensure(svals, sizeof(uint32_t) * n1));
+        CUDA_TRY(ensure(vals_alt, sizeof(uint32_t) * n1));
+        const sr::KeyLayout L = layout();
+        sr::SortPlan sp = sr::sort_plan(cap, L.pbits + L.rbits + L.xbits, nullptr);
+        CUDA_TRY(ensure(sort_scratch, sr::sort_scratch_bytes(sp)));
+        CUDA_TRY(ensure(wind_status, sizeof(uint64_t) * sr::winding_status_words(cap)));
+        const size_t d1 = 2 * n1;
+        CUDA_TRY(ensure(draw, sizeof(int4) * d1));
+        CUDA_TRY(ensure(draw_row, sizeof(uint32_t) * d1));
+        CUDA_TRY(ensure(rkeys, sizeof(uint32_t) * d1));
+        CUDA_TRY(ensure(rvals, sizeof(uint32_t) * d1));
+        CUDA_TRY(ensure(rkeys_alt, sizeof(uint32_t) * d1));
+        CUDA_TRY(ensure(rvals_alt, sizeof(uint32_t) * d1));
+        sr::SortPlan rp = sr::sort_plan((int64_t)d1, bits_for(total_rows), nullptr);
+        CUDA_TRY(ensure(row_sort_scratch, sr::sort_scratch_bytes(rp)));
+        if (flags & SR_FLAG_KEEP_STAGES) {
+            CUDA_TRY(ensure(d_fkey, sizeof(int32_t) * n1));
+            CUDA_TRY(ensure(d_fwn, sizeof(int32_t) * n1));
+            CUDA_TRY(ensure(d_fleft, sizeof(int32_t) * n1));
+            CUDA_TRY(ensure(d_wscan, sizeof(int32_t) * (n1 + 1)));
+            CUDA_TRY(ensure(d_fflag, sizeof(int32_t) * n1));
+            CUDA_TRY(ensure(d_sflag, sizeof(int32_t) * n1));
+            CUDA_TRY(ensure(d_skey, sizeof(int32_t) * n1));
+        }
+        return SR_OK;
+    }
+
+    // Transform, count, chain order and offset scan (no allocation, no wait).
+    sr_status enqueue_front(cudaStream_t st) {
+        using namespace sr;
+        uint32_t* ctlp = ctl.as<uint32_t>();
+        uint32_t* status = ctlp + CTL_STATUS;
+        CUDA_TRY(cudaMemsetAsync(ctlp, 0, sizeof(uint32_t) * CTL_WORDS, st));
+        CUDA_TRY(cudaMemsetAsync(path_visible.p, 0, sizeof(int32_t) * std::max<uint32_t>(P, 1), st));
+        CUDA_TRY(cudaMemsetAsync(scan_status.p, 0, sizeof(uint64_t) * scan_status_words(C), st));
+        CUDA_TRY(cudaMemsetAsync(totals.p, 0, sizeof(uint64_t) * 4, st));
+        mark(ST_TRANSFORM, false);
+        launch_transform(pos.as<float2>(), pos_path.as<uint32_t>(), V, table(), tpos.as<float2>(),
+                         path_visible.as<int32_t>(), st);
+        mark(ST_TRANSFORM, true);
+        const GeomArgs g = geom(0);
+        const ChainWork cw = chain_work();
+        const uint32_t lc = list_cap();
+        SortPlan cp = sort_plan(lc, chain_key_bits(), ctlp + CTL_CHAINS);
+        uint32_t* cl = chain_lists.as<uint32_t>();
+        mark(ST_COUNT, false);
+        launch_count(g, cut.as<float>(), count.as<int32_t>(), cw, status, st);
+        launch_sort_u32(cp, cw.chain_keys, cw.chain_items, cw.sorted_keys, cw.sorted_items, cl + 4 * (size_t)lc,
+                        cl + 5 * (size_t)lc, chain_sort_scratch.p, status, st);
+        mark(ST_COUNT, true);
+        mark(ST_SCAN, false);
+        launch_exclusive_scan_i32(count.as<int32_t>(), offs.as<int32_t>(), C, scan_status.as<uint64_t>(),
+                                  ctlp + CTL_SCAN_COUNTER, status, st);
+        mark(ST_SCAN, true);
+        CUDA_TRY(cudaGetLastError());
+        return SR_OK;
+    }
+
+    // Everything after the count, sized for `cap` records (no allocation,
+    // no wait).  The kernels read the actual count from offs[C].
+    sr_status enqueue_back(cudaStream_t st, int64_t cap) {
+        using namespace sr;
+        uint32_t* ctlp = ctl.as<uint32_t>();
+        uint32_t* status = ctlp + CTL_STATUS;
+        const bool keep = (flags & SR_FLAG_KEEP_STAGES) != 0;
+        const uint32_t* n_dev = reinterpret_cast<const uint32_t*>(offs.as<int32_t>() + C);
+        const GeomArgs g = geom(cap);
+        const ChainWork cw = chain_work();
+        DebugOut dbg{nullptr, nullptr, nullptr};
+        if (keep) {
+            dbg.fkey = d_fkey.as<int32_t>();
+            dbg.fwn = d_fwn.as<int32_t>();
+            dbg.fleft = d_fleft.as<int32_t>();
+            CUDA_TRY(cudaMemsetAsync(d_wscan.p, 0, sizeof(int32_t) * ((size_t)std::max<int64_t>(cap, 1) + 1), st));
+        }
+        mark(ST_CHAINS, false);
+        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, st);
+        mark(ST_CHAINS, true);
+        mark(ST_MERGE, false);
+        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, st);
+        mark(ST_MERGE, true);
+        mark(ST_FRAGMENT, false);
+        launch_fragment(g, rec.as<int2>(), cap, n_dev, keys.as<uint64_t>(), wnp.as<uint8_t>(), dbg, st);
+        mark(ST_FRAGMENT, true);
+        const KeyLayout L = g.L;
+        SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev);
+        mark(ST_SORT, false);
+        launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(), svals.as<uint32_t>(),
+                        keys_alt.as<uint64_t>(), vals_alt.as<uint32_t>(), sort_scratch.p, status, st);
+        mark(ST_SORT, true);
+        CUDA_TRY(cudaMemsetAsync(wind_status.p, 0, sizeof(uint64_t) * winding_status_words(cap), st));
+        WindArgs wa;
+        wa.n = cap;
+        wa.n_dev = n_dev;
+        wa.skeys = skeys.as<uint64_t>();
+        wa.svals = svals.as<uint32_t>();
+        wa.wnp = wnp.as<uint8_t>();
+        wa.fill_rule = fill_rule.as<uint32_t>();
+        wa.fill_info = fill_info.as<uint32_t>();
+        wa.n_paths = P;
+        wa.W = Wmax;
+        wa.H = Hmax;
+        wa.F = F;
+        wa.pixel_mode = g.pixel_mode;
+        wa.L = L;
+        wa.st = table();
+        wa.draw = draw.as<int4>();
+        wa.draw_capacity = 2 * std::max<int64_t>(cap, 1);
+        wa.draw_row = draw_row.as<uint32_t>();
+        wa.totals = totals.as<uint64_t>();
+        wa.n_draw = ctlp + CTL_NDRAW;
+        wa.dbg_wscan = keep ? d_wscan.as<int32_t>() : nullptr;
+        wa.dbg_fflag = keep ? d_fflag.as<int32_t>() : nullptr;
+        wa.dbg_sflag = keep ? d_sflag.as<int32_t>() : nullptr;
+        wa.dbg_skey = keep ? d_skey.as<int32_t>() : nullptr;
+        mark(ST_WINDING, false);
+        launch_winding_emit(wa, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
+        mark(ST_WINDING, true);
+        const int64_t dcap = 2 * std::max<int64_t>(cap, 1);
+        SortPlan rp = sort_plan(dcap, bits_for(total_rows), ctlp + CTL_NDRAW);
+        mark(ST_ROWSORT, false);
+        launch_sort_u32(rp, draw_row.as<uint32_t>(), nullptr, rkeys.as<uint32_t>(), rvals.as<uint32_t>(),
+                        rkeys_alt.as<uint32_t>(), rvals_alt.as<uint32_t>(), row_sort_scratch.p, status, st);
+        launch_row_bounds(rkeys.as<uint32_t>(), dcap, ctlp + CTL_NDRAW, (int32_t)total_rows, row_start.as<int32_t>(),
+                          st);
+        mark(ST_ROWSORT, true);
+        ResolveArgs ra;
+        ra.draw = draw.as<int4>();
+        ra.row_sorted_idx = rvals.as<uint32_t>();
+        ra.row_start = row_start.as<int32_t>();
+        ra.cta_base = cta_base_d.as<uint32_t>();
+        ra.scenes = scenes_d.as<SceneInfo>();
+        ra.n_scenes = S;
+        ra.F = F;
+        ra.pixel_mode = g.pixel_mode;
+        ra.image = image.as<uint32_t>();
+        mark(ST_RESOLVE, false);
+        launch_resolve(ra, res_ctas, st);
+        mark(ST_RESOLVE, true);
+        CUDA_TRY(cudaGetLastError());
+        return SR_OK;
+    }
+
+    // Read N back (the reference's count read-back, scanline_rasterizer.cpp:355-356).
+    sr_status read_count(cudaStream_t st, int64_t* N) {
+        CUDA_TRY(cudaMemcpyAsync(&h_u32[0], offs.as<int32_t>() + C, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&h_u32[1], ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        SR_TRY(check_status_word(h_u32[1]));
+        *N = (int64_t)(int32_t)h_u32[0];
+        if (*N < 0 || *N >= (1ll << 30))
+            return fail(SR_ERR_OVERFLOW_REFIT, "record count %lld out of range", (long long)*N);
+        return SR_OK;
+    }
+
+    // One frame.  cap < 0: size the record buffers exactly (one host wait
+    // for N); cap >= 0: use that capacity without waiting.
+    sr_status frame(cudaStream_t st, int64_t cap) {
+        CUDA_TRY(cudaSetDevice(device));
+        if (!loaded) return fail(SR_ERR_NO_SCENE, "render before a scene was loaded");
+        cur = st;
+        stages_valid = false;
+        const uint64_t launches0 = sr::launches_so_far();
+        SR_TRY(prepare_front());
+        SR_TRY(enqueue_front(st));
+        if (cap < 0) {
+            int64_t N = 0;
+            SR_TRY(read_count(st, &N));
+            cap = N;
+        }
+        SR_TRY(reserve(cap));
+        SR_TRY(enqueue_back(st, cap));
+        stats.kernel_launches = (uint32_t)(sr::launches_so_far() - launches0);
+        ev_pending = (flags & SR_FLAG_PROFILE) != 0;
+        last_cap = cap;
+        return SR_OK;
+    }
+
+    // Waits for the frame and collects its counters and status.
+    sr_status finish(cudaStream_t st) {
+        CUDA_TRY(cudaMemcpyAsync(&h_u32[0], offs.as<int32_t>() + C, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&h_u32[1], ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(h_u64, totals.p, sizeof(uint64_t) * 2, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        last_N = (int64_t)(int32_t)h_u32[0];
+        last_O = (int64_t)(h_u64[0] + h_u64[1]);
+        stats.n_intersections = (uint64_t)last_N;
+        stats.n_draw_records = (uint64_t)last_O;
+        stats.n_merged_fragments = h_u64[0];
+        stats.n_spans = h_u64[1];
+        const sr::KeyLayout L = layout();
+        stats.key_bits = L.pbits + L.rbits + L.xbits;
+        stats.sort_passes = sr::sort_plan(1, stats.key_bits).passes;
+        SR_TRY(check_status_word(h_u32[1]));
+        if (last_N > last_cap)
+            return fail(SR_ERR_OVERFLOW_REFIT, "frame needs %lld records, capacity %lld", (long long)last_N,
+                        (long long)last_cap);
+        stages_valid = (flags & SR_FLAG_KEEP_STAGES) != 0;
+        return SR_OK;
+    }
+
+    sr_status collect_events() {
+        if (!ev_pending) return SR_OK;
+        CUDA_TRY(cudaEventSynchronize(ev[2 * ST_RESOLVE + 1]));
+        for (int s = 0; s < ST_COUNT_ALL; ++s) {
+            float ms = 0.f;
+            if (ev[2 * s] && ev[2 * s + 1]) CUDA_TRY(cudaEventElapsedTime(&ms, ev[2 * s], ev[2 * s + 1]));
+            stats.stage_ms[s] = ms;
+        }
+        ev_pending = false;
+        return SR_OK;
+    }
 };
 
-static sr_status check_status_word(uint32_t s) {
-    if (s == 0) return SR_OK;
-    if (s & sr::ERR_LOOKBACK_TIMEOUT) return fail(SR_ERR_TIMEOUT, "device look-back wait timed out (status 0x%x)", s);
-    if (s & sr::ERR_CAPACITY) return fail(SR_ERR_OVERFLOW_REFIT, "device buffer capacity exceeded (status 0x%x)", s);
-    return fail(SR_ERR_INTERNAL, "device consistency check failed (status 0x%x)", s);
-}
+struct sr_ctx {
+    Pipeline p;
+    HostScenes h;
+    int32_t W = 0, H = 0;
+    float mvp[16];
+};
 
-static sr_status render_frame(sr_ctx* c, cudaStream_t st) {
-    using namespace sr;
-    const bool keep = (c->flags & SR_FLAG_KEEP_STAGES) != 0;
-    const uint32_t V = c->V, C = c->C, P = c->P;
-    CUDA_TRY(cudaSetDevice(c->device));
-    CUDA_TRY(ensure(c->tpos, sizeof(float2) * std::max<uint32_t>(V, 1)));
-    CUDA_TRY(ensure(c->path_visible, sizeof(int32_t) * std::max<uint32_t>(P, 1)));
-    CUDA_TRY(ensure(c->cut, sizeof(float) * 5 * (size_t)std::max<uint32_t>(C, 1)));
-    CUDA_TRY(ensure(c->count, sizeof(int32_t) * ((size_t)C + 1)));
-    CUDA_TRY(ensure(c->offs, sizeof(int32_t) * ((size_t)C + 1)));
-    CUDA_TRY(ensure(c->ctl, sizeof(uint32_t) * CTL_WORDS));
-    CUDA_TRY(ensure(c->scan_status, sizeof(uint64_t) * scan_status_words(C)));
-    CUDA_TRY(ensure(c->pieces, piece_table_bytes(std::max<uint32_t>(C, 1))));
-    const uint32_t list_cap = chain_list_capacity(std::max<uint32_t>(C, 1));
-    CUDA_TRY(ensure(c->chain_lists, sizeof(uint32_t) * 4 * (size_t)list_cap));
-    CUDA_TRY(ensure(c->long_list, sizeof(uint32_t) * (size_t)list_cap));
-    uint32_t* ctl = c->ctl.as<uint32_t>();
-    uint32_t* status = ctl + CTL_STATUS;
-
-    CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * CTL_WORDS, st));
-    CUDA_TRY(cudaMemsetAsync(c->path_visible.p, 0, sizeof(int32_t) * std::max<uint32_t>(P, 1), st));
-    CUDA_TRY(cudaMemsetAsync(c->scan_status.p, 0, sizeof(uint64_t) * scan_status_words(C), st));
-
-    c->cur_stream = st;
-    const uint64_t launches0 = launches_so_far();
-    // K1 transform (transform_pos.comp)
-    c->mark(ST_TRANSFORM, false);
-    launch_transform(c->pos.as<float2>(), c->pos_path.as<uint32_t>(), V, c->mvp, (float)c->W, (float)c->H,
-                     c->tpos.as<float2>(), c->path_visible.as<int32_t>(), st);
-    c->mark(ST_TRANSFORM, true);
-    GeomArgs g;
-    g.n_curves = C;
-    g.curve_type = c->curve_type.as<uint32_t>();
-    g.curve_pos = c->curve_pos.as<uint32_t>();
-    g.curve_path = c->curve_path.as<uint32_t>();
-    g.tpos = c->tpos.as<float2>();
-    g.path_visible = c->path_visible.as<int32_t>();
-    g.W = c->W;
-    g.H = c->H;
-    g.F = c->F;
-    g.pixel_mode = c->mode == SR_MODE_PIXEL;
-    g.L = c->layout();
-    // K2 count pass + K3 offset scan (make_intersection_0.comp, naive_scan.comp)
-    ChainWork cw;
-    cw.pieces = c->pieces.as<uint4>();
-    cw.chain_lists = c->chain_lists.as<uint32_t>();
-    cw.list_cap = list_cap;
-    cw.bucket_count = ctl + CTL_BUCKETS;
-    cw.long_list = c->long_list.as<uint32_t>();
-    cw.long_count = ctl + CTL_LONG;
-    c->mark(ST_COUNT, false);
-    launch_count(g, c->cut.as<float>(), c->count.as<int32_t>(), cw, status, st);
-    c->mark(ST_COUNT, true);
-    c->mark(ST_SCAN, false);
-    launch_exclusive_scan_i32(c->count.as<int32_t>(), c->offs.as<int32_t>(), C, c->scan_status.as<uint64_t>(),
-                              ctl + CTL_SCAN_COUNTER, status, st);
-    c->mark(ST_SCAN, true);
-    CUDA_TRY(cudaGetLastError());
-    // read back N, as the reference does (scanline_rasterizer.cpp:355-356)
-    CUDA_TRY(cudaMemcpyAsync(&c->h_n[0], c->offs.as<int32_t>() + C, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(&c->h_n[1], status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    {
-        sr_status s = check_status_word((uint32_t)c->h_n[1]);
-        if (s != SR_OK) return s;
+// Batch of scenes (several uneven scenes per frame).
+struct sr_batch {
+    Pipeline p;
+    HostScenes h;
+    bool committed = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t graph_cap = -1;
+    uint32_t graph_launches = 0;
+    uint32_t overflows = 0, refits = 0;
+    cudaStream_t cap_stream = nullptr;   // captures run here: the legacy stream cannot be captured
+    ~sr_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
     }
-    const int64_t N = c->h_n[0];
-    if (N < 0 || N >= (1ll << 30)) return fail(SR_ERR_OVERFLOW_REFIT, "record count %lld out of range", (long long)N);
-    c->last_N = N;
-    const size_t n1 = (size_t)std::max<int64_t>(N, 1);
-
-    CUDA_TRY(ensure(c->cbuf, sizeof(int32_t) * n1));
-    CUDA_TRY(ensure(c->rec, sizeof(int2) * n1));
-    CUDA_TRY(ensure(c->keys, sizeof(uint64_t) * n1));
-    CUDA_TRY(ensure(c->keys_alt, sizeof(uint64_t) * n1));
-    CUDA_TRY(ensure(c->skeys, sizeof(uint64_t) * n1));
-    CUDA_TRY(ensure(c->wnp, n1));
-    CUDA_TRY(ensure(c->svals, sizeof(uint32_t) * n1));
-    CUDA_TRY(ensure(c->vals_alt, sizeof(uint32_t) * n1));
-    DebugOut dbg{nullptr, nullptr, nullptr};
-    if (keep) {
-        CUDA_TRY(ensure(c->d_fkey, sizeof(int32_t) * n1));
-        CUDA_TRY(ensure(c->d_fwn, sizeof(int32_t) * n1));
-        CUDA_TRY(ensure(c->d_fleft, sizeof(int32_t) * n1));
-        CUDA_TRY(ensure(c->d_wscan, sizeof(int32_t) * (n1 + 1)));
-        CUDA_TRY(ensure(c->d_fflag, sizeof(int32_t) * n1));
-        CUDA_TRY(ensure(c->d_sflag, sizeof(int32_t) * n1));
-        CUDA_TRY(ensure(c->d_skey, sizeof(int32_t) * n1));
-        dbg.fkey = c->d_fkey.as<int32_t>();
-        dbg.fwn = c->d_fwn.as<int32_t>();
-        dbg.fleft = c->d_fleft.as<int32_t>();
-        CUDA_TRY(cudaMemsetAsync(c->d_wscan.p, 0, sizeof(int32_t) * (n1 + 1), st));
-    }
-    // K4 intersections: crossing chains, then the per-curve merge
-    c->mark(ST_CHAINS, false);
-    launch_chains(g, c->offs.as<int32_t>(), cw, c->cbuf.as<int32_t>(), c->sm_count, st);
-    c->mark(ST_CHAINS, true);
-    c->mark(ST_MERGE, false);
-    launch_merge(g, c->offs.as<int32_t>(), cw, c->cbuf.as<int32_t>(), c->rec.as<int2>(), status, st);
-    c->mark(ST_MERGE, true);
-    // K5 fragments and sort keys
-    c->mark(ST_FRAGMENT, false);
-    launch_fragment(g, c->rec.as<int2>(), N, c->keys.as<uint64_t>(), c->wnp.as<uint8_t>(), dbg, st);
-    c->mark(ST_FRAGMENT, true);
-    CUDA_TRY(cudaGetLastError());
-
-    // K6 sort by (path, row rank, x)
-    const KeyLayout L = g.L;
-    uint32_t key_bits = L.pbits + L.rbits + L.xbits;
-    SortPlan sp = sort_plan(N, key_bits);
-    CUDA_TRY(ensure(c->sort_scratch, sort_scratch_bytes(sp)));
-    c->mark(ST_SORT, false);
-    launch_sort_u64(sp, c->keys.as<uint64_t>(), nullptr, c->skeys.as<uint64_t>(), c->svals.as<uint32_t>(),
-                    c->keys_alt.as<uint64_t>(), c->vals_alt.as<uint32_t>(), c->sort_scratch.p, status, st);
-    c->mark(ST_SORT, true);
-    CUDA_TRY(cudaGetLastError());
-
-    // K7..K9 winding scan, flags and draw-list emit
-    const int64_t draw_cap = 2 * (int64_t)n1;
-    CUDA_TRY(ensure(c->draw, sizeof(int4) * (size_t)draw_cap));
-    CUDA_TRY(ensure(c->draw_row, sizeof(uint32_t) * (size_t)draw_cap));
-    CUDA_TRY(ensure(c->totals, sizeof(uint64_t) * 4));
-    CUDA_TRY(ensure(c->wind_status, sizeof(uint64_t) * winding_status_words(N)));
-    CUDA_TRY(cudaMemsetAsync(c->wind_status.p, 0, sizeof(uint64_t) * winding_status_words(N), st));
-    CUDA_TRY(cudaMemsetAsync(c->totals.p, 0, sizeof(uint64_t) * 4, st));
-    WindArgs wa;
-    wa.n = N;
-    wa.skeys = c->skeys.as<uint64_t>();
-    wa.svals = c->svals.as<uint32_t>();
-    wa.wnp = c->wnp.as<uint8_t>();
-    wa.fill_rule = c->fill_rule.as<uint32_t>();
-    wa.fill_info = c->fill_info.as<uint32_t>();
-    wa.n_paths = P;
-    wa.W = c->W;
-    wa.H = c->H;
-    wa.F = c->F;
-    wa.pixel_mode = g.pixel_mode;
-    wa.L = L;
-    wa.draw = c->draw.as<int4>();
-    wa.draw_capacity = draw_cap;
-    wa.draw_row = c->draw_row.as<uint32_t>();
-    wa.row_count = nullptr;
-    wa.totals = c->totals.as<uint64_t>();
-    wa.dbg_wscan = keep ? c->d_wscan.as<int32_t>() : nullptr;
-    wa.dbg_fflag = keep ? c->d_fflag.as<int32_t>() : nullptr;
-    wa.dbg_sflag = keep ? c->d_sflag.as<int32_t>() : nullptr;
-    wa.dbg_skey = keep ? c->d_skey.as<int32_t>() : nullptr;
-    c->mark(ST_WINDING, false);
-    launch_winding_emit(wa, c->wind_status.as<uint64_t>(), ctl + CTL_WIND_COUNTER, status, st);
-    c->mark(ST_WINDING, true);
-    CUDA_TRY(cudaGetLastError());
-    // read back the draw-list size (scanline_rasterizer.cpp:578-580)
-    CUDA_TRY(cudaMemcpyAsync(c->h_tot, c->totals.p, sizeof(uint64_t) * 2, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(&c->h_n[1], status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    {
-        sr_status s = check_status_word((uint32_t)c->h_n[1]);
-        if (s != SR_OK) return s;
-    }
-    const int64_t O = (int64_t)(c->h_tot[0] + c->h_tot[1]);
-    c->last_O = O;
-    c->stats.n_intersections = (uint64_t)N;
-    c->stats.n_draw_records = (uint64_t)O;
-    c->stats.n_merged_fragments = c->h_tot[0];
-    c->stats.n_spans = c->h_tot[1];
-    c->stats.key_bits = key_bits;
-    c->stats.sort_passes = sp.passes;
-
-    // K10 resolve: stable sort of draw records by cell row, then paint rows
-    const int32_t rows = L.Hy;
-    const size_t o1 = (size_t)std::max<int64_t>(O, 1);
-    CUDA_TRY(ensure(c->rkeys, sizeof(uint32_t) * o1));
-    CUDA_TRY(ensure(c->rvals, sizeof(uint32_t) * o1));
-    CUDA_TRY(ensure(c->rkeys_alt, sizeof(uint32_t) * o1));
-    CUDA_TRY(ensure(c->rvals_alt, sizeof(uint32_t) * o1));
-    CUDA_TRY(ensure(c->row_start, sizeof(int32_t) * ((size_t)rows + 1)));
-    SortPlan rp = sort_plan(O, bits_for((uint64_t)rows));
-    CUDA_TRY(ensure(c->row_sort_scratch, sort_scratch_bytes(rp)));
-    c->mark(ST_ROWSORT, false);
-    launch_sort_u32(rp, c->draw_row.as<uint32_t>(), nullptr, c->rkeys.as<uint32_t>(), c->rvals.as<uint32_t>(),
-                    c->rkeys_alt.as<uint32_t>(), c->rvals_alt.as<uint32_t>(), c->row_sort_scratch.p, status, st);
-    launch_row_bounds(c->rkeys.as<uint32_t>(), O, rows, c->row_start.as<int32_t>(), st);
-    c->mark(ST_ROWSORT, true);
-    ResolveArgs ra;
-    ra.draw = c->draw.as<int4>();
-    ra.row_sorted_idx = c->rvals.as<uint32_t>();
-    ra.row_start = c->row_start.as<int32_t>();
-    ra.W = c->W;
-    ra.H = c->H;
-    ra.F = c->F;
-    ra.pixel_mode = g.pixel_mode;
-    ra.image = c->image.as<uint32_t>();
-    c->mark(ST_RESOLVE, false);
-    launch_resolve(ra, st);
-    c->mark(ST_RESOLVE, true);
-    CUDA_TRY(cudaGetLastError());
-    c->stats.kernel_launches = (uint32_t)(launches_so_far() - launches0);
-    c->ev_pending = (c->flags & SR_FLAG_PROFILE) != 0;
-    c->stages_valid = keep;
-    return SR_OK;
-}
+};
 
 extern "C" {
 
@@ -393,103 +661,48 @@ sr_status sr_create(uint32_t width, uint32_t height, const sr_options* opt, sr_c
     int ndev = 0;
     CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (o.device < 0 || o.device >= ndev) return fail(SR_ERR_INVALID_ARG, "device %d not present", o.device);
-    CUDA_TRY(cudaSetDevice(o.device));
     sr_ctx* c = new sr_ctx();
-    c->device = o.device;
-    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, o.device);
-    if (c->sm_count <= 0) c->sm_count = 148;
+    sr_status s = c->p.init(o.device, o.mode, o.flags);
+    if (s != SR_OK) {
+        delete c;
+        return s;
+    }
     c->W = (int32_t)width;
     c->H = (int32_t)height;
-    c->mode = o.mode;
-    c->F = o.mode == SR_MODE_PIXEL ? 1 : 2;
-    c->flags = o.flags;
-    const float id[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-    std::memcpy(c->mvp.m, id, sizeof id);
-    cudaError_t e = cudaMallocHost(&c->h_n, sizeof(int32_t) * 4);
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_tot, sizeof(uint64_t) * 4);
-    if (e == cudaSuccess) e = ensure(c->image, (size_t)width * height * 4);
-    if (e != cudaSuccess) {
-        delete c;
-        return fail(e == cudaErrorMemoryAllocation ? SR_ERR_OOM : SR_ERR_CUDA, "sr_create: %s", cudaGetErrorString(e));
-    }
+    std::memcpy(c->mvp, kIdentity, sizeof c->mvp);
     *out = c;
     return SR_OK;
 }
 
 sr_status sr_load_scene(sr_ctx* c, const sr_scene_view* s) {
     if (!c || !s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
-    const uint32_t V = s->n_points, C = s->n_curves, P = s->n_paths;
-    if ((V && (!s->position || !s->pos_path_idx)) || (C && (!s->curve_pos_map || !s->curve_type || !s->curve_path_idx)) ||
-        (P && (!s->fill_rule || !s->fill_info)))
-        return fail(SR_ERR_INVALID_ARG, "scene array missing");
-    if (C > (1u << 28) || V > (1u << 30) || P > (1u << 26)) return fail(SR_ERR_INVALID_ARG, "scene too large");
-    for (uint32_t i = 0; i < C; ++i) {
-        uint32_t t = s->curve_type[i];
-        if (t != SR_CURVE_LINE && t != SR_CURVE_QUADRIC && t != SR_CURVE_CUBIC)
-            return fail(SR_ERR_INVALID_ARG, "curve %u: unsupported type 0x%x", i, t);
-        if ((uint64_t)s->curve_pos_map[i] + (t & 7u) > V)
-            return fail(SR_ERR_INVALID_ARG, "curve %u: control points out of range", i);
-        if (s->curve_path_idx[i] >= P) return fail(SR_ERR_INVALID_ARG, "curve %u: path index out of range", i);
-        if (i > 0 && s->curve_path_idx[i] < s->curve_path_idx[i - 1])
-            return fail(SR_ERR_INVALID_ARG, "curves must be grouped by path in path order");
-    }
-    for (uint32_t i = 0; i < V; ++i)
-        if (s->pos_path_idx[i] >= P) return fail(SR_ERR_INVALID_ARG, "point %u: path index out of range", i);
-    for (uint32_t i = 0; i < P; ++i)
-        if (s->fill_rule[i] > 1u) return fail(SR_ERR_INVALID_ARG, "path %u: fill rule %u", i, s->fill_rule[i]);
-    CUDA_TRY(cudaSetDevice(c->device));
-    CUDA_TRY(ensure(c->pos, sizeof(float) * 2 * (size_t)std::max<uint32_t>(V, 1)));
-    CUDA_TRY(ensure(c->pos_path, sizeof(uint32_t) * std::max<uint32_t>(V, 1)));
-    CUDA_TRY(ensure(c->curve_pos, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
-    CUDA_TRY(ensure(c->curve_type, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
-    CUDA_TRY(ensure(c->curve_path, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
-    CUDA_TRY(ensure(c->fill_rule, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
-    CUDA_TRY(ensure(c->fill_info, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
-    if (V) {
-        CUDA_TRY(cudaMemcpy(c->pos.p, s->position, sizeof(float) * 2 * (size_t)V, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(c->pos_path.p, s->pos_path_idx, sizeof(uint32_t) * V, cudaMemcpyHostToDevice));
-    }
-    if (C) {
-        CUDA_TRY(cudaMemcpy(c->curve_pos.p, s->curve_pos_map, sizeof(uint32_t) * C, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(c->curve_type.p, s->curve_type, sizeof(uint32_t) * C, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(c->curve_path.p, s->curve_path_idx, sizeof(uint32_t) * C, cudaMemcpyHostToDevice));
-    }
-    if (P) {
-        CUDA_TRY(cudaMemcpy(c->fill_rule.p, s->fill_rule, sizeof(uint32_t) * P, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(c->fill_info.p, s->fill_info, sizeof(uint32_t) * P, cudaMemcpyHostToDevice));
-    }
-    c->V = V;
-    c->C = C;
-    c->P = P;
-    c->loaded = true;
-    c->stages_valid = false;
-    return SR_OK;
+    SR_TRY(validate_scene(s));
+    c->h.clear();
+    append_scene(c->h, (uint32_t)c->W, (uint32_t)c->H, s, c->mvp);
+    return c->p.upload(c->h);
 }
 
 sr_status sr_set_mvp(sr_ctx* c, const float m[16]) {
     if (!c || !m) return fail(SR_ERR_INVALID_ARG, "NULL argument");
-    std::memcpy(c->mvp.m, m, sizeof(float) * 16);
+    std::memcpy(c->mvp, m, sizeof(float) * 16);
+    if (c->p.loaded) {
+        std::memcpy(c->p.info[0].mvp, m, sizeof(float) * 16);
+        CUDA_TRY(cudaSetDevice(c->p.device));
+        return c->p.upload_table();
+    }
     return SR_OK;
 }
 
 sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) {
     if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
-    if (!c->loaded) return fail(SR_ERR_NO_SCENE, "sr_render before sr_load_scene");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    c->stages_valid = false;
-    sr_status s = render_frame(c, st);
-    if (s != SR_OK) return s;
+    SR_TRY(c->p.frame(st, -1));
     if (rgba_out) {
         size_t bytes = (size_t)c->W * c->H * 4;
-        CUDA_TRY(cudaMemcpyAsync(rgba_out, c->image.p, bytes,
+        CUDA_TRY(cudaMemcpyAsync(rgba_out, c->p.image.p, bytes,
                                  out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
     }
-    if (!out_is_device || !rgba_out) {
-        CUDA_TRY(cudaMemcpyAsync(&c->h_n[1], c->ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        return check_status_word((uint32_t)c->h_n[1]);
-    }
-    return SR_OK;
+    return c->p.finish(st);
 }
 
 sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void* rgba_out, int out_is_device,
@@ -497,99 +710,97 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
     if (n < 0 || n >= (1ll << 30) || (n > 0 && !records)) return fail(SR_ERR_INVALID_ARG, "bad draw list");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    CUDA_TRY(cudaSetDevice(c->device));
-    const int32_t rows = (c->H + c->F - 1) / c->F;
+    Pipeline& p = c->p;
+    CUDA_TRY(cudaSetDevice(p.device));
+    if (!p.loaded || p.S != 1) {
+        // a canvas with no scene: the draw list alone decides the pixels
+        c->h.clear();
+        sr_scene_view empty{};
+        append_scene(c->h, (uint32_t)c->W, (uint32_t)c->H, &empty, c->mvp);
+        SR_TRY(p.upload(c->h));
+    }
+    const int32_t rows = (int32_t)p.total_rows;
     const size_t n1 = (size_t)std::max<int64_t>(n, 1);
     std::vector<uint32_t> row((size_t)n);
     for (int64_t i = 0; i < n; ++i) {
         int32_t y = records[4 * i] >> 16;
-        row[(size_t)i] = (y < 0 || y >= c->H) ? (uint32_t)rows : (uint32_t)(y / c->F);
+        row[(size_t)i] = (y < 0 || y >= c->H) ? (uint32_t)rows : (uint32_t)(y / p.F);
     }
-    CUDA_TRY(ensure(c->draw, sizeof(int4) * n1));
-    CUDA_TRY(ensure(c->draw_row, sizeof(uint32_t) * n1));
-    CUDA_TRY(ensure(c->ctl, sizeof(uint32_t) * CTL_WORDS));
-    CUDA_TRY(ensure(c->rkeys, sizeof(uint32_t) * n1));
-    CUDA_TRY(ensure(c->rvals, sizeof(uint32_t) * n1));
-    CUDA_TRY(ensure(c->rkeys_alt, sizeof(uint32_t) * n1));
-    CUDA_TRY(ensure(c->rvals_alt, sizeof(uint32_t) * n1));
-    CUDA_TRY(ensure(c->row_start, sizeof(int32_t) * ((size_t)rows + 1)));
-    CUDA_TRY(cudaMemsetAsync(c->ctl.p, 0, sizeof(uint32_t) * CTL_WORDS, st));
+    CUDA_TRY(ensure(p.draw, sizeof(int4) * n1));
+    CUDA_TRY(ensure(p.draw_row, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(p.rkeys, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(p.rvals, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(p.rkeys_alt, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(p.rvals_alt, sizeof(uint32_t) * n1));
+    CUDA_TRY(ensure(p.row_start, sizeof(int32_t) * ((size_t)rows + 1)));
+    CUDA_TRY(cudaMemsetAsync(p.ctl.p, 0, sizeof(uint32_t) * CTL_WORDS, st));
     if (n) {
-        CUDA_TRY(cudaMemcpyAsync(c->draw.p, records, sizeof(int4) * (size_t)n, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(cudaMemcpyAsync(c->draw_row.p, row.data(), sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(p.draw.p, records, sizeof(int4) * (size_t)n, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(p.draw_row.p, row.data(), sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
     }
     sr::SortPlan rp = sr::sort_plan(n, bits_for((uint64_t)rows));
-    CUDA_TRY(ensure(c->row_sort_scratch, sr::sort_scratch_bytes(rp)));
-    uint32_t* status = c->ctl.as<uint32_t>() + CTL_STATUS;
-    sr::launch_sort_u32(rp, c->draw_row.as<uint32_t>(), nullptr, c->rkeys.as<uint32_t>(), c->rvals.as<uint32_t>(),
-                        c->rkeys_alt.as<uint32_t>(), c->rvals_alt.as<uint32_t>(), c->row_sort_scratch.p, status, st);
-    sr::launch_row_bounds(c->rkeys.as<uint32_t>(), n, rows, c->row_start.as<int32_t>(), st);
+    CUDA_TRY(ensure(p.row_sort_scratch, sr::sort_scratch_bytes(rp)));
+    uint32_t* status = p.ctl.as<uint32_t>() + CTL_STATUS;
+    sr::launch_sort_u32(rp, p.draw_row.as<uint32_t>(), nullptr, p.rkeys.as<uint32_t>(), p.rvals.as<uint32_t>(),
+                        p.rkeys_alt.as<uint32_t>(), p.rvals_alt.as<uint32_t>(), p.row_sort_scratch.p, status, st);
+    sr::launch_row_bounds(p.rkeys.as<uint32_t>(), n, nullptr, rows, p.row_start.as<int32_t>(), st);
     sr::ResolveArgs ra;
-    ra.draw = c->draw.as<int4>();
-    ra.row_sorted_idx = c->rvals.as<uint32_t>();
-    ra.row_start = c->row_start.as<int32_t>();
-    ra.W = c->W;
-    ra.H = c->H;
-    ra.F = c->F;
-    ra.pixel_mode = c->mode == SR_MODE_PIXEL;
-    ra.image = c->image.as<uint32_t>();
-    sr::launch_resolve(ra, st);
+    ra.draw = p.draw.as<int4>();
+    ra.row_sorted_idx = p.rvals.as<uint32_t>();
+    ra.row_start = p.row_start.as<int32_t>();
+    ra.cta_base = p.cta_base_d.as<uint32_t>();
+    ra.scenes = p.scenes_d.as<sr::SceneInfo>();
+    ra.n_scenes = p.S;
+    ra.F = p.F;
+    ra.pixel_mode = p.mode == SR_MODE_PIXEL;
+    ra.image = p.image.as<uint32_t>();
+    sr::launch_resolve(ra, p.res_ctas, st);
     CUDA_TRY(cudaGetLastError());
-    c->last_O = n;
+    p.last_O = n;
     if (rgba_out) {
-        CUDA_TRY(cudaMemcpyAsync(rgba_out, c->image.p, (size_t)c->W * c->H * 4,
+        CUDA_TRY(cudaMemcpyAsync(rgba_out, p.image.p, (size_t)c->W * c->H * 4,
                                  out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
     }
-    if (!out_is_device || !rgba_out) {
-        CUDA_TRY(cudaMemcpyAsync(&c->h_n[1], status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        return check_status_word((uint32_t)c->h_n[1]);
-    }
-    return SR_OK;
+    CUDA_TRY(cudaMemcpyAsync(&p.h_u32[1], status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return check_status_word(p.h_u32[1]);
 }
 
 sr_status sr_get_stats(const sr_ctx* cc, sr_stats* out) {
     if (!cc || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     sr_ctx* c = const_cast<sr_ctx*>(cc);
-    if (c->ev_pending) {
-        CUDA_TRY(cudaEventSynchronize(c->ev[2 * ST_RESOLVE + 1]));
-        for (int s = 0; s < ST_COUNT_ALL; ++s) {
-            float ms = 0.f;
-            if (c->ev[2 * s] && c->ev[2 * s + 1]) CUDA_TRY(cudaEventElapsedTime(&ms, c->ev[2 * s], c->ev[2 * s + 1]));
-            c->stats.stage_ms[s] = ms;
-        }
-        c->ev_pending = false;
-    }
-    *out = c->stats;
+    SR_TRY(c->p.collect_events());
+    *out = c->p.stats;
     return SR_OK;
 }
 
 sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
     if (!c || !bytes) return fail(SR_ERR_INVALID_ARG, "NULL argument");
-    const size_t N = (size_t)c->last_N, O = (size_t)c->last_O;
+    Pipeline& p = c->p;
+    const size_t N = (size_t)p.last_N, O = (size_t)p.last_O;
     const void* src = nullptr;
     size_t need = 0;
     bool need_stages = true;
     switch (stage) {
-        case SR_STAGE_TRANSFORMED_POS: src = c->tpos.p; need = 8 * (size_t)c->V; need_stages = false; break;
-        case SR_STAGE_PATH_VISIBLE: src = c->path_visible.p; need = 4 * (size_t)c->P; need_stages = false; break;
-        case SR_STAGE_CUTPOINTS: src = c->cut.p; need = 20 * (size_t)c->C; need_stages = false; break;
-        case SR_STAGE_CURVE_COUNT: src = c->count.p; need = 4 * (size_t)c->C; need_stages = false; break;
-        case SR_STAGE_CURVE_OFFSET: src = c->offs.p; need = 4 * ((size_t)c->C + 1); need_stages = false; break;
-        case SR_STAGE_INTERSECTION: src = c->rec.p; need = 8 * N; need_stages = false; break;
-        case SR_STAGE_FRAG_KEY: src = c->d_fkey.p; need = 4 * N; break;
-        case SR_STAGE_FRAG_WINDING: src = c->d_fwn.p; need = 4 * N; break;
-        case SR_STAGE_FRAG_LEFT: src = c->d_fleft.p; need = 4 * N; break;
-        case SR_STAGE_SORTED_KEY: src = c->d_skey.p; need = 4 * N; break;
-        case SR_STAGE_SORTED_INDEX: src = c->svals.p; need = 4 * N; need_stages = false; break;
-        case SR_STAGE_WINDING_SCAN: src = c->d_wscan.p; need = 4 * (N + 1); break;
-        case SR_STAGE_FRAG_FLAG: src = c->d_fflag.p; need = 4 * N; break;
-        case SR_STAGE_SPAN_FLAG: src = c->d_sflag.p; need = 4 * N; break;
-        case SR_STAGE_DRAW_LIST: src = c->draw.p; need = 16 * O; need_stages = false; break;
-        case SR_STAGE_IMAGE: src = c->image.p; need = (size_t)c->W * c->H * 4; need_stages = false; break;
+        case SR_STAGE_TRANSFORMED_POS: src = p.tpos.p; need = 8 * (size_t)p.V; need_stages = false; break;
+        case SR_STAGE_PATH_VISIBLE: src = p.path_visible.p; need = 4 * (size_t)p.P; need_stages = false; break;
+        case SR_STAGE_CUTPOINTS: src = p.cut.p; need = 20 * (size_t)p.C; need_stages = false; break;
+        case SR_STAGE_CURVE_COUNT: src = p.count.p; need = 4 * (size_t)p.C; need_stages = false; break;
+        case SR_STAGE_CURVE_OFFSET: src = p.offs.p; need = 4 * ((size_t)p.C + 1); need_stages = false; break;
+        case SR_STAGE_INTERSECTION: src = p.rec.p; need = 8 * N; need_stages = false; break;
+        case SR_STAGE_FRAG_KEY: src = p.d_fkey.p; need = 4 * N; break;
+        case SR_STAGE_FRAG_WINDING: src = p.d_fwn.p; need = 4 * N; break;
+        case SR_STAGE_FRAG_LEFT: src = p.d_fleft.p; need = 4 * N; break;
+        case SR_STAGE_SORTED_KEY: src = p.d_skey.p; need = 4 * N; break;
+        case SR_STAGE_SORTED_INDEX: src = p.svals.p; need = 4 * N; need_stages = false; break;
+        case SR_STAGE_WINDING_SCAN: src = p.d_wscan.p; need = 4 * (N + 1); break;
+        case SR_STAGE_FRAG_FLAG: src = p.d_fflag.p; need = 4 * N; break;
+        case SR_STAGE_SPAN_FLAG: src = p.d_sflag.p; need = 4 * N; break;
+        case SR_STAGE_DRAW_LIST: src = p.draw.p; need = 16 * O; need_stages = false; break;
+        case SR_STAGE_IMAGE: src = p.image.p; need = (size_t)c->W * c->H * 4; need_stages = false; break;
         default: return fail(SR_ERR_INVALID_ARG, "unknown stage %d", stage);
     }
-    if (need_stages && !c->stages_valid)
+    if (need_stages && !p.stages_valid)
         return fail(SR_ERR_INVALID_ARG, "stage %d needs a render with SR_FLAG_KEEP_STAGES", stage);
     if (!dst) {
         *bytes = need;
@@ -597,7 +808,7 @@ sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
     }
     if (*bytes < need) return fail(SR_ERR_INVALID_ARG, "buffer of %zu bytes, need %zu", *bytes, need);
     if (need && !src) return fail(SR_ERR_INVALID_ARG, "stage %d not available", stage);
-    CUDA_TRY(cudaSetDevice(c->device));
+    CUDA_TRY(cudaSetDevice(p.device));
     if (need) CUDA_TRY(cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost));
     *bytes = need;
     return SR_OK;
@@ -630,9 +841,224 @@ sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, 
 
 void sr_destroy(sr_ctx* c) {
     if (!c) return;
-    cudaSetDevice(c->device);
+    cudaSetDevice(c->p.device);
     cudaDeviceSynchronize();
     delete c;
+}
+
+// ------------------------------------------------------------- batches ---
+
+sr_status sr_batch_create(const sr_options* opt, sr_batch** out) {
+    if (!out) return fail(SR_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    sr_options o{};
+    o.struct_size = sizeof(sr_options);
+    o.mode = SR_MODE_PIXEL;
+    if (opt) {
+        if (opt->struct_size < sizeof(sr_options)) return fail(SR_ERR_INVALID_ARG, "sr_options.struct_size too small");
+        o = *opt;
+    }
+    if (o.mode != SR_MODE_REFERENCE && o.mode != SR_MODE_PIXEL) return fail(SR_ERR_INVALID_ARG, "unknown mode %d", o.mode);
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (o.device < 0 || o.device >= ndev) return fail(SR_ERR_INVALID_ARG, "device %d not present", o.device);
+    sr_batch* b = new sr_batch();
+    sr_status s = b->p.init(o.device, o.mode, o.flags & ~SR_FLAG_KEEP_STAGES);
+    if (s != SR_OK) {
+        delete b;
+        return s;
+    }
+    *out = b;
+    return SR_OK;
+}
+
+sr_status sr_batch_add_scene(sr_batch* b, uint32_t width, uint32_t height, const sr_scene_view* s, const float* mvp,
+                             uint32_t* index) {
+    if (!b || !s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (width == 0 || height == 0 || width > 16384 || height > 16384)
+        return fail(SR_ERR_INVALID_ARG, "canvas %ux%u outside 1..16384", width, height);
+    SR_TRY(validate_scene(s));
+    if ((uint64_t)b->h.n_paths() + s->n_paths > (1u << 26) || (uint64_t)b->h.n_curves() + s->n_curves > (1u << 27))
+        return fail(SR_ERR_INVALID_ARG, "batch too large");
+    if (index) *index = (uint32_t)b->h.info.size();
+    append_scene(b->h, width, height, s, mvp);
+    b->committed = false;
+    return SR_OK;
+}
+
+sr_status sr_batch_add_synth(sr_batch* b, const sr_synth_params* prm, uint32_t count, uint32_t* first_index) {
+    if (!b || !prm) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (prm->struct_size < sizeof(sr_synth_params) || prm->preset < 0 || prm->preset > 2)
+        return fail(SR_ERR_INVALID_ARG, "bad synth parameters");
+    // generate in parallel, append in order
+    std::vector<srsynth::Scene> sc(count);
+    unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), count));
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+        for (uint32_t i = next.fetch_add(1); i < count; i = next.fetch_add(1)) {
+            srsynth::Params q;
+            q.preset = prm->preset;
+            q.seed = prm->seed;
+            q.scene_index = prm->scene_index + i;
+            q.width = prm->width;
+            q.height = prm->height;
+            q.n_paths = prm->n_paths;
+            srsynth::generate(q, sc[i]);
+        }
+    };
+    std::vector<std::thread> ts;
+    for (unsigned t = 1; t < nt; ++t) ts.emplace_back(work);
+    work();
+    for (auto& t : ts) t.join();
+    if (first_index) *first_index = (uint32_t)b->h.info.size();
+    for (uint32_t i = 0; i < count; ++i) {
+        const srsynth::Scene& s = sc[i];
+        sr_scene_view v{s.n_points(), s.n_curves(), s.n_paths(), s.pos.data(), s.pos_path.data(), s.curve_pos.data(),
+                        s.curve_type.data(), s.curve_path.data(), s.fill_rule.data(), s.fill_info.data()};
+        append_scene(b->h, s.width, s.height, &v, nullptr);
+    }
+    b->committed = false;
+    return SR_OK;
+}
+
+sr_status sr_batch_commit(sr_batch* b) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    SR_TRY(b->p.upload(b->h));
+    b->committed = true;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->graph_cap = -1;
+    return SR_OK;
+}
+
+sr_status sr_batch_set_mvp(sr_batch* b, uint32_t index, const float m[16]) {
+    if (!b || !m || index >= b->h.info.size()) return fail(SR_ERR_INVALID_ARG, "bad argument");
+    std::memcpy(b->h.info[index].mvp, m, sizeof(float) * 16);
+    if (b->committed) {
+        std::memcpy(b->p.info[index].mvp, m, sizeof(float) * 16);
+        CUDA_TRY(cudaSetDevice(b->p.device));
+        return b->p.upload_table();
+    }
+    return SR_OK;
+}
+
+sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* o, void* stream) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    sr_batch_render_opts d{};
+    d.struct_size = sizeof(d);
+    d.record_capacity = -1;
+    if (o) {
+        if (o->struct_size < sizeof(sr_batch_render_opts)) return fail(SR_ERR_INVALID_ARG, "opts.struct_size too small");
+        d = *o;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Pipeline& p = b->p;
+    CUDA_TRY(cudaSetDevice(p.device));
+    const int64_t cap = d.record_capacity;
+    if (cap >= 0 && d.use_graph) {
+        if (!b->exec || b->graph_cap != cap) {
+            if (b->exec) cudaGraphExecDestroy(b->exec);
+            if (b->graph) cudaGraphDestroy(b->graph);
+            b->exec = nullptr;
+            b->graph = nullptr;
+            // one plain frame first: it allocates every buffer and sets the
+            // kernels' attributes, so the capture records launches only
+            SR_TRY(p.frame(st, cap));
+            sr_status fs = p.finish(st);
+            if (fs != SR_OK && fs != SR_ERR_OVERFLOW_REFIT) return fs;
+            if (!b->cap_stream) CUDA_TRY(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            const uint64_t l0 = sr::launches_so_far();
+            cudaStream_t cs = b->cap_stream;
+            p.capturing = true;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            sr_status s1 = SR_OK, s2 = SR_OK;
+            if (e == cudaSuccess) {
+                s1 = p.enqueue_front(cs);
+                if (s1 == SR_OK) s2 = p.enqueue_back(cs, cap);
+                cudaError_t e2 = cudaStreamEndCapture(cs, &b->graph);   // always end the capture
+                if (e2 != cudaSuccess) e = e2;
+            }
+            p.capturing = false;
+            SR_TRY(s1);
+            SR_TRY(s2);
+            CUDA_TRY(e);
+            CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+            b->graph_cap = cap;
+            b->graph_launches = (uint32_t)(sr::launches_so_far() - l0);
+        }
+        CUDA_TRY(cudaGraphLaunch(b->exec, st));
+        p.last_cap = cap;
+        p.stats.kernel_launches = b->graph_launches;
+        p.ev_pending = false;
+    } else {
+        SR_TRY(p.frame(st, cap));
+    }
+    sr_status s = p.finish(st);
+    if (s == SR_ERR_OVERFLOW_REFIT && d.refit_on_overflow) {
+        ++b->overflows;
+        ++b->refits;
+        SR_TRY(p.frame(st, -1));   // the exact count pass
+        s = p.finish(st);
+    } else if (s == SR_ERR_OVERFLOW_REFIT) {
+        ++b->overflows;
+    }
+    return s;
+}
+
+sr_status sr_batch_get_image(sr_batch* b, uint32_t index, void* rgba_out, int out_is_device, void* stream) {
+    if (!b || !rgba_out || index >= b->p.S) return fail(SR_ERR_INVALID_ARG, "bad argument");
+    const sr::SceneInfo& si = b->p.info[index];
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaSetDevice(b->p.device));
+    CUDA_TRY(cudaMemcpyAsync(rgba_out, b->p.image.as<uint32_t>() + si.image_off, (size_t)si.W * si.H * 4,
+                             out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (!out_is_device) CUDA_TRY(cudaStreamSynchronize(st));
+    return SR_OK;
+}
+
+sr_status sr_batch_info(const sr_batch* b, uint32_t index, uint32_t* width, uint32_t* height) {
+    if (!b || index >= b->h.info.size()) return fail(SR_ERR_INVALID_ARG, "bad argument");
+    if (width) *width = (uint32_t)b->h.info[index].W;
+    if (height) *height = (uint32_t)b->h.info[index].H;
+    return SR_OK;
+}
+
+sr_status sr_batch_get_stats(const sr_batch* cb, sr_batch_stats* out) {
+    if (!cb || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    sr_batch* b = const_cast<sr_batch*>(cb);
+    SR_TRY(b->p.collect_events());
+    std::memset(out, 0, sizeof *out);
+    out->frame = b->p.stats;
+    out->n_scenes = (uint32_t)b->h.info.size();
+    out->n_paths = b->h.n_paths();
+    out->n_curves = b->h.n_curves();
+    out->record_capacity = b->p.last_cap;
+    out->overflows = b->overflows;
+    out->refits = b->refits;
+    out->graph_captured = b->exec != nullptr;
+    return SR_OK;
+}
+
+sr_status sr_batch_clear(sr_batch* b) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    b->h.clear();
+    b->committed = false;
+    return SR_OK;
+}
+
+void sr_batch_destroy(sr_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->p.device);
+    cudaDeviceSynchronize();
+    delete b;
 }
 
 }  // extern "C"

@@ -17,7 +17,7 @@ namespace sr {
 // are grouped by path) before one atomicOr per run.
 __global__ void __launch_bounds__(256) k_transform(const float2* __restrict__ pos,
                                                    const uint32_t* __restrict__ pos_path, uint32_t n_points,
-                                                   Mvp M, float fw, float fh, float2* __restrict__ tpos,
+                                                   const SceneTable t, float2* __restrict__ tpos,
                                                    int32_t* __restrict__ path_visible) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t lane = lane_id();
@@ -25,14 +25,17 @@ __global__ void __launch_bounds__(256) k_transform(const float2* __restrict__ po
     int32_t v = 0;
     if (i < n_points) {
         float2 p = pos[i];
+        pidx = pos_path[i];
+        const SceneInfo& si = scene_of_path(t, pidx);
+        const float fw = (float)si.W, fh = (float)si.H;
         float o[4];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             // dot((x, y, 0, 1), m_r) summed left to right
-            float acc = __fmul_rn(p.x, M.m[4 * r + 0]);
-            acc = __fadd_rn(acc, __fmul_rn(p.y, M.m[4 * r + 1]));
-            acc = __fadd_rn(acc, __fmul_rn(0.0f, M.m[4 * r + 2]));
-            acc = __fadd_rn(acc, __fmul_rn(1.0f, M.m[4 * r + 3]));
+            float acc = __fmul_rn(p.x, si.mvp[4 * r + 0]);
+            acc = __fadd_rn(acc, __fmul_rn(p.y, si.mvp[4 * r + 1]));
+            acc = __fadd_rn(acc, __fmul_rn(0.0f, si.mvp[4 * r + 2]));
+            acc = __fadd_rn(acc, __fmul_rn(1.0f, si.mvp[4 * r + 3]));
             o[r] = acc;
         }
         float ox = __fdiv_rn(o[0], o[3]);
@@ -52,7 +55,6 @@ __global__ void __launch_bounds__(256) k_transform(const float2* __restrict__ po
             case 0x22: v = 0x00000001; break;
             default: break;
         }
-        pidx = pos_path[i];
     }
     // segmented OR-scan over runs of equal pidx
 #pragma unroll
@@ -133,11 +135,17 @@ SR_DEV uint32_t pack_n(int32_t nx, bool xneg, int32_t ny, bool yneg) {
 SR_DEV int32_t piece_nx(uint32_t n) { return (int32_t)(n & 0x7FFFu); }
 SR_DEV int32_t piece_ny(uint32_t n) { return (int32_t)((n >> 16) & 0x7FFFu); }
 
-// Chain buckets by length, longest first, so that the longest dependency
-// chains start in the first wave of k_chains.
-SR_DEV uint32_t chain_bucket(int32_t len) {
-    return len >= 1024 ? 0u : (len >= 256 ? 1u : (len >= 32 ? 2u : 3u));
+// Sort key of a chain: longest length class first (so the longest dependency
+// chains start in the first wave of k_chains), then cubic, quadric, line, so
+// that a warp runs one curve type with lengths within a factor of 2.
+SR_DEV uint32_t chain_key(int32_t len, uint32_t type) {
+    uint32_t lg = 31u - (uint32_t)__clz(len);
+    if (lg > 14u) lg = 14u;
+    uint32_t cls = type == 4u ? 0u : (type == 3u ? 1u : 2u);
+    return ((14u - lg) << 2) | cls;
 }
+SR_DEV bool chain_key_long(uint32_t key) { return (key >> 2) <= 14u - 5u; }   // >= 32 crossings
+constexpr uint32_t kChainKeyBits = 6;
 
 // get_xy_begin_end_delta + udpate_cut_range for one axis
 // (make_intersection_1.comp:150-213): number of grid crossings, first
@@ -163,23 +171,27 @@ SR_DEV int32_t axis_range_rd(float a0, float a1, int32_t size, int32_t F, float&
 // make_intersection_0.comp:226-411.  One thread per curve: path cull,
 // monotonic cut points (cached, 5 floats per curve), the number of records
 // the curve emits (the reference's count), and the set-up of each piece's
-// x and y crossing chains, which are appended to length buckets.
+// x and y crossing chains, which are appended with their sort keys.
 __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restrict__ cut_cache,
                                                int32_t* __restrict__ count, uint4* __restrict__ pieces,
-                                               uint32_t* __restrict__ chain_lists, uint32_t list_cap,
-                                               uint32_t* __restrict__ bucket_count, uint32_t* __restrict__ long_list,
-                                               uint32_t* __restrict__ long_count, uint32_t* __restrict__ status) {
+                                               uint32_t* __restrict__ chain_items, uint32_t* __restrict__ chain_keys,
+                                               uint32_t list_cap, uint32_t* __restrict__ chain_count,
+                                               uint32_t* __restrict__ long_list, uint32_t* __restrict__ long_count,
+                                               uint32_t* __restrict__ status) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = c < g.n_curves;
     uint32_t my_chains[2 * kMaxPieces];
-    uint32_t my_bucket[2 * kMaxPieces];
+    uint32_t my_key[2 * kMaxPieces];
     int n_chains = 0;
     uint32_t long_mask = 0;   // pieces merged by k_merge_long
     if (active) {
         uint32_t type = g.curve_type[c];
         CurvePts P;
         load_curve(g.tpos, g.curve_pos[c], type, P);
-        bool vis = path_visible_mask(g.path_visible[g.curve_path[c]]);
+        const uint32_t path = g.curve_path[c];
+        bool vis = path_visible_mask(g.path_visible[path]);
+        const SceneInfo& si = scene_of_path(g.st, path);
+        const int32_t W = si.W, H = si.H;
         const int32_t F = g.F;
         uint32_t n = 0;
         float q[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -265,24 +277,24 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
                 yb = wadd(f2i(__fmul_rn(floorf(__fdiv_rn(y1, fF)), fF)), F);
                 ye = f2i(__fmul_rn(floorf(__fdiv_rn(y0, fF)), fF));
             }
-            int32_t nxc = cut_range(g.W, F, xb, xe);
-            int32_t nyc = cut_range(g.H, F, yb, ye);
+            int32_t nxc = cut_range(W, F, xb, xe);
+            int32_t nyc = cut_range(H, F, yb, ye);
             pc = wadd(pc, wadd(1, wadd(nxc, nyc)));
             // chain set-up: the intersection pass's own range formulas
             float sx, sy;
             bool xneg, yneg;
-            int32_t nx = axis_range_rd(x0, x1, g.W, F, sx, xneg);
-            int32_t ny = axis_range_rd(y0, y1, g.H, F, sy, yneg);
+            int32_t nx = axis_range_rd(x0, x1, W, F, sx, xneg);
+            int32_t ny = axis_range_rd(y0, y1, H, F, sy, yneg);
             int32_t tb = fbits(t1) & ~3;
             tb |= (floorf(x1) == x1) ? 2 : 3;   // make_intersection_1.comp:271-276
             pt[i] = make_uint4(pack_n(nx, xneg, ny, yneg), (uint32_t)tb, __float_as_uint(sx), __float_as_uint(sy));
             if (nx > 0) {
                 my_chains[n_chains] = (c << 4) | (i << 1) | 0u;
-                my_bucket[n_chains++] = chain_bucket(nx);
+                my_key[n_chains++] = chain_key(nx, type);
             }
             if (ny > 0) {
                 my_chains[n_chains] = (c << 4) | (i << 1) | 1u;
-                my_bucket[n_chains++] = chain_bucket(ny);
+                my_key[n_chains++] = chain_key(ny, type);
             }
             walk += 1 + nx + ny;
             if (1 + nx + ny >= kLongPiece) long_mask |= 1u << i;
@@ -308,20 +320,23 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
             else set_error(status, ERR_CAPACITY);
         }
     }
-    // append chains to their buckets (warp-aggregated per bucket)
+    // append the chains with their sort keys (warp-aggregated)
     for (int k = 0; k < 2 * kMaxPieces; ++k) {
         bool has = k < n_chains;
-        if (!__any_sync(0xFFFFFFFFu, has)) break;
-        uint32_t b = has ? my_bucket[k] : 4u;
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, b);
-        uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        uint32_t m = __ballot_sync(0xFFFFFFFFu, has);
+        if (!m) break;
+        uint32_t leader = (uint32_t)(__ffs(m) - 1);
         uint32_t base = 0;
-        if (has && lane == leader) base = atomicAdd(&bucket_count[b], (uint32_t)__popc(peers));
+        if (lane == leader) base = atomicAdd(chain_count, (uint32_t)__popc(m));
         base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (has) {
-            uint32_t slot = base + (uint32_t)__popc(peers & lanemask_lt());
-            if (slot < list_cap) chain_lists[(size_t)b * list_cap + slot] = my_chains[k];
-            else set_error(status, ERR_CAPACITY);
+            uint32_t slot = base + (uint32_t)__popc(m & lanemask_lt());
+            if (slot < list_cap) {
+                chain_items[slot] = my_chains[k];
+                chain_keys[slot] = my_key[k];
+            } else {
+                set_error(status, ERR_CAPACITY);
+            }
         }
     }
 }
@@ -424,21 +439,22 @@ SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t
 
 __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t* __restrict__ offs,
                                                 const uint4* __restrict__ pieces,
-                                                const uint32_t* __restrict__ chain_lists, uint32_t list_cap,
-                                                const uint32_t* __restrict__ bucket_count,
-                                                int32_t* __restrict__ cbuf) {
-    uint32_t nb[4];
-    uint32_t total = 0;
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        nb[b] = imin((int32_t)bucket_count[b], (int32_t)list_cap);
-        total += nb[b];
-    }
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += stride) {
-        uint32_t b = 0, r = it;
-        while (b < 3 && r >= nb[b]) { r -= nb[b]; ++b; }
-        uint32_t item = chain_lists[(size_t)b * list_cap + r];
+                                                const uint32_t* __restrict__ items, const uint32_t* __restrict__ keys,
+                                                uint32_t list_cap, const uint32_t* __restrict__ chain_count,
+                                                uint32_t* __restrict__ queue, int32_t* __restrict__ cbuf) {
+    const uint32_t total = imin((int32_t)*chain_count, (int32_t)list_cap);
+    const uint32_t lane = lane_id();
+    // warps take groups of 32 chains in list order, so the longest groups go
+    // to the first warp of every SM rather than to one block
+    for (;;) {
+        uint32_t grp = 0;
+        if (lane == 0) grp = atomicAdd(queue, 1u);
+        grp = __shfl_sync(0xFFFFFFFFu, grp, 0);
+        const uint32_t it = grp * 32u + lane;
+        if (grp * 32u >= total) break;
+        if (it >= total) continue;
+        uint32_t item = items[it];
+        const bool spec = chain_key_long(keys[it]);
         uint32_t c = item >> 4, piece = (item >> 1) & 7u;
         int side = (int)(item & 1u);
         uint32_t type = g.curve_type[c];
@@ -449,6 +465,7 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
         int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
         base += 1 + (side ? nx : 0);
         int32_t len = side ? ny : nx;
+        if (base + len > g.rec_cap) continue;   // overflow: k_merge reports it
         bool neg = side ? (me.x & 0x80000000u) != 0 : (me.x & 0x8000u) != 0;
         float x = __uint_as_float(side ? me.w : me.z);
         float dx = neg ? -(float)g.F : (float)g.F;
@@ -468,7 +485,6 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
         a.d12 = __fsub_rn(p[2], p[1]);
         a.d23 = __fsub_rn(p[3], p[2]);
         int32_t* out = cbuf + base;
-        const bool spec = b < 3;
         if (type == 2u) run_chain<2, false>(a, len, x, dx, t_lo, t_hi, side, out);
         else if (type == 3u) {
             if (spec) run_chain<3, true>(a, len, x, dx, t_lo, t_hi, side, out);
@@ -494,6 +510,10 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
     int64_t pc = offs[c];
     const int64_t end = offs[c + 1];
     if (pc >= end) return;
+    if (end > g.rec_cap) {
+        set_error(status, ERR_CAPACITY);
+        return;
+    }
     const uint4* pt = pieces + (size_t)c * kMaxPieces;
     const int32_t minus_one = fbits(-1.0f);
     const int32_t ex_x = fbits(2.0f), ex_y = fbits(2.0f) | 1;
@@ -588,6 +608,7 @@ __global__ void __launch_bounds__(256) k_merge_long(const GeomArgs g, const int3
         for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
         const int32_t nx = piece_nx(pt[piece].x), ny = piece_ny(pt[piece].x);
         const int32_t L = 1 + nx + ny;
+        if (base + L > g.rec_cap) continue;   // overflow: k_merge reports it
         const int32_t t0 = piece == 0 ? 0 : (int32_t)pt[piece - 1].y;
         const int32_t* X = cbuf + base + 1;
         const int32_t* Y = X + nx;
@@ -637,9 +658,10 @@ __global__ void __launch_bounds__(256) k_merge_long(const GeomArgs g, const int3
 // record's t and the next record's t (t = 1 when the next record belongs to
 // another curve), its cell, the 64-bit sort key, the winding change across
 // the sample row and (pixel mode) the part of it left of the cell centre.
-__global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* __restrict__ rec, int64_t n,
-                                                  uint64_t* __restrict__ keys, uint8_t* __restrict__ wnp,
-                                                  DebugOut dbg) {
+__global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* __restrict__ rec, int64_t n_cap,
+                                                  const uint32_t* __restrict__ n_dev, uint64_t* __restrict__ keys,
+                                                  uint8_t* __restrict__ wnp, DebugOut dbg) {
+    const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_cap) : n_cap;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int2 r0 = rec[i];
@@ -647,6 +669,13 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
     float t0 = gmax(bitsf(r0.y & ~3), 0.0f);
     float t1 = gmax(bitsf(r1.y & ~3), 0.0f);
     uint32_t c = (uint32_t)r0.x;
+    if (c >= g.n_curves) {
+        // only in a frame whose records overflowed their capacity (the
+        // frame is reported and discarded): never index with it
+        keys[i] = ~0ull;
+        wnp[i] = 0;
+        return;
+    }
     uint32_t path = g.curve_path[c];
     if (r0.x != r1.x) t1 = 1.0f;
     int32_t yx = (int32_t)0xFFFEFFFE, wn = 0, left = 0;
@@ -659,12 +688,13 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
         float pfx = interp(type, t0, P.x), pfy = interp(type, t0, P.y);
         float plx = interp(type, t1, P.x), ply = interp(type, t1, P.y);
         const int32_t F = g.F;
+        const SceneInfo& si = scene_of_path(g.st, path);
         const float invF = 1.0f / (float)F;   // exact: F is 1 or 2
         int32_t rx = wmul(float2int_rd(__fmul_rn(__fmul_rn(__fadd_rn(pfx, plx), 0.5f), invF)), F);
         int32_t ry = wmul(float2int_rd(__fmul_rn(__fmul_rn(__fadd_rn(pfy, ply), 0.5f), invF)), F);
-        pos_x = imin(imax(rx, -F), wadd(g.W & (int32_t)0xFFFFFFFE, F));
-        pos_y = imin(imax(ry, -F), wadd(g.H & (int32_t)0xFFFFFFFE, F));
-        if ((uint32_t)ry < (uint32_t)g.H) {
+        pos_x = imin(imax(rx, -F), wadd(si.W & (int32_t)0xFFFFFFFE, F));
+        pos_y = imin(imax(ry, -F), wadd(si.H & (int32_t)0xFFFFFFFE, F));
+        if ((uint32_t)ry < (uint32_t)si.H) {
             valid = true;
             yx = (int32_t)(((uint32_t)wadd(pos_y, 0x7FFF) << 16) | ((uint32_t)wadd(pos_x, 0x7FFF) & 0xFFFFu));
         }
@@ -690,11 +720,11 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
 }
 
 // -------------------------------------------------------------- launches --
-void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const Mvp& M, float fw,
-                      float fh, float2* tpos, int32_t* path_visible, cudaStream_t st) {
+void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const SceneTable& t,
+                      float2* tpos, int32_t* path_visible, cudaStream_t st) {
     if (n_points == 0) return;
     count_launches(1);
-    k_transform<<<(n_points + 255) / 256, 256, 0, st>>>(pos, pos_path, n_points, M, fw, fh, tpos, path_visible);
+    k_transform<<<(n_points + 255) / 256, 256, 0, st>>>(pos, pos_path, n_points, t, tpos, path_visible);
 }
 
 static int sm_count_hint() {
@@ -715,15 +745,18 @@ void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const Cha
                   cudaStream_t st) {
     if (g.n_curves == 0) return;
     count_launches(1);
-    k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count, w.pieces, w.chain_lists, w.list_cap,
-                                                      w.bucket_count, w.long_list, w.long_count, status);
+    k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count, w.pieces, w.chain_items, w.chain_keys,
+                                                      w.list_cap, w.chain_count, w.long_list, w.long_count, status);
 }
+
+uint32_t chain_key_bits() { return kChainKeyBits; }
 
 void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
                    cudaStream_t st) {
     if (g.n_curves == 0) return;
     count_launches(1);
-    k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.chain_lists, w.list_cap, w.bucket_count, cbuf);
+    k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
+                                            w.chain_count, w.chain_queue, cbuf);
 }
 
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
@@ -735,11 +768,11 @@ void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, in
                                                   cbuf, rec);
 }
 
-void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n, uint64_t* keys, uint8_t* wnp,
-                     const DebugOut& dbg, cudaStream_t st) {
-    if (n <= 0) return;
+void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n_cap, const uint32_t* n_dev, uint64_t* keys,
+                     uint8_t* wnp, const DebugOut& dbg, cudaStream_t st) {
+    if (n_cap <= 0) return;
     count_launches(1);
-    k_fragment<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rec, n, keys, wnp, dbg);
+    k_fragment<<<(unsigned)((n_cap + 255) / 256), 256, 0, st>>>(g, rec, n_cap, n_dev, keys, wnp, dbg);
 }
 
 }  // namespace sr

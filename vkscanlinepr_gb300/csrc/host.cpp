@@ -24,7 +24,7 @@ extern "C" const char* sr_host_last_error(void) { return g_host_err.c_str(); }
 extern "C" sr_status sr_synth_scene(const sr_synth_params* p, sr_scene_buf** out) {
     if (!p || !out) return SR_ERR_INVALID_ARG;
     if (p->struct_size < sizeof(sr_synth_params)) return SR_ERR_INVALID_ARG;
-    if (p->preset != 0 && p->preset != 1) return SR_ERR_INVALID_ARG;
+    if (p->preset < 0 || p->preset > 2) return SR_ERR_INVALID_ARG;
     srsynth::Params q;
     q.preset = p->preset;
     q.seed = p->seed;

@@ -17,7 +17,29 @@ struct Mvp {
     float m[16];   // rows m0..m3
 };
 
-// Scene + per-frame arrays the geometry kernels read.
+// One scene of a batch (device layout).  Paths of scene s are
+// [path_begin, path_end) in the batch's global path order; its cell rows
+// are [row_base, row_base + rows) of the batch's global row order; its
+// framebuffer starts at pixel image_off.
+struct SceneInfo {
+    int32_t W, H;
+    uint32_t path_begin, path_end;
+    uint32_t row_base, rows;
+    uint64_t image_off;
+    float mvp[16];
+};
+
+struct SceneTable {
+    const SceneInfo* scenes;
+    const uint32_t* path_scene;   // [n_paths] scene of each path
+    uint32_t n_scenes;
+};
+
+SR_DEV const SceneInfo& scene_of_path(const SceneTable& t, uint32_t path) { return t.scenes[t.path_scene[path]]; }
+
+// Scene + per-frame arrays the geometry kernels read.  W and H are the
+// largest canvas of the batch (key layout); each scene's own canvas comes
+// from the scene table.
 struct GeomArgs {
     uint32_t n_curves;
     const uint32_t* curve_type;
@@ -28,6 +50,8 @@ struct GeomArgs {
     int32_t W, H, F;
     int32_t pixel_mode;
     KeyLayout L;
+    SceneTable st;
+    int64_t rec_cap;   // capacity of the record buffers; larger counts are an overflow
 };
 
 // Optional reference-layout outputs for parity dumps (all NULL in production).
@@ -40,17 +64,22 @@ struct DebugOut {
 // Crossing-chain work of the intersection stage.
 struct ChainWork {
     uint4* pieces;            // [n_curves][5] per-piece chain set-up
-    uint32_t* chain_lists;    // [4][list_cap] chain ids by length bucket
+    uint32_t* chain_items;    // [list_cap] (curve << 4 | piece << 1 | side), append order
+    uint32_t* chain_keys;     // [list_cap] length-class / type sort key
+    uint32_t* sorted_items;   // [list_cap] the same, longest class first
+    uint32_t* sorted_keys;
     uint32_t list_cap;
-    uint32_t* bucket_count;   // [4] zeroed before the count pass
+    uint32_t* chain_count;    // [1] zeroed before the count pass
+    uint32_t* chain_queue;    // [1] zeroed before the chains
     uint32_t* long_list;      // [list_cap] (curve << 3 | piece) of long pieces
     uint32_t* long_count;     // [1] zeroed before the count pass
 };
 size_t piece_table_bytes(uint32_t n_curves);
+uint32_t chain_key_bits();
 uint32_t chain_list_capacity(uint32_t n_curves);
 
-void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const Mvp& M, float fw,
-                      float fh, float2* tpos, int32_t* path_visible, cudaStream_t st);
+void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const SceneTable& t,
+                      float2* tpos, int32_t* path_visible, cudaStream_t st);
 void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const ChainWork& w, uint32_t* status,
                   cudaStream_t st);
 // Crossing chains (longest first) then the per-curve merge into the
@@ -60,8 +89,9 @@ void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, i
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
                   uint32_t* status, cudaStream_t st);
 // One fragment per record: sort key + packed winding bits.
-void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n, uint64_t* keys, uint8_t* wnp,
-                     const DebugOut& dbg, cudaStream_t st);
+// n_cap launches the grid; the record count is read from n_dev (offs[C]).
+void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n_cap, const uint32_t* n_dev, uint64_t* keys,
+                     uint8_t* wnp, const DebugOut& dbg, cudaStream_t st);
 
 // ---- scan.cu
 // Exclusive scan of n int32 values into out[0..n] (out[n] = total), single
@@ -73,12 +103,13 @@ void launch_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, uint6
 
 // ---- sort.cu  (onesweep LSD radix sort, 8-bit digits)
 struct SortPlan {
-    int64_t n;
+    int64_t n;                 // element count, or the capacity when n_dev is set
+    const uint32_t* n_dev;     // optional device-side count (<= n), read by the kernels
     uint32_t key_bits;
     uint32_t passes;
     uint32_t tiles;
 };
-SortPlan sort_plan(int64_t n, uint32_t key_bits);
+SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev = nullptr);
 // Device scratch needed by a plan (bytes).
 size_t sort_scratch_bytes(const SortPlan& p);
 // Sorts (keys, values) stably by the low key_bits of the keys.  If
@@ -93,7 +124,8 @@ void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t*
 
 // ---- winding.cu
 struct WindArgs {
-    int64_t n;                      // N records (host copy)
+    int64_t n;                      // N records: the capacity when n_dev is set
+    const uint32_t* n_dev;          // device-side record count (offs[C])
     const uint64_t* skeys;          // sorted keys
     const uint32_t* svals;          // sorted record indices
     const uint8_t* wnp;             // packed winding bits by record index
@@ -103,11 +135,12 @@ struct WindArgs {
     int32_t W, H, F;
     int32_t pixel_mode;
     KeyLayout L;
+    SceneTable st;
     int4* draw;                     // [capacity] draw records
     int64_t draw_capacity;
-    uint32_t* draw_row;             // [capacity] cell row of each draw record
-    uint32_t* row_count;            // [rows] histogram of draw_row
+    uint32_t* draw_row;             // [capacity] global cell row of each draw record
     uint64_t* totals;               // [2] merged fragments, spans
+    uint32_t* n_draw;               // [1] merged fragments + spans
     // parity dumps (NULL in production)
     int32_t* dbg_wscan;             // [N+1]
     int32_t* dbg_fflag;             // [N]
@@ -119,15 +152,26 @@ void launch_winding_emit(const WindArgs& a, uint64_t* tile_status, uint32_t* til
                          cudaStream_t st);
 
 // ---- resolve.cu
+// Resolve work: each CTA paints rows_per_cta cell rows of one scene;
+// cta_base[s] is the first CTA of scene s (host-built, n_scenes+1 entries).
 struct ResolveArgs {
     const int4* draw;
-    const uint32_t* row_sorted_idx;   // draw indices sorted by cell row
-    const int32_t* row_start;         // [rows+1]
-    int32_t W, H, F;
+    const uint32_t* row_sorted_idx;   // draw indices sorted by global cell row
+    const int32_t* row_start;         // [total rows + 1]
+    const uint32_t* cta_base;         // [n_scenes + 1]
+    const SceneInfo* scenes;
+    uint32_t n_scenes;
+    int32_t F;
     int32_t pixel_mode;
-    uint32_t* image;                  // [W*H] RGBA8
+    uint32_t* image;                  // all scenes' RGBA8 framebuffers
 };
-void launch_resolve(const ResolveArgs& a, cudaStream_t st);
-void launch_row_bounds(const uint32_t* srows, int64_t n, int32_t rows, int32_t* row_start, cudaStream_t st);
+// Warps per resolve CTA and pixels per warp.
+constexpr int kResolveWarps = 16;
+constexpr int kResolveSeg = 256;
+uint32_t resolve_rows_per_cta(int32_t W);
+void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st);
+// n_dev (optional) holds the record count; n is the capacity.
+void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,
+                       cudaStream_t st);
 
 }  // namespace sr

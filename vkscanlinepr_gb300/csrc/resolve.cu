@@ -16,8 +16,9 @@
 namespace sr {
 
 // First index of every cell row in the row-sorted draw list.
-__global__ void k_row_bounds(const uint32_t* __restrict__ srows, int64_t n, int32_t rows,
-                             int32_t* __restrict__ row_start) {
+__global__ void k_row_bounds(const uint32_t* __restrict__ srows, int64_t n_cap, const uint32_t* __restrict__ n_dev,
+                             int32_t rows, int32_t* __restrict__ row_start) {
+    const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_cap) : n_cap;
     int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += stride) {
         int32_t cur = i < n ? (int32_t)srows[i] : rows;
@@ -36,14 +37,14 @@ __global__ void k_row_bounds(const uint32_t* __restrict__ srows, int64_t n, int3
 // integer exactly for every reachable u (checked exhaustively by the CPU
 // tests).  Alpha stays 255: (255*a + 255*(255-a) + 127) / 255 = 255.
 constexpr float kRound = 12582912.0f;   // 1.5 * 2^23
-constexpr int kK = 8;                   // pixels per lane; a warp owns 32*kK
-constexpr int kSeg = 32 * kK;
+constexpr int kK = kResolveSeg / 32;   // pixels per lane; a warp owns kResolveSeg pixels
 constexpr int kChunk = 512;
 
 struct PixRec {
     int32_t x0, x1;     // [x0, x1) clipped to >= 0
     float ia;           // 255 - a
     float sr, sg, sb;   // s*a per channel
+    int32_t row;        // cell row within the CTA
 };
 
 SR_DEV void blend3(float& r, float& g, float& b, const PixRec& q) {
@@ -54,15 +55,62 @@ SR_DEV void blend3(float& r, float& g, float& b, const PixRec& q) {
     b = __fsub_rn(__fmaf_rn(ub, inv, kRound), kRound);
 }
 
-__global__ void __launch_bounds__(512) k_resolve_pixel(const ResolveArgs a) {
+uint32_t resolve_rows_per_cta(int32_t W) {
+    int32_t segs = (W + kResolveSeg - 1) / kResolveSeg;
+    return segs >= kResolveWarps ? 1u : (uint32_t)(kResolveWarps / segs);
+}
+
+// Which rows and segment a warp paints: a CTA holds rows_per_cta cell rows
+// of one scene; small canvases give each row fewer warps than the CTA has.
+struct ResolveWork {
+    const SceneInfo* si;
+    int32_t W, r0, nr, segs, groups, my_row;
+    bool active;
+};
+
+SR_DEV ResolveWork resolve_work(const ResolveArgs& a) {
+    // scene of this CTA: last s with cta_base[s] <= blockIdx.x
+    uint32_t lo = 0, hi = a.n_scenes;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (a.cta_base[mid] <= blockIdx.x) lo = mid;
+        else hi = mid;
+    }
+    ResolveWork w;
+    w.si = &a.scenes[lo];
+    w.W = w.si->W;
+    w.segs = (w.W + kResolveSeg - 1) / kResolveSeg;
+    const int32_t R = w.segs >= kResolveWarps ? 1 : kResolveWarps / w.segs;
+    w.r0 = (int32_t)(blockIdx.x - a.cta_base[lo]) * R;
+    w.nr = imin(R, (int32_t)w.si->rows - w.r0);
+    const int warp = threadIdx.x >> 5;
+    if (w.segs >= kResolveWarps) {
+        w.my_row = 0;
+        w.groups = (w.segs + kResolveWarps - 1) / kResolveWarps;
+        w.active = true;
+    } else {
+        w.my_row = warp / w.segs;
+        w.groups = 1;
+        w.active = w.my_row < w.nr;
+    }
+    return w;
+}
+
+SR_DEV int32_t resolve_seg(const ResolveWork& w, int group) {
+    const int warp = threadIdx.x >> 5;
+    return w.segs >= kResolveWarps ? group * kResolveWarps + warp : warp % w.segs;
+}
+
+__global__ void __launch_bounds__(32 * kResolveWarps) k_resolve_pixel(const ResolveArgs a) {
     __shared__ PixRec sq[kChunk];
-    const int32_t row = blockIdx.x;
-    const int32_t W = a.W;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int32_t beg = a.row_start[row], end = a.row_start[row + 1];
-    uint32_t* out = a.image + (size_t)row * W;
-    for (int32_t group = 0; group < W; group += nw * kSeg) {
-        const int32_t seg = group + warp * kSeg;
+    const ResolveWork w = resolve_work(a);
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int32_t W = w.W;
+    const uint32_t gr0 = w.si->row_base + (uint32_t)w.r0;
+    const int32_t beg = a.row_start[gr0], end = a.row_start[gr0 + (uint32_t)w.nr];
+    for (int group = 0; group < w.groups; ++group) {
+        const int32_t seg = resolve_seg(w, group) * kResolveSeg;
+        const bool live = w.active && seg < W;
         float r[kK], g[kK], b[kK];
 #pragma unroll
         for (int j = 0; j < kK; ++j) r[j] = g[j] = b[j] = 255.0f;
@@ -80,14 +128,15 @@ __global__ void __launch_bounds__(512) k_resolve_pixel(const ResolveArgs a) {
                 pr.sr = (float)((col & 0xFFu) * al);
                 pr.sg = (float)(((col >> 8) & 0xFFu) * al);
                 pr.sb = (float)(((col >> 16) & 0xFFu) * al);
+                pr.row = (d.x >> 16) / a.F - w.r0;
                 sq[q] = pr;
             }
             __syncthreads();
-            if (seg >= W) continue;
+            if (!live) continue;
             for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
                 const int32_t qi = g0 + lane;
                 bool ov = false;
-                if (qi < cnt) ov = sq[qi].x0 < seg + kSeg && sq[qi].x1 > seg;
+                if (qi < cnt) ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg;
                 uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
                 while (m) {
                     const int q = g0 + __ffs(m) - 1;
@@ -109,7 +158,7 @@ __global__ void __launch_bounds__(512) k_resolve_pixel(const ResolveArgs a) {
                                 default: blend3(r[7], g[7], b[7], pr); break;
                             }
                         }
-                    } else if (pr.x0 <= seg && pr.x1 >= seg + kSeg) {
+                    } else if (pr.x0 <= seg && pr.x1 >= seg + kResolveSeg) {
 #pragma unroll
                         for (int j = 0; j < kK; ++j) blend3(r[j], g[j], b[j], pr);
                     } else {
@@ -122,7 +171,8 @@ __global__ void __launch_bounds__(512) k_resolve_pixel(const ResolveArgs a) {
                 }
             }
         }
-        if (seg < W) {
+        if (live) {
+            uint32_t* out = a.image + w.si->image_off + (size_t)(w.r0 + w.my_row) * W;
 #pragma unroll
             for (int j = 0; j < kK; ++j) {
                 int32_t p = seg + lane + 32 * j;
@@ -137,23 +187,24 @@ __global__ void __launch_bounds__(512) k_resolve_pixel(const ResolveArgs a) {
 }
 
 // ------------------------------------------------------- reference mode --
-// Overwrite in draw order (blending off), 2-pixel cell rows: each lane
-// keeps kK pixels of both rows of its warp's segment.
+// Overwrite in draw order (blending off); a cell row is FRAG_SIZE pixel
+// rows, painted alike.
 struct RefRec {
     int32_t x0, x1;
     uint32_t col;
+    int32_t row;
 };
 
-__global__ void __launch_bounds__(512) k_resolve_ref(const ResolveArgs a) {
+__global__ void __launch_bounds__(32 * kResolveWarps) k_resolve_ref(const ResolveArgs a) {
     __shared__ RefRec sq[kChunk];
-    const int32_t cell = blockIdx.x;
-    const int32_t W = a.W;
-    const int32_t y0 = cell * a.F;
-    const int32_t nrows = imin(a.F, a.H - y0);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int32_t beg = a.row_start[cell], end = a.row_start[cell + 1];
-    for (int32_t group = 0; group < W; group += nw * kSeg) {
-        const int32_t seg = group + warp * kSeg;
+    const ResolveWork w = resolve_work(a);
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int32_t W = w.W;
+    const uint32_t gr0 = w.si->row_base + (uint32_t)w.r0;
+    const int32_t beg = a.row_start[gr0], end = a.row_start[gr0 + (uint32_t)w.nr];
+    for (int group = 0; group < w.groups; ++group) {
+        const int32_t seg = resolve_seg(w, group) * kResolveSeg;
+        const bool live = w.active && seg < W;
         uint32_t px[kK];
 #pragma unroll
         for (int j = 0; j < kK; ++j) px[j] = 0xFFFFFFFFu;
@@ -166,14 +217,15 @@ __global__ void __launch_bounds__(512) k_resolve_ref(const ResolveArgs a) {
                 rr.x0 = d.x & 0xFFFF;
                 rr.x1 = wadd(rr.x0, d.y);
                 rr.col = (uint32_t)d.z;
+                rr.row = (d.x >> 16) / a.F - w.r0;
                 sq[q] = rr;
             }
             __syncthreads();
-            if (seg >= W) continue;
+            if (!live) continue;
             for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
                 const int32_t qi = g0 + lane;
                 bool ov = false;
-                if (qi < cnt) ov = sq[qi].x0 < seg + kSeg && sq[qi].x1 > seg;
+                if (qi < cnt) ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg;
                 uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
                 while (m) {
                     const int q = g0 + __ffs(m) - 1;
@@ -187,9 +239,11 @@ __global__ void __launch_bounds__(512) k_resolve_ref(const ResolveArgs a) {
                 }
             }
         }
-        if (seg < W) {
-            for (int32_t rr = 0; rr < nrows; ++rr) {
-                uint32_t* out = a.image + (size_t)(y0 + rr) * W;
+        if (live) {
+            const int32_t y0 = (w.r0 + w.my_row) * a.F;
+            const int32_t nrows = imin(a.F, w.si->H - y0);
+            for (int32_t yy = 0; yy < nrows; ++yy) {
+                uint32_t* out = a.image + w.si->image_off + (size_t)(y0 + yy) * W;
 #pragma unroll
                 for (int j = 0; j < kK; ++j) {
                     int32_t p = seg + lane + 32 * j;
@@ -200,22 +254,20 @@ __global__ void __launch_bounds__(512) k_resolve_ref(const ResolveArgs a) {
     }
 }
 
-void launch_resolve(const ResolveArgs& a, cudaStream_t st) {
-    int32_t rows = (a.H + a.F - 1) / a.F;
-    if (rows <= 0) return;
-    int warps = (a.W + kSeg - 1) / kSeg;
-    if (warps > 16) warps = 16;
+void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st) {
+    if (n_ctas == 0) return;
     count_launches(1);
-    if (a.pixel_mode) k_resolve_pixel<<<rows, 32 * warps, 0, st>>>(a);
-    else k_resolve_ref<<<rows, 32 * warps, 0, st>>>(a);
+    if (a.pixel_mode) k_resolve_pixel<<<n_ctas, 32 * kResolveWarps, 0, st>>>(a);
+    else k_resolve_ref<<<n_ctas, 32 * kResolveWarps, 0, st>>>(a);
 }
 
-void launch_row_bounds(const uint32_t* srows, int64_t n, int32_t rows, int32_t* row_start, cudaStream_t st) {
+void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,
+                       cudaStream_t st) {
     int64_t work = n + 1;
     int blocks = (int)((work + 255) / 256);
     if (blocks > 1216) blocks = 1216;
     count_launches(1);
-    k_row_bounds<<<blocks, 256, 0, st>>>(srows, n, rows, row_start);
+    k_row_bounds<<<blocks, 256, 0, st>>>(srows, n, n_dev, rows, row_start);
 }
 
 }  // namespace sr

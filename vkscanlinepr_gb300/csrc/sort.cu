@@ -53,9 +53,10 @@ Scratch carve(const SortPlan& p, void* base) {
 }
 }  // namespace
 
-SortPlan sort_plan(int64_t n, uint32_t key_bits) {
+SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev) {
     SortPlan p;
     p.n = n;
+    p.n_dev = n_dev;
     p.key_bits = key_bits;
     p.passes = (key_bits + kRadixBits - 1) / kRadixBits;
     if (p.passes == 0) p.passes = 1;
@@ -71,9 +72,11 @@ size_t sort_scratch_bytes(const SortPlan& p) {
 // Histogram of every pass's digits (grid-stride; warp-aggregated shared
 // atomics because neighbouring keys usually share their high digits).
 template <typename K>
-__global__ void __launch_bounds__(kThreads) k_hist(const K* __restrict__ keys, int64_t n, uint32_t passes,
+__global__ void __launch_bounds__(kThreads) k_hist(const K* __restrict__ keys, int64_t n_max,
+                                                   const uint32_t* __restrict__ n_dev, uint32_t passes,
                                                    uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[kMaxPasses][kRadix];
+    const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_max) : n_max;
     for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kThreads) (&sh[0][0])[i] = 0;
     __syncthreads();
     const uint32_t lane = lane_id();
@@ -140,7 +143,8 @@ template <typename K>
 __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ keys_in,
                                                        const uint32_t* __restrict__ vals_in,
                                                        K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-                                                       int64_t n, uint32_t shift,
+                                                       int64_t n_max, const uint32_t* __restrict__ n_dev,
+                                                       uint32_t shift,
                                                        const uint32_t* __restrict__ global_off,
                                                        uint32_t* __restrict__ lookback, uint32_t* counter,
                                                        uint32_t* status) {
@@ -151,7 +155,9 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ key
     if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
     __syncthreads();
     const uint32_t tile = S.tile;
+    const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_max) : n_max;
     const int64_t tbase = (int64_t)tile * kTile;
+    if (tbase >= n) return;   // launched for a larger capacity than this sort has
     const int64_t wbase = tbase + (int64_t)warp * (32 * kItems);
 
     // ---- load (warp-striped, coalesced) and rank within the warp
@@ -283,7 +289,7 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
     int hb = (int)((p.n + kThreads - 1) / kThreads);
     if (hb > kHistBlocks) hb = kHistBlocks;
     count_launches(1);
-    k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.passes, s.hist);
+    k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.n_dev, p.passes, s.hist);
     count_launches(1);
     k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
     const size_t smem = sizeof(OnesweepSmem<K>);
@@ -299,7 +305,7 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
         K* kdst = to_out ? keys_out : keys_alt;
         uint32_t* vdst = to_out ? vals_out : vals_alt;
         count_launches(1);
-        k_onesweep<K><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, pass * kRadixBits,
+        k_onesweep<K><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, p.n_dev, pass * kRadixBits,
                                                       s.hist + pass * kRadix,
                                                       s.lookback + (size_t)pass * (p.tiles + 1) * kRadix,
                                                       s.counters + pass, status);

@@ -129,7 +129,7 @@ struct Scene {
 };
 
 struct Params {
-    int preset = 0;           // 0 star cubics, 1 mixed
+    int preset = 0;           // 0 star cubics, 1 mixed, 2 one scene of a mixed batch
     uint64_t seed = 0;
     uint32_t scene_index = 0;
     uint32_t width = 1024, height = 1024;
@@ -143,7 +143,30 @@ struct Params {
 //             60/30/10 cubic/quadric/line, 30% even-odd, 5% figure-eights
 //             of 2 sub-contours, 2% full-canvas backgrounds, radius
 //             lognormal(ln 40, 1.0) clipped to [1, side/2].
+// Preset 2 (a batch of uneven scenes): scene `scene_index` of the batch has
+// a square canvas with side uniform over {256, 512, 1024, 2048} and a path
+// count lognormal(median 200, sigma 1) clipped to [10, 20000]; its paths are
+// drawn with the preset-1 generator.
+static inline void batch_scene_shape(uint64_t seed, uint32_t scene_index, uint32_t* side, uint32_t* paths) {
+    Rng g(mix3(seed ^ 0xB47C4u, scene_index, 0x5CE7Eu));
+    static const uint32_t sides[4] = {256, 512, 1024, 2048};
+    *side = sides[g.below(4)];
+    double p = pexp(plog(200.0) + pnormal(g));
+    if (p < 10.0) p = 10.0;
+    if (p > 20000.0) p = 20000.0;
+    *paths = (uint32_t)p;
+}
+
 static inline void preset_defaults(Params& p) {
+    if (p.preset == 2) {
+        uint32_t side, paths;
+        batch_scene_shape(p.seed, p.scene_index, &side, &paths);
+        p.preset = 1;
+        if (!p.width) p.width = side;
+        if (!p.height) p.height = side;
+        if (!p.n_paths) p.n_paths = paths;
+        return;
+    }
     if (p.preset == 0) {
         if (!p.width) p.width = 1024;
         if (!p.height) p.height = 1024;

@@ -7,11 +7,17 @@
 //   gen_merged_fragment_and_span.comp:33-103           draw-list emit
 //
 // Each CTA owns 2048 consecutive sorted records.  Chain A (decoupled
-// look-back) gives the exclusive winding prefix of the tile; the flags of
+// look-back) gives the exclusive winding prefix of each record; the flags of
 // each record follow; chain B (a second look-back, packed 31:31-bit counts
 // of merged fragments and spans) gives each record's output slot.  Draw
 // records come out in the reference's order: a record's merged fragment,
 // then the span ending at it.
+//
+// The reference's winding scan is global over its one scene's records
+// (scanline_rasterizer.cpp:479-506), so a path whose changes do not sum to
+// zero carries into the paths after it.  In a batch of scenes chain A is a
+// scan segmented at scene boundaries, so each scene sees exactly the global
+// scan it would see alone (with one scene the two are the same).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -24,6 +30,7 @@ constexpr int kTile = kThreads * kItems;
 constexpr uint64_t kFlagA = 1ull << 62;
 constexpr uint64_t kFlagP = 2ull << 62;
 constexpr uint64_t kValMask = (1ull << 62) - 1;
+constexpr uint64_t kHeadBit = 1ull << 61;   // chain A: the tile holds a scene's first record
 // chain B value: merged fragments in bits 31..61, spans in bits 0..30
 constexpr int kFragShift = 31;
 constexpr uint64_t kSpanMask = (1ull << 31) - 1;
@@ -57,7 +64,9 @@ SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
         uint64_t s = j >= 0 ? ld_acquire_u64(&tstat[j]) : kFlagP;
         uint32_t flag = (uint32_t)(s >> 62);
         uint32_t ready = __ballot_sync(0xFFFFFFFFu, flag != 0);
-        uint32_t pm = __ballot_sync(0xFFFFFFFFu, flag == 2);
+        // a tile that holds a segment head ends the look-back like an
+        // inclusive prefix does: its value already starts at that head
+        uint32_t pm = __ballot_sync(0xFFFFFFFFu, flag == 2 || (kSigned32 && flag == 1 && (s & kHeadBit)));
         int firstp = pm ? (__ffs(pm) - 1) : 31;
         uint32_t need = firstp == 31 ? 0xFFFFFFFFu : ((2u << firstp) - 1u);
         if ((ready & need) != need) {
@@ -68,7 +77,7 @@ SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
             __nanosleep(64);
             continue;
         }
-        uint64_t v = ((int)lane <= firstp) ? (s & kValMask) : 0ull;
+        uint64_t v = ((int)lane <= firstp) ? (s & (kSigned32 ? 0xFFFFFFFFull : kValMask)) : 0ull;
         if (kSigned32) {
             uint32_t w = (uint32_t)v;
 #pragma unroll
@@ -88,6 +97,7 @@ SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
 struct Smem {
     uint32_t tile;
     int32_t warpA[kThreads / 32];
+    int32_t warpAf[kThreads / 32];
     uint64_t warpB[kThreads / 32];
     int32_t prefixA;
     uint64_t prefixB;
@@ -104,9 +114,20 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
     if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
     __syncthreads();
     const uint32_t tile = S.tile;
-    const int64_t n = a.n;
+    const int64_t n = a.n_dev ? (int64_t)min((uint64_t)*a.n_dev, (uint64_t)a.n) : a.n;
     const int64_t tbase = (int64_t)tile * kTile;
     const int64_t num_tiles = (n + kTile - 1) / kTile;
+    if (tbase >= n) {
+        // launched for the capacity: nothing here; an empty frame still
+        // reports its (zero) totals
+        if (n == 0 && tile == 0 && threadIdx.x == 0) {
+            a.totals[0] = 0;
+            a.totals[1] = 0;
+            *a.n_draw = 0;
+            if (a.dbg_wscan) a.dbg_wscan[0] = 0;
+        }
+        return;
+    }
 
     // ---- stage keys (coalesced) and gather winding bits
     for (int j = threadIdx.x; j < kTile; j += kThreads) {
@@ -135,38 +156,95 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
 
     const int64_t ibase = tbase + (int64_t)threadIdx.x * kItems;
     int32_t wn[kItems];
-    int32_t wsum = 0;
+    bool hd[kItems];   // first record of a scene
+    // thread aggregate of the segmented scan: (head seen, sum since it)
+    bool tf = false;
+    int32_t tv = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         int64_t i = ibase + k;
         int32_t w = 0;
-        if (i < n) w = sx2(S.wb[i - tbase]);
+        bool h = false;
+        if (i < n) {
+            w = sx2(S.wb[i - tbase]);
+            const int jl = (int)(i - tbase);
+            const uint32_t p1 = (uint32_t)(S.keys[jl + 1] >> (a.L.xbits + a.L.rbits));
+            const uint32_t p0 = (uint32_t)(S.keys[jl] >> (a.L.xbits + a.L.rbits));
+            h = (i == 0) || (a.st.n_scenes > 1 && a.st.path_scene[p1] != a.st.path_scene[p0]);
+        }
         wn[k] = w;
-        wsum = wadd(wsum, w);
+        hd[k] = h;
+        if (h) {
+            tf = true;
+            tv = 0;
+        }
+        tv = wadd(tv, w);
     }
 
-    // ---- chain A: winding prefix
-    int32_t inclA = warp_incl<int32_t>(wsum);
-    if (lane == 31) S.warpA[warp] = inclA;
+    // ---- chain A: segmented winding prefix
+    // inclusive warp scan of (f, v) pairs: (fa, va) + (fb, vb) = (fa|fb, fb ? vb : va + vb)
+    bool fi = tf;
+    int32_t vi = tv;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        bool fp = __shfl_up_sync(0xFFFFFFFFu, (int)fi, d) != 0;
+        int32_t vp = __shfl_up_sync(0xFFFFFFFFu, vi, d);
+        if ((int)lane >= d) {
+            vi = fi ? vi : wadd(vp, vi);
+            fi = fi || fp;
+        }
+    }
+    // exclusive value for the lane
+    bool fe = __shfl_up_sync(0xFFFFFFFFu, (int)fi, 1) != 0;
+    int32_t ve = __shfl_up_sync(0xFFFFFFFFu, vi, 1);
+    if (lane == 0) {
+        fe = false;
+        ve = 0;
+    }
+    if (lane == 31) {
+        S.warpA[warp] = vi;
+        S.warpAf[warp] = fi ? 1 : 0;
+    }
     __syncthreads();
     if (warp == 0) {
-        int32_t w = lane < kThreads / 32 ? S.warpA[lane] : 0;
-        int32_t wi = warp_incl<int32_t>(w);
-        if (lane < kThreads / 32) S.warpA[lane] = wadd(wi, -w);
-        int32_t agg = __shfl_sync(0xFFFFFFFFu, wi, kThreads / 32 - 1);
-        if (lane == 0) st_release_u64(&tstatA[tile], (tile == 0 ? kFlagP : kFlagA) | (uint32_t)agg);
+        bool wf = lane < kThreads / 32 ? S.warpAf[lane] != 0 : false;
+        int32_t wv = lane < kThreads / 32 ? S.warpA[lane] : 0;
+        bool f2 = wf;
+        int32_t v2 = wv;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            bool fp = __shfl_up_sync(0xFFFFFFFFu, (int)f2, d) != 0;
+            int32_t vp = __shfl_up_sync(0xFFFFFFFFu, v2, d);
+            if ((int)lane >= d) {
+                v2 = f2 ? v2 : wadd(vp, v2);
+                f2 = f2 || fp;
+            }
+        }
+        // exclusive per warp, and the tile aggregate
+        bool xf = __shfl_up_sync(0xFFFFFFFFu, (int)f2, 1) != 0;
+        int32_t xv = __shfl_up_sync(0xFFFFFFFFu, v2, 1);
+        if (lane == 0) {
+            xf = false;
+            xv = 0;
+        }
+        const bool aggf = __shfl_sync(0xFFFFFFFFu, (int)f2, kThreads / 32 - 1) != 0;
+        const int32_t agg = __shfl_sync(0xFFFFFFFFu, v2, kThreads / 32 - 1);
+        if (lane == 0)
+            st_release_u64(&tstatA[tile], (tile == 0 ? kFlagP : kFlagA) | (aggf ? kHeadBit : 0ull) | (uint32_t)agg);
         int32_t excl = 0;
         if (tile > 0) {
             excl = (int32_t)(uint32_t)lookback<true>(tstatA, tile, status);
-            if (lane == 0) st_release_u64(&tstatA[tile], kFlagP | (uint32_t)wadd(excl, agg));
+            if (lane == 0) st_release_u64(&tstatA[tile], kFlagP | (uint32_t)(aggf ? agg : wadd(excl, agg)));
         }
-        if (lane == 0) {
-            S.prefixA = excl;
-            if (tile == num_tiles - 1 && a.dbg_wscan) a.dbg_wscan[n] = wadd(excl, agg);
+        // carry into each warp: the tile prefix combined with the warp's exclusive pair
+        if (lane < kThreads / 32) {
+            S.warpA[lane] = xf ? xv : wadd(excl, xv);
         }
+        if (lane == 0 && tile == num_tiles - 1 && a.dbg_wscan) a.dbg_wscan[n] = aggf ? agg : wadd(excl, agg);
     }
     __syncthreads();
-    int32_t wrun = wadd(wadd(S.prefixA, S.warpA[warp]), wadd(inclA, -wsum));
+    // carry into this thread, then per record (reset at scene heads)
+    int32_t wrun = fe ? ve : wadd(S.warpA[warp], ve);
 
     // ---- flags
     uint32_t ff[kItems], sf[kItems];
@@ -175,6 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         int64_t i = ibase + k;
+        if (hd[k]) wrun = 0;
         int32_t wscan = wrun;
         wrun = wadd(wrun, wn[k]);
         ff[k] = 0;
@@ -183,7 +262,8 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         int jl = (int)(i - tbase);
         uint64_t k1 = S.keys[jl + 1];
         Decoded d1 = unpack_key(a.L, k1);
-        bool on = !(d1.x < 0 || d1.y < 0 || d1.x >= a.W || d1.y >= a.H);
+        const SceneInfo& si = scene_of_path(a.st, d1.path);
+        bool on = !(d1.x < 0 || d1.y < 0 || d1.x >= si.W || d1.y >= si.H);
         uint32_t rule = a.fill_rule[d1.path];
         if (i == 0) {
             ff[k] = on ? 1u : 0u;
@@ -246,6 +326,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
                 uint64_t tot = excl + agg;
                 a.totals[0] = tot >> kFragShift;
                 a.totals[1] = tot & kSpanMask;
+                *a.n_draw = (uint32_t)((tot >> kFragShift) + (tot & kSpanMask));
             }
         }
     }
@@ -262,11 +343,12 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         int jl = (int)(i - tbase);
         Decoded d1 = unpack_key(a.L, S.keys[jl + 1]);
         int32_t info = (int32_t)a.fill_info[d1.path];
+        const uint32_t row_base = scene_of_path(a.st, d1.path).row_base;
         int64_t o = (int64_t)(fb + sb);
         if (ff[k]) {
             if (o < a.draw_capacity) {
                 a.draw[o] = make_int4((int32_t)((uint32_t)d1.y << 16) | d1.x, F, info, (int32_t)(fb + 1));
-                a.draw_row[o] = (uint32_t)(d1.y / F);
+                a.draw_row[o] = row_base + (uint32_t)(d1.y / F);
             } else {
                 set_error(status, ERR_CAPACITY);
             }
@@ -277,7 +359,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
             int32_t x0 = imax(0, wadd(d0.x, F));
             if (o < a.draw_capacity) {
                 a.draw[o] = make_int4((int32_t)((uint32_t)d0.y << 16) | x0, d1.x - x0, info, 0);
-                a.draw_row[o] = (uint32_t)(d0.y / F);
+                a.draw_row[o] = row_base + (uint32_t)(d0.y / F);
             } else {
                 set_error(status, ERR_CAPACITY);
             }
