@@ -53,6 +53,11 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="frame4096", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=4096,
+                    help="scenes of the batched workload (0 skips it)")
+    ap.add_argument("--batch-size", type=int, default=512, help="scenes per resident batch")
+    ap.add_argument("--plain-scenes", type=int, default=512,
+                    help="scenes the plain per-scene renderer is timed on")
     return ap.parse_args()
 
 
@@ -178,6 +183,73 @@ def run_cpu_baseline(scene_oracle, W, H, budget_s=20.0):
                       % (len(times), threads)}, img
 
 
+def run_batched(sr, args, sptr, steps):
+    """Configuration 2: uneven scenes (side 256..2048, lognormal path
+    counts), rendered as resident batches replaying captured CUDA graphs,
+    against the plain renderer (load + render per scene)."""
+    total, per = args.batch_scenes, args.batch_size
+    seed = 2
+    t0 = time.perf_counter()
+    batches = []
+    for k in range((total + per - 1) // per):
+        n = min(per, total - k * per)
+        b = sr.SceneBatch(mode=sr.MODE_PIXEL)
+        b.add_synth(2, seed, n, scene_index=k * per)
+        b.commit()
+        batches.append(b)
+    build_s = time.perf_counter() - t0
+    caps, records = [], 0
+    for b in batches:           # exact frame: learns each batch's record count
+        b.render(stream=sptr)
+        st = b.stats()
+        caps.append(st["n_intersections"])
+        records += st["n_intersections"]
+    for b, c in zip(batches, caps):
+        b.render(capacity=c, graph=True, stream=sptr)   # capture
+    times = []
+    for _ in range(steps):
+        t1 = time.perf_counter()
+        for b, c in zip(batches, caps):
+            b.render(capacity=c, graph=True, stream=sptr)
+        times.append(time.perf_counter() - t1)
+    overflows = sum(b.stats()["overflows"] for b in batches)
+    batched_sps = total / (sum(times) / len(times))
+    # plain per-scene renderer on the first scenes of the same set
+    nplain = min(args.plain_scenes, total)
+    ctx = None
+    plain_t = 0.0
+    exact = 0
+    checked = 0
+    for i in range(nplain):
+        sc = sr.synth_scene(2, seed, scene_index=i)
+        if ctx is None or (ctx.width, ctx.height) != (sc.width, sc.height):
+            if ctx is not None:
+                ctx.close()
+            ctx = sr.ScanlineVGRasterizer(mode=sr.MODE_PIXEL)
+            ctx.initialize(None, sc.width, sc.height)
+            ctx.loadVG(sc)
+            ctx.render_device(stream=sptr)   # warm the context's buffers
+        t1 = time.perf_counter()
+        ctx.loadVG(sc)
+        ctx.render_device(stream=sptr)
+        plain_t += time.perf_counter() - t1
+        if i < 24:
+            img = ctx.render()
+            checked += 1
+            exact += int(np.array_equal(img, batches[i // per].image(i % per)))
+    if ctx is not None:
+        ctx.close()
+    plain_sps = nplain / plain_t
+    for b in batches:
+        b.close()
+    return {"scenes": total, "records": int(records), "resident_batches": len(batches),
+            "scenes_per_s": round(batched_sps, 1), "ms_per_batch_of_all": round(1000 * sum(times) / len(times), 2),
+            "sizing": "record capacity from the previous exact frame, frame replayed as a CUDA graph",
+            "overflows": int(overflows), "plain_scenes_per_s": round(plain_sps, 1),
+            "plain_sample": nplain, "speedup_vs_plain": round(batched_sps / plain_sps, 2),
+            "bit_exact_vs_plain": "%d/%d" % (exact, checked), "build_s": round(build_s, 2)}
+
+
 def oracle_scene(preset, seed, W, H, P):
     import oracle
     return oracle.synth(preset, seed, width=W, height=H, n_paths=P)
@@ -299,6 +371,9 @@ def main():
     e2e = {"value": round(world * e2e_steps / e2e_s, 4), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(W * H * 4)}
     gpu_img = out_img.copy()
+    r.close()
+
+    batched = run_batched(sr, args, sptr, max(2, min(args.steps, 5))) if args.batch_scenes > 0 else None
 
     # ---- roofline of the dominant stage
     peak, peak_kind = measured_peaks()
@@ -333,13 +408,14 @@ def main():
             "samples_per_s": round(value * W * H, 1),
             "roofline": roofline, "stages": stages, "e2e": e2e, "clocks": clocks,
             "gpu_launches": int(launches)}
+    if batched is not None:
+        line["batched"] = batched
 
     if rank == 0 and not args.no_cpu_baseline:
         so = oracle_scene(preset, seed, W, H, P)
         cpu, ref_img = run_cpu_baseline(so, W, H)
         line["cpu_baseline"] = cpu
         line["bit_exact"] = bool(np.array_equal(ref_img, gpu_img))
-    r.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -336,6 +336,46 @@ struct Pipeline {
         return SR_OK;
     }
 
+    // One scene straight from the caller's arrays (no host staging copy;
+    // the copies run at pinned-memory speed when the caller's arrays are
+    // pinned).
+    sr_status upload_single(const sr_scene_view* s, int32_t W, int32_t H, const float* mvp) {
+        CUDA_TRY(cudaSetDevice(device));
+        S = 1;
+        V = s->n_points;
+        C = s->n_curves;
+        P = s->n_paths;
+        info.assign(1, sr::SceneInfo{});
+        info[0].W = W;
+        info[0].H = H;
+        info[0].path_begin = 0;
+        info[0].path_end = P;
+        std::memcpy(info[0].mvp, mvp, sizeof info[0].mvp);
+        CUDA_TRY(ensure(pos, sizeof(float) * 2 * (size_t)std::max<uint32_t>(V, 1)));
+        CUDA_TRY(ensure(pos_path, sizeof(uint32_t) * std::max<uint32_t>(V, 1)));
+        CUDA_TRY(ensure(curve_pos, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(curve_type, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(curve_path, sizeof(uint32_t) * std::max<uint32_t>(C, 1)));
+        CUDA_TRY(ensure(fill_rule, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        CUDA_TRY(ensure(fill_info, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        CUDA_TRY(ensure(path_scene, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        auto up = [](DevBuf& d, const void* src, size_t bytes) -> cudaError_t {
+            return bytes ? cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+        };
+        CUDA_TRY(up(pos, s->position, sizeof(float) * 2 * (size_t)V));
+        CUDA_TRY(up(pos_path, s->pos_path_idx, sizeof(uint32_t) * V));
+        CUDA_TRY(up(curve_pos, s->curve_pos_map, sizeof(uint32_t) * C));
+        CUDA_TRY(up(curve_type, s->curve_type, sizeof(uint32_t) * C));
+        CUDA_TRY(up(curve_path, s->curve_path_idx, sizeof(uint32_t) * C));
+        CUDA_TRY(up(fill_rule, s->fill_rule, sizeof(uint32_t) * P));
+        CUDA_TRY(up(fill_info, s->fill_info, sizeof(uint32_t) * P));
+        CUDA_TRY(cudaMemset(path_scene.p, 0, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        SR_TRY(upload_table());
+        loaded = true;
+        stages_valid = false;
+        return SR_OK;
+    }
+
     sr::GeomArgs geom(int64_t cap) const {
         sr::GeomArgs g;
         g.n_curves = C;
@@ -618,7 +658,6 @@ struct Pipeline {
 
 struct sr_ctx {
     Pipeline p;
-    HostScenes h;
     int32_t W = 0, H = 0;
     float mvp[16];
 };
@@ -677,9 +716,7 @@ sr_status sr_create(uint32_t width, uint32_t height, const sr_options* opt, sr_c
 sr_status sr_load_scene(sr_ctx* c, const sr_scene_view* s) {
     if (!c || !s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     SR_TRY(validate_scene(s));
-    c->h.clear();
-    append_scene(c->h, (uint32_t)c->W, (uint32_t)c->H, s, c->mvp);
-    return c->p.upload(c->h);
+    return c->p.upload_single(s, c->W, c->H, c->mvp);
 }
 
 sr_status sr_set_mvp(sr_ctx* c, const float m[16]) {
@@ -714,10 +751,8 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     CUDA_TRY(cudaSetDevice(p.device));
     if (!p.loaded || p.S != 1) {
         // a canvas with no scene: the draw list alone decides the pixels
-        c->h.clear();
         sr_scene_view empty{};
-        append_scene(c->h, (uint32_t)c->W, (uint32_t)c->H, &empty, c->mvp);
-        SR_TRY(p.upload(c->h));
+        SR_TRY(p.upload_single(&empty, c->W, c->H, c->mvp));
     }
     const int32_t rows = (int32_t)p.total_rows;
     const size_t n1 = (size_t)std::max<int64_t>(n, 1);
