@@ -58,6 +58,10 @@ def parse_args():
     ap.add_argument("--batch-size", type=int, default=512, help="scenes per resident batch")
     ap.add_argument("--plain-scenes", type=int, default=512,
                     help="scenes the plain per-scene renderer is timed on")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-sizing configuration")
+    ap.add_argument("--train-epochs", type=int, default=30)
+    ap.add_argument("--small-batch", type=int, default=32,
+                    help="scenes per batch in the learned-vs-exact sizing stream")
     return ap.parse_args()
 
 
@@ -240,14 +244,161 @@ def run_batched(sr, args, sptr, steps):
     if ctx is not None:
         ctx.close()
     plain_sps = nplain / plain_t
+    learned = None
+    if not args.no_learned:
+        learned = run_learned(sr, args, sptr, batches)
     for b in batches:
         b.close()
-    return {"scenes": total, "records": int(records), "resident_batches": len(batches),
+    return learned, {"scenes": total, "records": int(records), "resident_batches": len(batches),
             "scenes_per_s": round(batched_sps, 1), "ms_per_batch_of_all": round(1000 * sum(times) / len(times), 2),
             "sizing": "record capacity from the previous exact frame, frame replayed as a CUDA graph",
             "overflows": int(overflows), "plain_scenes_per_s": round(plain_sps, 1),
             "plain_sample": nplain, "speedup_vs_plain": round(batched_sps / plain_sps, 2),
             "bit_exact_vs_plain": "%d/%d" % (exact, checked), "build_s": round(build_s, 2)}
+
+
+def _labels_of(sr, batches_spec, sptr):
+    """Features, exact-count labels and scene path ranges of the paths of
+    several synthetic batches: [(preset, seed, count, first_scene_index), ...]."""
+    xs, ts, ranges, paths = [], [], [0], 0
+    for preset, seed, count, first in batches_spec:
+        b = sr.SceneBatch(mode=sr.MODE_PIXEL)
+        b.add_synth(preset, seed, count, scene_index=first)
+        b.commit()
+        xs.append(b.features(stream=sptr))
+        ts.append(b.labels(stream=sptr))
+        ranges.extend(int(v) + paths for v in b.path_ranges()[1:])
+        paths += xs[-1].shape[0]
+        b.close()
+    return sr.concat_device(xs), sr.concat_device(ts), np.array(ranges), paths
+
+
+def run_learned(sr, args, sptr, batches):
+    """Configuration 3: the sizing network trained on ~200k paths of the
+    4096^2 and batch generators (labels from the exact count pass), margins
+    calibrated on held-out scenes, evaluated on the batched workload's
+    scenes: per-path overflow, over-allocation, and the time sizing from the
+    network saves against waiting for the exact count."""
+    import ctypes as _ct
+    import torch
+    t0 = time.perf_counter()
+    x, t, _, n_train = _labels_of(sr, [(1, 101 + i, 1, 0) for i in range(4)] + [(2, 102, 384, 0)], sptr)
+    label_s = time.perf_counter() - t0
+    xv, tv, val_ranges, n_val = _labels_of(sr, [(2, 103, 96, 0)], sptr)
+    sz = sr.Sizer(seed=1)
+    sz.set_norm(sr.sizer_norm(x.numpy(), t.numpy()))
+    t0 = time.perf_counter()
+    loss = sz.train(x, t, epochs=args.train_epochs, batch=4096, lr=1e-3, seed=7, stream=sptr)
+    train_s = time.perf_counter() - t0
+    steps = sz.state()["step"]
+    pv = sz.predict(xv).numpy()
+    margins = sr.calibrate_margins(pv, tv.numpy(), val_ranges)
+    val_loss, _ = sz.loss_grad(xv, tv)
+    # evaluation on the batched workload's scenes (seed 2), one resident
+    # batch at a time so only one holds planned-size buffers
+    for b in batches:
+        b.release()
+    paths = over_r = over_d = 0
+    acc = {k: 0 for k in ("records", "draws", "path_records", "path_draws", "exact_r", "exact_d")}
+    plan_ms, overflows = [], 0
+    t_exact = t_learned = 0.0
+    for b in batches:
+        t1 = time.perf_counter()
+        pl = b.plan(sz, margins, stream=sptr)
+        plan_ms.append(1000 * (time.perf_counter() - t1))
+        j = b.judge(stream=sptr)
+        paths += j["paths"]
+        over_r += j["paths_over_records"]
+        over_d += j["paths_over_draws"]
+        for k in ("records", "draws", "path_records", "path_draws"):
+            acc[k] += pl[k]
+        acc["exact_r"] += j["records"]
+        acc["exact_d"] += j["draws"]
+        # the batch rendered once: waiting for the exact count against a
+        # plan plus a pre-sized frame; both warmed first
+        b.render(capacity=pl["records"], draw_capacity=pl["draws"], stream=sptr)
+        b.render(stream=sptr)
+        t1 = time.perf_counter()
+        b.render(stream=sptr)
+        t_exact += time.perf_counter() - t1
+        o0 = b.stats()["overflows"]
+        t1 = time.perf_counter()
+        pl = b.plan(sz, margins, stream=sptr)
+        b.render(capacity=pl["records"], draw_capacity=pl["draws"], stream=sptr)
+        t_learned += time.perf_counter() - t1
+        overflows += b.stats()["overflows"] - o0
+        b.release()
+    # a stream of serving-sized batches of new scenes: each is assembled on
+    # the host, uploaded, sized and rendered.  With exact sizing the host
+    # waits inside every frame for its count, so it cannot assemble the next
+    # batch while the GPU renders; planned frames are enqueued whole and the
+    # host moves on to the next batch.
+    sb = args.small_batch
+    nsb = max(2, min(48, args.batch_scenes // max(1, sb)))
+    scenes = [sr.synth_scene(2, 2, scene_index=i) for i in range(nsb * sb)]
+    rs, ss = torch.cuda.Stream(), torch.cuda.Stream()
+    rsp, ssp = _ct.c_void_p(rs.cuda_stream), _ct.c_void_p(ss.cuda_stream)
+    objs = [sr.SceneBatch(mode=sr.MODE_PIXEL) for _ in range(2)]
+
+    def fill(b, k):
+        b.clear()
+        for sc in scenes[k * sb:(k + 1) * sb]:
+            b.add_scene(sc)
+        b.commit()
+
+    def exact_stream():
+        for k in range(nsb):
+            b = objs[k % 2]
+            fill(b, k)
+            b.render(stream=rsp)
+
+    def learned_stream():
+        prev = None
+        for k in range(nsb):
+            b = objs[k % 2]
+            fill(b, k)
+            pl = b.plan(sz, margins, stream=ssp)
+            b.enqueue(pl["records"], draw_capacity=pl["draws"], stream=rsp)
+            if prev is not None:
+                prev.finish()
+            prev = b
+        prev.finish()
+    exact_stream()
+    learned_stream()
+    torch.cuda.synchronize()
+    o0 = sum(b.stats()["overflows"] for b in objs)
+    t1 = time.perf_counter()
+    exact_stream()
+    t_small_exact = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    learned_stream()
+    t_small_learned = time.perf_counter() - t1
+    small_over = sum(b.stats()["overflows"] for b in objs) - o0
+    for b in objs:
+        b.close()
+    sz.close()
+    return {
+        "train_paths": int(n_train), "val_paths": int(n_val), "label_s": round(label_s, 2),
+        "train_steps": int(steps), "train_s": round(train_s, 3), "train_mse": round(loss, 5),
+        "val_mse": round(val_loss, 5), "margins": [round(m, 4) for m in margins],
+        "eval_paths": int(paths),
+        "overflow_paths_records": round(over_r / max(paths, 1), 5),
+        "overflow_paths_draws": round(over_d / max(paths, 1), 5),
+        "path_allot_over_exact": [round(acc["path_records"] / max(acc["exact_r"], 1), 3),
+                                  round(acc["path_draws"] / max(acc["exact_d"], 1), 3)],
+        "frame_capacity_over_exact": [round(acc["records"] / max(acc["exact_r"], 1), 3),
+                                      round(acc["draws"] / max(acc["exact_d"], 1), 3)],
+        "plan_ms_per_batch": round(statistics.median(plan_ms), 3),
+        "batch_frames_overflowed": int(overflows),
+        "big_batches": {"scenes_per_batch": args.batch_size, "exact_s": round(t_exact, 4),
+                        "learned_s": round(t_learned, 4), "saved_frac": round(1 - t_learned / t_exact, 4)},
+        "stream": {"scenes_per_batch": sb, "batches": nsb, "exact_s": round(t_small_exact, 4),
+                   "learned_s": round(t_small_learned, 4),
+                   "saved_frac": round(1 - t_small_learned / t_small_exact, 4),
+                   "scenes_per_s_exact": round(nsb * sb / t_small_exact, 1),
+                   "scenes_per_s_learned": round(nsb * sb / t_small_learned, 1),
+                   "overflowed": int(small_over)},
+    }
 
 
 def oracle_scene(preset, seed, W, H, P):
@@ -373,7 +524,8 @@ def main():
     gpu_img = out_img.copy()
     r.close()
 
-    batched = run_batched(sr, args, sptr, max(2, min(args.steps, 5))) if args.batch_scenes > 0 else None
+    learned, batched = (run_batched(sr, args, sptr, max(2, min(args.steps, 5))) if args.batch_scenes > 0
+                        else (None, None))
 
     # ---- roofline of the dominant stage
     peak, peak_kind = measured_peaks()
@@ -410,6 +562,8 @@ def main():
             "gpu_launches": int(launches)}
     if batched is not None:
         line["batched"] = batched
+    if learned is not None:
+        line["learned"] = learned
 
     if rank == 0 and not args.no_cpu_baseline:
         so = oracle_scene(preset, seed, W, H, P)

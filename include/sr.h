@@ -240,6 +240,11 @@ typedef struct sr_batch_render_opts {
                                     >= 0: pre-sized, no mid-frame wait */
     uint32_t refit_on_overflow;  /* on overflow, rerun with exact sizing */
     uint32_t reserved;
+    int64_t  draw_capacity;      /* draw records (merged fragments + spans) the
+                                    frame may emit; <= 0: 2 x record_capacity,
+                                    which always suffices.  Callers built
+                                    against the 24-byte form of this struct get
+                                    the default. */
 } sr_batch_render_opts;
 
 typedef struct sr_batch_stats {
@@ -261,11 +266,141 @@ sr_status sr_batch_add_synth(sr_batch* b, const sr_synth_params* p, uint32_t cou
 sr_status sr_batch_commit(sr_batch* b);
 sr_status sr_batch_set_mvp(sr_batch* b, uint32_t index, const float m[16]);
 sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* opts, void* stream);
+/* sr_batch_render in two halves for hosts that keep several batches in
+ * flight: enqueue returns once the frame is queued on `stream` (it needs
+ * record_capacity >= 0, so nothing waits mid-frame); query reports whether
+ * the frame has finished on the device; finish waits for it, checks for
+ * overflow and, with refit_on_overflow, reruns it with exact sizing.  One
+ * frame per batch may be in flight. */
+sr_status sr_batch_enqueue(sr_batch* b, const sr_batch_render_opts* opts, void* stream);
+sr_status sr_batch_query(sr_batch* b, int* done);
+sr_status sr_batch_finish(sr_batch* b);
 sr_status sr_batch_get_image(sr_batch* b, uint32_t index, void* rgba_out, int out_is_device, void* stream);
 sr_status sr_batch_info(const sr_batch* b, uint32_t index, uint32_t* width, uint32_t* height);
 sr_status sr_batch_get_stats(const sr_batch* b, sr_batch_stats* out);
 sr_status sr_batch_clear(sr_batch* b);
 void sr_batch_destroy(sr_batch* b);
+
+/* ------------------------------------------------------------------ */
+/* Learned buffer sizing (replaces the count read-back of              */
+/* scanline_rasterizer.cpp:337-358 and pre-sizes the fragment buffers   */
+/* of :578-584; no reference counterpart for the network itself).       */
+/* ------------------------------------------------------------------ */
+
+/* A 6 -> 64 -> 64 -> 2 GELU network that predicts, per path, log(1 + its
+ * intersection records) and log(1 + its draw records) from 6 features of
+ * its control points.  Weights are BF16 with an FP32 master copy;
+ * arithmetic is FP32.  Training (Adam) and inference run on the GPU.
+ * Feature row of a path (all log1p except the last):
+ *   segments, clipped bbox width, clipped bbox height (cells),
+ *   control-polygon length (cells), sum |turn angle| (turns),
+ *   cubic fraction.
+ * The normaliser maps features and targets to standard units:
+ *   norm = x_mean[6], x_inv_std[6], y_mean[2], y_std[2]. */
+#define SR_SIZER_FEATURES 6
+#define SR_SIZER_OUTPUTS 2
+#define SR_SIZER_PARAMS 4738
+#define SR_SIZER_NORM 16
+typedef struct sr_sizer sr_sizer;
+
+typedef struct sr_sizer_train_opts {
+    uint32_t struct_size;
+    uint32_t batch;      /* minibatch size (default 4096) */
+    uint32_t epochs;     /* passes over the data (default 1) */
+    uint32_t shuffle;    /* reshuffle every epoch (default 1) */
+    float    lr;         /* Adam learning rate (default 1e-3) */
+    float    beta1, beta2, eps;   /* defaults 0.9, 0.999, 1e-8 */
+    uint64_t seed;       /* shuffle seed */
+} sr_sizer_train_opts;
+
+/* Weights drawn from a seeded uniform of variance 1/fan_in, zero biases,
+ * identity normaliser, zero Adam state. */
+sr_status sr_sizer_create(int device, uint64_t seed, sr_sizer** out);
+void sr_sizer_destroy(sr_sizer* s);
+sr_status sr_sizer_set_norm(sr_sizer* s, const float norm[SR_SIZER_NORM]);
+/* Checkpoint: FP32 parameters, Adam moments, normaliser and step count
+ * (any pointer may be NULL to skip that part). */
+sr_status sr_sizer_get_state(const sr_sizer* s, float* params, float* adam_m, float* adam_v,
+                             float norm[SR_SIZER_NORM], int64_t* step);
+sr_status sr_sizer_set_state(sr_sizer* s, const float* params, const float* adam_m, const float* adam_v,
+                             const float norm[SR_SIZER_NORM], int64_t step);
+/* Mean squared error (standard units, over n rows and both outputs) and
+ * its gradient with respect to the parameters, at the current weights.
+ * d_x[n][6], d_t[n][2] are device arrays; h_grad[SR_SIZER_PARAMS] host. */
+sr_status sr_sizer_loss_grad(sr_sizer* s, const float* d_x, const float* d_t, uint32_t n, float* h_grad,
+                             float* h_loss);
+/* Adam training on device rows (d_x, d_t); h_loss (optional) receives the
+ * mean squared error of the last epoch. */
+sr_status sr_sizer_train(sr_sizer* s, const float* d_x, const float* d_t, uint32_t n,
+                         const sr_sizer_train_opts* opts, float* h_loss, void* stream);
+/* d_y[n][2] = predicted log(1 + records), log(1 + draw records). */
+sr_status sr_sizer_predict(const sr_sizer* s, const float* d_x, uint32_t n, float* d_y, void* stream);
+
+/* Per-path features of a committed batch under its current transforms:
+ * d_feats[n_paths][6] (device). */
+sr_status sr_batch_path_features(sr_batch* b, float* d_feats, void* stream);
+/* Renders the batch once with exact sizing, counting records and draw
+ * records per path: d_labels[n_paths][2] = log(1 + records),
+ * log(1 + draw records) (device).  The images are those of a plain render. */
+sr_status sr_batch_path_labels(sr_batch* b, float* d_labels, void* stream);
+
+/* Margins in log units.  A path's allotment is ceil(exp(y + path margin) - 1)
+ * for its predicted y = log(1 + count); allotments are what the exact count
+ * pass judges path by path.  The frame capacities sum the same expression
+ * with the frame margins, which can be much smaller: errors of many paths
+ * average out. */
+typedef struct sr_sizing_margins {
+    uint32_t struct_size;
+    float path_records, path_draws;
+    float frame_records, frame_draws;
+} sr_sizing_margins;
+
+typedef struct sr_sizing_plan {
+    int64_t  records;        /* record capacity of the frame */
+    int64_t  draws;          /* draw-record capacity (at most 2 x records) */
+    int64_t  path_records;   /* sums of the per-path allotments */
+    int64_t  path_draws;
+    uint64_t device_bytes;   /* device memory of the batch with the frame capacities */
+} sr_sizing_plan;
+
+/* Sizes the next frame from the network: features, prediction, per-path
+ * allotments and frame capacities.  Pass plan.records / plan.draws as the
+ * render's capacities.  scene_caps (optional, [n_scenes][2] host) gets each
+ * scene's record and draw capacity.  One host wait. */
+sr_status sr_batch_plan(sr_batch* b, const sr_sizer* s, const sr_sizing_margins* margins, sr_sizing_plan* plan,
+                        int64_t* scene_caps, void* stream);
+/* path_begin[n_scenes + 1]: the first path of each scene in the batch's
+ * path order (the rows of sr_batch_path_features / _labels). */
+sr_status sr_batch_path_ranges(const sr_batch* b, uint32_t* path_begin);
+
+typedef struct sr_sizing_judge {
+    uint32_t paths;              /* paths in the batch */
+    uint32_t paths_over_records; /* paths whose exact records exceed their allotment */
+    uint32_t paths_over_draws;   /* likewise for draw records */
+    uint32_t reserved;
+    int64_t  records;            /* exact totals */
+    int64_t  draws;
+} sr_sizing_judge;
+
+/* Runs the exact count pass (a render with exact sizing and per-path
+ * counters) and compares every path with the allotment of the last
+ * sr_batch_plan. */
+sr_status sr_batch_judge(sr_batch* b, sr_sizing_judge* out, void* stream);
+
+/* Device bytes the batch holds when rendered with capacities (records,
+ * draws); draws <= 0 means 2 x records. */
+sr_status sr_batch_frame_bytes(sr_batch* b, int64_t records, int64_t draws, uint64_t* bytes);
+/* Frees the batch's record- and draw-sized buffers (scenes and images stay;
+ * the next frame reallocates what it needs) and drops its captured graph. */
+sr_status sr_batch_release(sr_batch* b);
+/* Device bytes the batch holds now. */
+sr_status sr_batch_held_bytes(const sr_batch* b, uint64_t* bytes);
+
+/* Plain device memory for hosts without a CUDA binding of their own. */
+void* sr_device_alloc(int device, size_t bytes);
+void sr_device_free(void* p);
+/* Synchronous copy between any host and device addresses. */
+sr_status sr_memcpy(void* dst, const void* src, size_t bytes);
 
 /* ------------------------------------------------------------------ */
 /* Scene sources: synthetic generator and RVG loader (host only).      */

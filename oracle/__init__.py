@@ -27,6 +27,7 @@ STAGES = {
     "curve_offset": 4, "intersection": 5, "frag_key": 6, "frag_winding": 7,
     "sorted_key": 8, "sorted_index": 9, "winding_scan": 10, "frag_flag": 11,
     "span_flag": 12, "draw_list": 13, "image": 14, "frag_left": 15,
+    "path_draws": 100,
 }
 
 

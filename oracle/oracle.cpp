@@ -47,6 +47,9 @@
 
 namespace orc {
 
+// Oracle-only stage id: draw records per path (the labels of learned sizing).
+constexpr int kStagePathDraws = 100;
+
 // ------------------------------------------------------------- helpers ----
 template <class R> struct FT;
 template <> struct FT<float> {
@@ -220,6 +223,7 @@ template <class R> struct Frame {
     std::vector<int32_t> fflag, sflag;   // N
     std::vector<int32_t> fscan;          // 2N+1
     std::vector<int32_t> draw;           // 4*O
+    std::vector<int32_t> path_draws;     // P: draw records per path (sizing labels)
     std::vector<uint32_t> image;         // W*H
     int64_t N = 0, O = 0, n_frag = 0, n_span = 0;
     double ms[8] = {0};
@@ -678,6 +682,9 @@ template <class R> struct Frame {
         n_span = fscan[2 * N] - n_frag;
         O = n_frag + n_span;
         draw.assign(4 * (size_t)O, 0);
+        path_draws.assign(s->n_paths, 0);
+        for (int64_t i = 0; i < N; ++i)
+            if (fflag[i] | sflag[i]) path_draws[fpath[i] & 0x3FFFFFFF] += fflag[i] + sflag[i];
         parallel_for(threads, N, 65536, [&](int64_t b, int64_t e) {
             for (int64_t i = b; i < e; ++i) {
                 int32_t ff = fflag[i], sf = sflag[i];
@@ -864,6 +871,7 @@ int or_get(const or_frame* fr, int stage, const void** ptr, size_t* bytes) {
         case SR_STAGE_DRAW_LIST: return set(F.draw.data(), F.draw.size() * 4);
         case SR_STAGE_IMAGE: return set(F.image.data(), F.image.size() * 4);
         case SR_STAGE_FRAG_LEFT: return set(F.fleft.data(), F.fleft.size() * 4);
+        case orc::kStagePathDraws: return set(F.path_draws.data(), F.path_draws.size() * 4);
         default: return 1;
     }
 }

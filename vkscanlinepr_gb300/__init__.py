@@ -75,7 +75,32 @@ STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment
 class BatchRenderOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("use_graph", ctypes.c_uint32),
                 ("record_capacity", ctypes.c_int64), ("refit_on_overflow", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("reserved", ctypes.c_uint32), ("draw_capacity", ctypes.c_int64)]
+
+
+SIZER_FEATURES, SIZER_OUTPUTS, SIZER_PARAMS, SIZER_NORM = 6, 2, 4738, 16
+
+
+class SizerTrainOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("batch", ctypes.c_uint32), ("epochs", ctypes.c_uint32),
+                ("shuffle", ctypes.c_uint32), ("lr", ctypes.c_float), ("beta1", ctypes.c_float),
+                ("beta2", ctypes.c_float), ("eps", ctypes.c_float), ("seed", ctypes.c_uint64)]
+
+
+class SizingMargins(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("path_records", ctypes.c_float), ("path_draws", ctypes.c_float),
+                ("frame_records", ctypes.c_float), ("frame_draws", ctypes.c_float)]
+
+
+class SizingPlan(ctypes.Structure):
+    _fields_ = [("records", ctypes.c_int64), ("draws", ctypes.c_int64), ("path_records", ctypes.c_int64),
+                ("path_draws", ctypes.c_int64), ("device_bytes", ctypes.c_uint64)]
+
+
+class SizingJudge(ctypes.Structure):
+    _fields_ = [("paths", ctypes.c_uint32), ("paths_over_records", ctypes.c_uint32),
+                ("paths_over_draws", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("records", ctypes.c_int64), ("draws", ctypes.c_int64)]
 
 
 class SynthParams(ctypes.Structure):
@@ -99,7 +124,12 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_scene_buf_free", "sr_exclusive_scan_i32", "sr_render_draw_list",
            "sr_exclusive_scan_i32_noalloc", "sr_batch_create", "sr_batch_add_scene", "sr_batch_add_synth",
            "sr_batch_commit", "sr_batch_set_mvp", "sr_batch_render", "sr_batch_get_image", "sr_batch_info",
-           "sr_batch_get_stats", "sr_batch_clear", "sr_batch_destroy"]
+           "sr_batch_get_stats", "sr_batch_clear", "sr_batch_destroy", "sr_scene_buf_size", "sr_host_alloc",
+           "sr_host_free", "sr_sizer_create", "sr_sizer_destroy", "sr_sizer_set_norm", "sr_sizer_get_state",
+           "sr_sizer_set_state", "sr_sizer_loss_grad", "sr_sizer_train", "sr_sizer_predict",
+           "sr_batch_path_features", "sr_batch_path_labels", "sr_batch_plan", "sr_batch_judge",
+           "sr_batch_frame_bytes", "sr_device_alloc", "sr_device_free", "sr_memcpy", "sr_batch_enqueue",
+           "sr_batch_query", "sr_batch_finish", "sr_batch_release", "sr_batch_held_bytes", "sr_batch_path_ranges"]
 
 _lib = None
 
@@ -149,6 +179,9 @@ def lib():
     L.sr_batch_commit.argtypes = [vp]
     L.sr_batch_set_mvp.argtypes = [vp, ctypes.c_uint32, vp]
     L.sr_batch_render.argtypes = [vp, ctypes.POINTER(BatchRenderOpts), vp]
+    L.sr_batch_enqueue.argtypes = [vp, ctypes.POINTER(BatchRenderOpts), vp]
+    L.sr_batch_query.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.sr_batch_finish.argtypes = [vp]
     L.sr_batch_get_image.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_int, vp]
     L.sr_batch_info.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
                                 ctypes.POINTER(ctypes.c_uint32)]
@@ -156,6 +189,29 @@ def lib():
     L.sr_batch_clear.argtypes = [vp]
     L.sr_batch_destroy.argtypes = [vp]
     L.sr_batch_destroy.restype = None
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.sr_sizer_create.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.sr_sizer_destroy.argtypes = [vp]
+    L.sr_sizer_destroy.restype = None
+    L.sr_sizer_set_norm.argtypes = [vp, vp]
+    L.sr_sizer_get_state.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_int64)]
+    L.sr_sizer_set_state.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int64]
+    L.sr_sizer_loss_grad.argtypes = [vp, vp, vp, ctypes.c_uint32, vp, fp]
+    L.sr_sizer_train.argtypes = [vp, vp, vp, ctypes.c_uint32, ctypes.POINTER(SizerTrainOpts), fp, vp]
+    L.sr_sizer_predict.argtypes = [vp, vp, ctypes.c_uint32, vp, vp]
+    L.sr_batch_path_features.argtypes = [vp, vp, vp]
+    L.sr_batch_path_labels.argtypes = [vp, vp, vp]
+    L.sr_batch_plan.argtypes = [vp, vp, ctypes.POINTER(SizingMargins), ctypes.POINTER(SizingPlan), vp, vp]
+    L.sr_batch_path_ranges.argtypes = [vp, vp]
+    L.sr_batch_judge.argtypes = [vp, ctypes.POINTER(SizingJudge), vp]
+    L.sr_batch_frame_bytes.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
+    L.sr_batch_release.argtypes = [vp]
+    L.sr_batch_held_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+    L.sr_device_alloc.argtypes = [ctypes.c_int, ctypes.c_size_t]
+    L.sr_device_alloc.restype = vp
+    L.sr_device_free.argtypes = [vp]
+    L.sr_device_free.restype = None
+    L.sr_memcpy.argtypes = [vp, vp, ctypes.c_size_t]
     _lib = L
     return L
 
@@ -459,9 +515,83 @@ class SceneBatch:
         a = np.ascontiguousarray(m, np.float32).reshape(16)
         _check(lib().sr_batch_set_mvp(self._h, int(index), a.ctypes.data))
 
-    def render(self, capacity=-1, graph=False, refit=True, stream=None):
-        o = BatchRenderOpts(ctypes.sizeof(BatchRenderOpts), 1 if graph else 0, int(capacity), 1 if refit else 0, 0)
+    def render(self, capacity=-1, graph=False, refit=True, stream=None, draw_capacity=-1):
+        o = BatchRenderOpts(ctypes.sizeof(BatchRenderOpts), 1 if graph else 0, int(capacity), 1 if refit else 0, 0,
+                            int(draw_capacity))
         _check(lib().sr_batch_render(self._h, ctypes.byref(o), stream))
+
+    def enqueue(self, capacity, graph=False, refit=True, stream=None, draw_capacity=-1):
+        """Queues a pre-sized frame and returns without waiting (see finish)."""
+        o = BatchRenderOpts(ctypes.sizeof(BatchRenderOpts), 1 if graph else 0, int(capacity), 1 if refit else 0, 0,
+                            int(draw_capacity))
+        _check(lib().sr_batch_enqueue(self._h, ctypes.byref(o), stream))
+
+    def done(self):
+        d = ctypes.c_int()
+        _check(lib().sr_batch_query(self._h, ctypes.byref(d)))
+        return bool(d.value)
+
+    def finish(self):
+        _check(lib().sr_batch_finish(self._h))
+
+    def n_paths(self):
+        return self.stats()["n_paths"]
+
+    def features(self, out=None, stream=None):
+        """Per-path sizing features under the current transforms: DeviceArray [P, 6]."""
+        n = self.n_paths()
+        out = out if out is not None else DeviceArray((n, SIZER_FEATURES), np.float32)
+        _check(lib().sr_batch_path_features(self._h, out.ptr, stream))
+        return out
+
+    def labels(self, out=None, stream=None):
+        """Renders once with exact sizing and per-path counters: DeviceArray [P, 2]
+        of log(1 + records), log(1 + draw records)."""
+        n = self.n_paths()
+        out = out if out is not None else DeviceArray((n, SIZER_OUTPUTS), np.float32)
+        _check(lib().sr_batch_path_labels(self._h, out.ptr, stream))
+        return out
+
+    def plan(self, sizer, margins, per_scene=False, stream=None):
+        """Capacities of the next frame from the sizing network.  margins:
+        (path_records, path_draws, frame_records, frame_draws) in log units."""
+        m = SizingMargins(ctypes.sizeof(SizingMargins), *[float(v) for v in margins])
+        p = SizingPlan()
+        sc = None
+        if per_scene:
+            sc = np.zeros((self.stats()["n_scenes"], 2), np.int64)
+        _check(lib().sr_batch_plan(self._h, sizer._h, ctypes.byref(m), ctypes.byref(p),
+                                   sc.ctypes.data if sc is not None else None, stream))
+        d = {k: getattr(p, k) for k, _ in SizingPlan._fields_}
+        if per_scene:
+            d["scenes"] = sc
+        return d
+
+    def path_ranges(self):
+        """First path of each scene (n_scenes + 1 entries)."""
+        out = np.zeros(self.stats()["n_scenes"] + 1, np.uint32)
+        _check(lib().sr_batch_path_ranges(self._h, out.ctypes.data))
+        return out
+
+    def judge(self, stream=None):
+        """Exact count pass against the last plan's per-path allotments."""
+        j = SizingJudge()
+        _check(lib().sr_batch_judge(self._h, ctypes.byref(j), stream))
+        return {k: getattr(j, k) for k, _ in SizingJudge._fields_ if k != "reserved"}
+
+    def release(self):
+        """Frees the record-sized buffers (scenes and images stay)."""
+        _check(lib().sr_batch_release(self._h))
+
+    def held_bytes(self):
+        b = ctypes.c_uint64()
+        _check(lib().sr_batch_held_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def frame_bytes(self, records, draws=-1):
+        b = ctypes.c_uint64()
+        _check(lib().sr_batch_frame_bytes(self._h, int(records), int(draws), ctypes.byref(b)))
+        return b.value
 
     def size(self, index):
         w, h = ctypes.c_uint32(), ctypes.c_uint32()
@@ -497,3 +627,178 @@ class SceneBatch:
             self.close()
         except Exception:
             pass
+
+
+class DeviceArray:
+    """Device memory owned through sr_device_alloc (no CUDA binding needed)."""
+
+    def __init__(self, shape, dtype, device=0):
+        self.shape = tuple(int(x) for x in np.atleast_1d(shape))
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        p = lib().sr_device_alloc(int(device), max(self.nbytes, 1))
+        if not p:
+            raise SRError(2, "sr_device_alloc of %d bytes failed" % self.nbytes)
+        self.ptr = ctypes.c_void_p(p)
+
+    @classmethod
+    def from_numpy(cls, a, device=0):
+        a = np.ascontiguousarray(a)
+        d = cls(a.shape, a.dtype, device)
+        if a.nbytes:
+            _check(lib().sr_memcpy(d.ptr, a.ctypes.data, a.nbytes))
+        return d
+
+    def numpy(self):
+        a = np.empty(self.shape, self.dtype)
+        if self.nbytes:
+            _check(lib().sr_memcpy(a.ctypes.data, self.ptr, self.nbytes))
+        return a
+
+    def rows(self, start, stop):
+        """A view of rows [start, stop) (no copy; valid while self lives)."""
+        v = DeviceArray.__new__(DeviceArray)
+        row = int(np.prod(self.shape[1:])) * self.dtype.itemsize
+        v.shape = (stop - start,) + self.shape[1:]
+        v.dtype = self.dtype
+        v.nbytes = (stop - start) * row
+        v.ptr = ctypes.c_void_p(self.ptr.value + start * row)
+        v._base = self
+        return v
+
+    def free(self):
+        if getattr(self, "_base", None) is None and self.ptr:
+            lib().sr_device_free(self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def concat_device(arrays):
+    """Concatenates device arrays along rows into a new DeviceArray."""
+    rows = sum(a.shape[0] for a in arrays)
+    out = DeviceArray((rows,) + arrays[0].shape[1:], arrays[0].dtype)
+    off = 0
+    for a in arrays:
+        if a.nbytes:
+            _check(lib().sr_memcpy(ctypes.c_void_p(out.ptr.value + off), a.ptr, a.nbytes))
+        off += a.nbytes
+    return out
+
+
+def sizer_norm(features, labels):
+    """Normaliser (x mean, x inverse std, y mean, y std) of host arrays."""
+    f = np.asarray(features, np.float64)
+    t = np.asarray(labels, np.float64)
+    xs = f.std(0)
+    ys = t.std(0)
+    xs[xs < 1e-6] = 1.0
+    ys[ys < 1e-6] = 1.0
+    return np.concatenate([f.mean(0), 1.0 / xs, t.mean(0), ys]).astype(np.float32)
+
+
+class Sizer:
+    """The learned-sizing network (sr_sizer_*): 6 -> 64 -> 64 -> 2 GELU,
+    BF16 weights with FP32 accumulation, Adam, all on the GPU."""
+
+    def __init__(self, device=0, seed=0):
+        h = ctypes.c_void_p()
+        _check(lib().sr_sizer_create(int(device), int(seed), ctypes.byref(h)))
+        self._h = h
+        self.device = device
+
+    def set_norm(self, norm):
+        a = np.ascontiguousarray(norm, np.float32).reshape(SIZER_NORM)
+        _check(lib().sr_sizer_set_norm(self._h, a.ctypes.data))
+
+    def state(self):
+        p = np.empty(SIZER_PARAMS, np.float32)
+        m = np.empty(SIZER_PARAMS, np.float32)
+        v = np.empty(SIZER_PARAMS, np.float32)
+        nm = np.empty(SIZER_NORM, np.float32)
+        step = ctypes.c_int64()
+        _check(lib().sr_sizer_get_state(self._h, p.ctypes.data, m.ctypes.data, v.ctypes.data, nm.ctypes.data,
+                                        ctypes.byref(step)))
+        return {"params": p, "adam_m": m, "adam_v": v, "norm": nm, "step": step.value}
+
+    def load_state(self, st):
+        arr = {k: np.ascontiguousarray(st[k], np.float32) for k in ("params", "adam_m", "adam_v", "norm")}
+        _check(lib().sr_sizer_set_state(self._h, arr["params"].ctypes.data, arr["adam_m"].ctypes.data,
+                                        arr["adam_v"].ctypes.data, arr["norm"].ctypes.data, int(st["step"])))
+
+    def save(self, path):
+        np.savez(path, **self.state())
+
+    def load(self, path):
+        with np.load(path) as z:
+            self.load_state({k: z[k] for k in z.files})
+
+    def loss_grad(self, x, t):
+        g = np.empty(SIZER_PARAMS, np.float32)
+        loss = ctypes.c_float()
+        _check(lib().sr_sizer_loss_grad(self._h, x.ptr, t.ptr, int(x.shape[0]), g.ctypes.data, ctypes.byref(loss)))
+        return float(loss.value), g
+
+    def train(self, x, t, epochs=1, batch=4096, lr=1e-3, shuffle=True, seed=0, beta1=0.9, beta2=0.999, eps=1e-8,
+              stream=None):
+        o = SizerTrainOpts(ctypes.sizeof(SizerTrainOpts), int(batch), int(epochs), 1 if shuffle else 0, lr, beta1,
+                           beta2, eps, int(seed))
+        loss = ctypes.c_float()
+        _check(lib().sr_sizer_train(self._h, x.ptr, t.ptr, int(x.shape[0]), ctypes.byref(o), ctypes.byref(loss),
+                                    stream))
+        return float(loss.value)
+
+    def predict(self, x, out=None, stream=None):
+        n = int(x.shape[0])
+        out = out if out is not None else DeviceArray((n, SIZER_OUTPUTS), np.float32, self.device)
+        _check(lib().sr_sizer_predict(self._h, x.ptr, n, out.ptr, stream))
+        return out
+
+    def close(self):
+        if self._h:
+            lib().sr_sizer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def calibrate_margins(pred, labels, path_begin, path_quantile=0.995, frame_slack=0.02):
+    """Sizing margins from held-out rows: pred and labels [P, 2] in
+    log(1 + count) units, path_begin [S + 1] the scenes' path ranges.
+
+    The path margins are the `path_quantile` quantile of the per-path
+    residuals (so about 1 - path_quantile of the paths exceed their
+    allotment).  The frame margins are the smallest margins under which the
+    summed capacity of every held-out scene covers its exact count, plus
+    `frame_slack`."""
+    pred = np.asarray(pred, np.float64)
+    lab = np.asarray(labels, np.float64)
+    exact = np.rint(np.expm1(lab))
+    out = []
+    for o in range(2):
+        out.append(float(np.quantile(lab[:, o] - pred[:, o], path_quantile)))
+    for o in range(2):
+        need = -np.inf
+        for s in range(len(path_begin) - 1):
+            a, b = int(path_begin[s]), int(path_begin[s + 1])
+            if b <= a:
+                continue
+            want = exact[a:b, o].sum()
+            if want <= 0:
+                continue
+            lo, hi = -8.0, 8.0
+            for _ in range(40):      # smallest m with sum(ceil(expm1(pred + m))) >= want
+                mid = 0.5 * (lo + hi)
+                got = np.ceil(np.expm1(np.minimum(pred[a:b, o] + mid, 21.0))).clip(0).sum()
+                lo, hi = (lo, mid) if got >= want else (mid, hi)
+            need = max(need, hi)
+        out.append(float((need if np.isfinite(need) else 0.0) + frame_slack))
+    return tuple(out)

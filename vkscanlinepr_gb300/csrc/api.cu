@@ -16,6 +16,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -212,12 +213,18 @@ struct Pipeline {
     DevBuf cbuf, rec, keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status, draw, draw_row, totals;
     DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, image;
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
+    // learned sizing: per-path curve ranges, draw counters, features,
+    // predictions, allotments and their sums
+    DevBuf path_first, path_draw, feats, preds, allot, plan_tot, judge_out;
+    bool path_first_valid = false, count_paths = false, planned = false;
+    unsigned long long* h_plan_ptr = nullptr;   // pinned plan totals
+    size_t h_plan_words = 0;
     // host scalars (pinned): N, status; fragments, spans
     uint32_t* h_u32 = nullptr;
     uint64_t* h_u64 = nullptr;
     // results
     sr_stats stats{};
-    int64_t last_N = 0, last_O = 0, last_cap = 0;
+    int64_t last_N = 0, last_O = 0, last_cap = 0, last_dcap = 0;
     bool stages_valid = false;
     // profiling
     cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
@@ -230,12 +237,14 @@ struct Pipeline {
                          &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf, &rec, &keys, &keys_alt,
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
                          &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &image, &d_fkey,
-                         &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
+                         &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
+                         &feats, &preds, &allot, &plan_tot, &judge_out};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
         if (h_u32) cudaFreeHost(h_u32);
         if (h_u64) cudaFreeHost(h_u64);
+        if (h_plan_ptr) cudaFreeHost(h_plan_ptr);
     }
 
     sr_status init(int dev, int32_t m, uint32_t fl) {
@@ -333,6 +342,8 @@ struct Pipeline {
         SR_TRY(upload_table());
         loaded = true;
         stages_valid = false;
+        path_first_valid = false;
+        planned = false;
         return SR_OK;
     }
 
@@ -373,6 +384,8 @@ struct Pipeline {
         SR_TRY(upload_table());
         loaded = true;
         stages_valid = false;
+        path_first_valid = false;
+        planned = false;
         return SR_OK;
     }
 
@@ -433,30 +446,96 @@ struct Pipeline {
         return SR_OK;
     }
 
-    // Buffers of the stages after the count, for `cap` records.
-    sr_status reserve(int64_t cap) {
+    // Draw-record capacity: every record gives at most one merged fragment
+    // and one span, so 2 x records always suffices.
+    static int64_t draw_cap_for(int64_t cap, int64_t dcap) {
+        return dcap > 0 ? dcap : 2 * std::max<int64_t>(cap, 1);
+    }
+
+    // Bytes each post-count buffer needs for `cap` records and `dcap` draw
+    // records; fn(buffer, bytes) is called once per buffer.
+    template <typename Fn>
+    void post_count_buffers(int64_t cap, int64_t dcap, Fn&& fn) {
         const size_t n1 = (size_t)std::max<int64_t>(cap, 1);
-        CUDA_TRY(ensure(cbuf, sizeof(int32_t) * n1));
-        CUDA_TRY(ensure(rec, sizeof(int2) * n1));
-        CUDA_TRY(ensure(keys, sizeof(uint64_t) * n1));
-        CUDA_TRY(ensure(keys_alt, sizeof(uint64_t) * n1));
-        CUDA_TRY(ensure(skeys, sizeof(uint64_t) * n1));
-        CUDA_TRY(ensure(wnp, n1));
-        CUDA_TRY(ensure(svals, sizeof(uint32_t) * n1));
-        CUDA_TRY(ensure(vals_alt, sizeof(uint32_t) * n1));
+        fn(cbuf, sizeof(int32_t) * n1);
+        fn(rec, sizeof(int2) * n1);
+        fn(keys, sizeof(uint64_t) * n1);
+        fn(keys_alt, sizeof(uint64_t) * n1);
+        fn(skeys, sizeof(uint64_t) * n1);
+        fn(wnp, n1);
+        fn(svals, sizeof(uint32_t) * n1);
+        fn(vals_alt, sizeof(uint32_t) * n1);
         const sr::KeyLayout L = layout();
-        sr::SortPlan sp = sr::sort_plan(cap, L.pbits + L.rbits + L.xbits, nullptr);
-        CUDA_TRY(ensure(sort_scratch, sr::sort_scratch_bytes(sp)));
-        CUDA_TRY(ensure(wind_status, sizeof(uint64_t) * sr::winding_status_words(cap)));
-        const size_t d1 = 2 * n1;
-        CUDA_TRY(ensure(draw, sizeof(int4) * d1));
-        CUDA_TRY(ensure(draw_row, sizeof(uint32_t) * d1));
-        CUDA_TRY(ensure(rkeys, sizeof(uint32_t) * d1));
-        CUDA_TRY(ensure(rvals, sizeof(uint32_t) * d1));
-        CUDA_TRY(ensure(rkeys_alt, sizeof(uint32_t) * d1));
-        CUDA_TRY(ensure(rvals_alt, sizeof(uint32_t) * d1));
-        sr::SortPlan rp = sr::sort_plan((int64_t)d1, bits_for(total_rows), nullptr);
-        CUDA_TRY(ensure(row_sort_scratch, sr::sort_scratch_bytes(rp)));
+        fn(sort_scratch, sr::sort_scratch_bytes(sr::sort_plan(cap, L.pbits + L.rbits + L.xbits, nullptr)));
+        fn(wind_status, sizeof(uint64_t) * sr::winding_status_words(cap));
+        const size_t d1 = (size_t)draw_cap_for(cap, dcap);
+        fn(draw, sizeof(int4) * d1);
+        fn(draw_row, sizeof(uint32_t) * d1);
+        fn(rkeys, sizeof(uint32_t) * d1);
+        fn(rvals, sizeof(uint32_t) * d1);
+        fn(rkeys_alt, sizeof(uint32_t) * d1);
+        fn(rvals_alt, sizeof(uint32_t) * d1);
+        fn(row_sort_scratch, sr::sort_scratch_bytes(sr::sort_plan((int64_t)d1, bits_for(total_rows), nullptr)));
+    }
+
+    // Device bytes a frame of this scene set holds with capacities (cap,
+    // dcap): scene arrays, per-frame arrays, post-count buffers and images,
+    // each rounded as the allocator rounds it.
+    uint64_t frame_bytes(int64_t cap, int64_t dcap) {
+        uint64_t total = 0;
+        auto add = [&](size_t b) {
+            size_t want = std::max<size_t>(b + b / 4, 256);
+            total += (want + 255) & ~(size_t)255;
+        };
+        const size_t v1 = std::max<uint32_t>(V, 1), c1 = std::max<uint32_t>(C, 1), p1 = std::max<uint32_t>(P, 1);
+        add(8 * v1); add(4 * v1);                                   // pos, pos_path
+        add(4 * c1); add(4 * c1); add(4 * c1);                      // curve arrays
+        add(4 * p1); add(4 * p1); add(4 * p1);                      // fill rule/info, path scene
+        add(sizeof(sr::SceneInfo) * std::max<uint32_t>(S, 1)); add(4 * ((size_t)S + 1));
+        add(4 * std::max<uint64_t>(total_pixels, 1));               // images
+        add(8 * v1); add(4 * p1); add(20 * c1); add(4 * (c1 + 1)); add(4 * (c1 + 1));
+        add(8 * sr::scan_status_words(C)); add(sr::piece_table_bytes((uint32_t)c1));
+        const size_t lc = list_cap();
+        add(4 * 6 * lc); add(4 * lc);
+        add(sr::sort_scratch_bytes(sr::sort_plan((int64_t)lc, sr::chain_key_bits(), nullptr)));
+        add(32); add(4 * ((size_t)total_rows + 1));
+        post_count_buffers(cap, dcap, [&](DevBuf&, size_t b) { add(b); });
+        return total;
+    }
+
+    // Frees the buffers sized by the record count (they are reallocated by
+    // the next frame).
+    void release_post_count() {
+        post_count_buffers(0, 0, [](DevBuf& b, size_t) { release(b); });
+        DevBuf* dbg[] = {&d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
+        for (DevBuf* b : dbg) release(*b);
+        stages_valid = false;
+    }
+
+    // Device bytes currently held by this pipeline.
+    uint64_t held_bytes() const {
+        const DevBuf* all[] = {&pos, &pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info,
+                               &path_scene, &scenes_d, &cta_base_d, &tpos, &path_visible, &cut, &count, &offs,
+                               &ctl, &scan_status, &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf,
+                               &rec, &keys, &keys_alt, &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status,
+                               &draw, &draw_row, &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt,
+                               &row_sort_scratch, &row_start, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan,
+                               &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
+                               &plan_tot, &judge_out};
+        uint64_t t = 0;
+        for (const DevBuf* b : all) t += b->cap;
+        return t;
+    }
+
+    // Buffers of the stages after the count, for `cap` records and `dcap`
+    // draw records.
+    sr_status reserve(int64_t cap, int64_t dcap) {
+        cudaError_t err = cudaSuccess;
+        post_count_buffers(cap, dcap, [&](DevBuf& b, size_t bytes) {
+            if (err == cudaSuccess) err = ensure(b, bytes);
+        });
+        CUDA_TRY(err);
+        const size_t n1 = (size_t)std::max<int64_t>(cap, 1);
         if (flags & SR_FLAG_KEEP_STAGES) {
             CUDA_TRY(ensure(d_fkey, sizeof(int32_t) * n1));
             CUDA_TRY(ensure(d_fwn, sizeof(int32_t) * n1));
@@ -478,6 +557,7 @@ struct Pipeline {
         CUDA_TRY(cudaMemsetAsync(path_visible.p, 0, sizeof(int32_t) * std::max<uint32_t>(P, 1), st));
         CUDA_TRY(cudaMemsetAsync(scan_status.p, 0, sizeof(uint64_t) * scan_status_words(C), st));
         CUDA_TRY(cudaMemsetAsync(totals.p, 0, sizeof(uint64_t) * 4, st));
+        if (count_paths) CUDA_TRY(cudaMemsetAsync(path_draw.p, 0, sizeof(uint32_t) * std::max<uint32_t>(P, 1), st));
         mark(ST_TRANSFORM, false);
         launch_transform(pos.as<float2>(), pos_path.as<uint32_t>(), V, table(), tpos.as<float2>(),
                          path_visible.as<int32_t>(), st);
@@ -502,7 +582,7 @@ struct Pipeline {
 
     // Everything after the count, sized for `cap` records (no allocation,
     // no wait).  The kernels read the actual count from offs[C].
-    sr_status enqueue_back(cudaStream_t st, int64_t cap) {
+    sr_status enqueue_back(cudaStream_t st, int64_t cap, int64_t dcap_req) {
         using namespace sr;
         uint32_t* ctlp = ctl.as<uint32_t>();
         uint32_t* status = ctlp + CTL_STATUS;
@@ -549,10 +629,12 @@ struct Pipeline {
         wa.L = L;
         wa.st = table();
         wa.draw = draw.as<int4>();
-        wa.draw_capacity = 2 * std::max<int64_t>(cap, 1);
+        const int64_t dcap = draw_cap_for(cap, dcap_req);
+        wa.draw_capacity = dcap;
         wa.draw_row = draw_row.as<uint32_t>();
         wa.totals = totals.as<uint64_t>();
         wa.n_draw = ctlp + CTL_NDRAW;
+        wa.path_draw = count_paths ? path_draw.as<uint32_t>() : nullptr;
         wa.dbg_wscan = keep ? d_wscan.as<int32_t>() : nullptr;
         wa.dbg_fflag = keep ? d_fflag.as<int32_t>() : nullptr;
         wa.dbg_sflag = keep ? d_sflag.as<int32_t>() : nullptr;
@@ -560,7 +642,6 @@ struct Pipeline {
         mark(ST_WINDING, false);
         launch_winding_emit(wa, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
         mark(ST_WINDING, true);
-        const int64_t dcap = 2 * std::max<int64_t>(cap, 1);
         SortPlan rp = sort_plan(dcap, bits_for(total_rows), ctlp + CTL_NDRAW);
         mark(ST_ROWSORT, false);
         launch_sort_u32(rp, draw_row.as<uint32_t>(), nullptr, rkeys.as<uint32_t>(), rvals.as<uint32_t>(),
@@ -598,8 +679,9 @@ struct Pipeline {
     }
 
     // One frame.  cap < 0: size the record buffers exactly (one host wait
-    // for N); cap >= 0: use that capacity without waiting.
-    sr_status frame(cudaStream_t st, int64_t cap) {
+    // for N); cap >= 0: use that capacity without waiting.  dcap <= 0 sizes
+    // the draw records at 2 x cap.
+    sr_status frame(cudaStream_t st, int64_t cap, int64_t dcap = -1) {
         CUDA_TRY(cudaSetDevice(device));
         if (!loaded) return fail(SR_ERR_NO_SCENE, "render before a scene was loaded");
         cur = st;
@@ -611,21 +693,34 @@ struct Pipeline {
             int64_t N = 0;
             SR_TRY(read_count(st, &N));
             cap = N;
+            dcap = -1;
         }
-        SR_TRY(reserve(cap));
-        SR_TRY(enqueue_back(st, cap));
+        SR_TRY(reserve(cap, dcap));
+        SR_TRY(enqueue_back(st, cap, dcap));
         stats.kernel_launches = (uint32_t)(sr::launches_so_far() - launches0);
         ev_pending = (flags & SR_FLAG_PROFILE) != 0;
         last_cap = cap;
+        last_dcap = draw_cap_for(cap, dcap);
         return SR_OK;
     }
 
     // Waits for the frame and collects its counters and status.
-    sr_status finish(cudaStream_t st) {
+    // Queues the copies of the frame's counters into pinned host memory.
+    sr_status enqueue_readback(cudaStream_t st) {
         CUDA_TRY(cudaMemcpyAsync(&h_u32[0], offs.as<int32_t>() + C, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(&h_u32[1], ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(h_u64, totals.p, sizeof(uint64_t) * 2, cudaMemcpyDeviceToHost, st));
+        return SR_OK;
+    }
+
+    sr_status finish(cudaStream_t st) {
+        SR_TRY(enqueue_readback(st));
         CUDA_TRY(cudaStreamSynchronize(st));
+        return collect();
+    }
+
+    // The frame's counters and status, once the read-back has landed.
+    sr_status collect() {
         last_N = (int64_t)(int32_t)h_u32[0];
         last_O = (int64_t)(h_u64[0] + h_u64[1]);
         stats.n_intersections = (uint64_t)last_N;
@@ -639,6 +734,9 @@ struct Pipeline {
         if (last_N > last_cap)
             return fail(SR_ERR_OVERFLOW_REFIT, "frame needs %lld records, capacity %lld", (long long)last_N,
                         (long long)last_cap);
+        if (last_O > last_dcap)
+            return fail(SR_ERR_OVERFLOW_REFIT, "frame needs %lld draw records, capacity %lld", (long long)last_O,
+                        (long long)last_dcap);
         stages_valid = (flags & SR_FLAG_KEEP_STAGES) != 0;
         return SR_OK;
     }
@@ -669,16 +767,45 @@ struct sr_batch {
     bool committed = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int64_t graph_cap = -1;
+    int64_t graph_cap = -1, graph_dcap = -1;
     uint32_t graph_launches = 0;
     uint32_t overflows = 0, refits = 0;
     cudaStream_t cap_stream = nullptr;   // captures run here: the legacy stream cannot be captured
+    // a frame enqueued by sr_batch_enqueue and not yet finished
+    bool inflight = false;
+    cudaEvent_t done = nullptr;
+    sr_batch_render_opts pending{};
+    cudaStream_t pending_stream = nullptr;
     ~sr_batch() {
+        if (done) cudaEventDestroy(done);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (cap_stream) cudaStreamDestroy(cap_stream);
     }
 };
+
+static_assert(SR_SIZER_PARAMS == sr::kMlpParams && SR_SIZER_FEATURES == sr::kMlpIn &&
+                  SR_SIZER_OUTPUTS == sr::kMlpOut && SR_SIZER_NORM == sr::kMlpNorm,
+              "sizer constants");
+
+// The learned-sizing network: parameters, Adam state and training scratch
+// on one device.
+struct sr_sizer {
+    int device = 0, sm_count = 148;
+    DevBuf master, wb, grad, m, v, norm, loss;   // loss: one float
+    DevBuf keys, perm, keys_out, alt_k, alt_v, sort_scratch, ctl;
+    int64_t step = 0;
+    float* h_loss = nullptr;
+    ~sr_sizer() {
+        DevBuf* all[] = {&master, &wb, &grad, &m, &v, &norm, &loss, &keys, &perm, &keys_out, &alt_k, &alt_v,
+                         &sort_scratch, &ctl};
+        for (DevBuf* b : all) release(*b);
+        if (h_loss) cudaFreeHost(h_loss);
+    }
+};
+
+// Per-path curve ranges of a batch (curves are grouped by path in order).
+static sr_status batch_path_first(sr_batch* b);
 
 extern "C" {
 
@@ -958,6 +1085,7 @@ sr_status sr_batch_add_synth(sr_batch* b, const sr_synth_params* prm, uint32_t c
 
 sr_status sr_batch_commit(sr_batch* b) {
     if (!b) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (b->inflight) return fail(SR_ERR_INVALID_ARG, "commit while a frame is in flight");
     SR_TRY(b->p.upload(b->h));
     b->committed = true;
     if (b->exec) {
@@ -969,6 +1097,7 @@ sr_status sr_batch_commit(sr_batch* b) {
         b->graph = nullptr;
     }
     b->graph_cap = -1;
+    b->graph_dcap = -1;
     return SR_OK;
 }
 
@@ -983,29 +1112,37 @@ sr_status sr_batch_set_mvp(sr_batch* b, uint32_t index, const float m[16]) {
     return SR_OK;
 }
 
-sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* o, void* stream) {
-    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
-    if (!b->committed) SR_TRY(sr_batch_commit(b));
-    sr_batch_render_opts d{};
-    d.struct_size = sizeof(d);
-    d.record_capacity = -1;
+static sr_status batch_opts(const sr_batch_render_opts* o, sr_batch_render_opts* d) {
+    std::memset(d, 0, sizeof *d);
+    d->struct_size = sizeof *d;
+    d->record_capacity = -1;
+    d->draw_capacity = -1;
     if (o) {
-        if (o->struct_size < sizeof(sr_batch_render_opts)) return fail(SR_ERR_INVALID_ARG, "opts.struct_size too small");
-        d = *o;
+        const size_t base = offsetof(sr_batch_render_opts, draw_capacity);
+        if (o->struct_size < base) return fail(SR_ERR_INVALID_ARG, "opts.struct_size too small");
+        std::memcpy(d, o, o->struct_size < sizeof *d ? base : sizeof *d);
+        d->struct_size = sizeof *d;
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return SR_OK;
+}
+
+// Enqueues one frame of the batch (with exact sizing this waits once for
+// the record count); the frame's end is recorded in b->done.
+static sr_status batch_enqueue(sr_batch* b, const sr_batch_render_opts& d, cudaStream_t st) {
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
     Pipeline& p = b->p;
     CUDA_TRY(cudaSetDevice(p.device));
     const int64_t cap = d.record_capacity;
+    const int64_t dcap = cap >= 0 ? Pipeline::draw_cap_for(cap, d.draw_capacity) : -1;
     if (cap >= 0 && d.use_graph) {
-        if (!b->exec || b->graph_cap != cap) {
+        if (!b->exec || b->graph_cap != cap || b->graph_dcap != dcap) {
             if (b->exec) cudaGraphExecDestroy(b->exec);
             if (b->graph) cudaGraphDestroy(b->graph);
             b->exec = nullptr;
             b->graph = nullptr;
             // one plain frame first: it allocates every buffer and sets the
             // kernels' attributes, so the capture records launches only
-            SR_TRY(p.frame(st, cap));
+            SR_TRY(p.frame(st, cap, dcap));
             sr_status fs = p.finish(st);
             if (fs != SR_OK && fs != SR_ERR_OVERFLOW_REFIT) return fs;
             if (!b->cap_stream) CUDA_TRY(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
@@ -1017,7 +1154,7 @@ sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* o, void* stre
             sr_status s1 = SR_OK, s2 = SR_OK;
             if (e == cudaSuccess) {
                 s1 = p.enqueue_front(cs);
-                if (s1 == SR_OK) s2 = p.enqueue_back(cs, cap);
+                if (s1 == SR_OK) s2 = p.enqueue_back(cs, cap, dcap);
                 cudaError_t e2 = cudaStreamEndCapture(cs, &b->graph);   // always end the capture
                 if (e2 != cudaSuccess) e = e2;
             }
@@ -1027,16 +1164,33 @@ sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* o, void* stre
             CUDA_TRY(e);
             CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
             b->graph_cap = cap;
+            b->graph_dcap = dcap;
             b->graph_launches = (uint32_t)(sr::launches_so_far() - l0);
         }
         CUDA_TRY(cudaGraphLaunch(b->exec, st));
         p.last_cap = cap;
+        p.last_dcap = dcap;
         p.stats.kernel_launches = b->graph_launches;
         p.ev_pending = false;
     } else {
-        SR_TRY(p.frame(st, cap));
+        SR_TRY(p.frame(st, cap, dcap));
     }
-    sr_status s = p.finish(st);
+    SR_TRY(p.enqueue_readback(st));
+    if (!b->done) CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(b->done, st));
+    b->inflight = true;
+    return SR_OK;
+}
+
+// Waits for the enqueued frame; on overflow reruns it with exact sizing
+// when asked to.
+static sr_status batch_finish(sr_batch* b, const sr_batch_render_opts& d, cudaStream_t st) {
+    Pipeline& p = b->p;
+    CUDA_TRY(cudaSetDevice(p.device));
+    b->inflight = false;
+    // wait for this frame only: later work on the same stream may still run
+    CUDA_TRY(cudaEventSynchronize(b->done));
+    sr_status s = p.collect();
     if (s == SR_ERR_OVERFLOW_REFIT && d.refit_on_overflow) {
         ++b->overflows;
         ++b->refits;
@@ -1046,6 +1200,49 @@ sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* o, void* stre
         ++b->overflows;
     }
     return s;
+}
+
+sr_status sr_batch_render(sr_batch* b, const sr_batch_render_opts* o, void* stream) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
+    sr_batch_render_opts d;
+    SR_TRY(batch_opts(o, &d));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SR_TRY(batch_enqueue(b, d, st));
+    return batch_finish(b, d, st);
+}
+
+sr_status sr_batch_enqueue(sr_batch* b, const sr_batch_render_opts* o, void* stream) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
+    if (b->inflight) return fail(SR_ERR_INVALID_ARG, "batch already has a frame in flight");
+    sr_batch_render_opts d;
+    SR_TRY(batch_opts(o, &d));
+    if (d.record_capacity < 0) return fail(SR_ERR_INVALID_ARG, "sr_batch_enqueue needs record_capacity >= 0");
+    b->pending = d;
+    b->pending_stream = static_cast<cudaStream_t>(stream);
+    return batch_enqueue(b, d, b->pending_stream);
+}
+
+sr_status sr_batch_query(sr_batch* b, int* done) {
+    if (!b || !done) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!b->inflight) {
+        *done = 1;
+        return SR_OK;
+    }
+    CUDA_TRY(cudaSetDevice(b->p.device));
+    cudaError_t e = cudaEventQuery(b->done);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return SR_OK;
+    }
+    CUDA_TRY(e);
+    *done = 1;
+    return SR_OK;
+}
+
+sr_status sr_batch_finish(sr_batch* b) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
+    if (!b->inflight) return fail(SR_ERR_INVALID_ARG, "no frame in flight");
+    return batch_finish(b, b->pending, b->pending_stream);
 }
 
 sr_status sr_batch_get_image(sr_batch* b, uint32_t index, void* rgba_out, int out_is_device, void* stream) {
@@ -1096,4 +1293,397 @@ void sr_batch_destroy(sr_batch* b) {
     delete b;
 }
 
+// ------------------------------------------------------- learned sizing ---
+
+sr_status sr_sizer_create(int device, uint64_t seed, sr_sizer** out) {
+    if (!out) return fail(SR_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(SR_ERR_INVALID_ARG, "device %d not present", device);
+    CUDA_TRY(cudaSetDevice(device));
+    sr_sizer* s = new sr_sizer();
+    s->device = device;
+    cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, device);
+    const size_t pb = sizeof(float) * sr::kMlpParams;
+    auto alloc = [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = ensure(s->master, pb)) || (e = ensure(s->wb, 2 * (size_t)sr::kMlpParams)) ||
+            (e = ensure(s->grad, pb)) || (e = ensure(s->m, pb)) || (e = ensure(s->v, pb)) ||
+            (e = ensure(s->norm, sizeof(float) * sr::kMlpNorm)) || (e = ensure(s->loss, sizeof(float) * 4)) ||
+            (e = ensure(s->ctl, sizeof(uint32_t) * 4)) || (e = cudaMallocHost(&s->h_loss, sizeof(float) * 4)))
+            return e;
+        return cudaSuccess;
+    };
+    cudaError_t e = alloc();
+    if (e != cudaSuccess) {
+        delete s;
+        CUDA_TRY(e);
+    }
+    // weights: uniform with variance 1/fan_in from a splitmix64 stream
+    std::vector<float> w(sr::kMlpParams, 0.0f);
+    uint64_t state = seed;
+    auto next = [&]() {
+        uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    const int H = sr::kMlpHidden, I = sr::kMlpIn, O = sr::kMlpOut;
+    struct Layer { int off, rows, fan_in; } layers[3] = {{0, H, I}, {H * I + H, H, H}, {H * I + H + H * H + H, O, H}};
+    for (const Layer& l : layers) {
+        const double a = std::sqrt(3.0 / l.fan_in);
+        for (int i = 0; i < l.rows * l.fan_in; ++i) w[(size_t)l.off + i] = (float)((2.0 * next() - 1.0) * a);
+    }
+    float nm[sr::kMlpNorm];
+    for (int i = 0; i < sr::kMlpNorm; ++i) nm[i] = 0.0f;
+    for (int i = 0; i < I; ++i) nm[I + i] = 1.0f;
+    for (int i = 0; i < O; ++i) nm[2 * I + O + i] = 1.0f;
+    sr_status st = sr_sizer_set_state(s, w.data(), nullptr, nullptr, nm, 0);
+    if (st != SR_OK) {
+        delete s;
+        return st;
+    }
+    *out = s;
+    return SR_OK;
+}
+
+void sr_sizer_destroy(sr_sizer* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    cudaDeviceSynchronize();
+    delete s;
+}
+
+sr_status sr_sizer_set_norm(sr_sizer* s, const float norm[SR_SIZER_NORM]) {
+    if (!s || !norm) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    for (int i = 0; i < sr::kMlpNorm; ++i)
+        if (!std::isfinite(norm[i])) return fail(SR_ERR_INVALID_ARG, "normaliser entry %d is not finite", i);
+    for (int i = 0; i < sr::kMlpOut; ++i)
+        if (!(norm[2 * sr::kMlpIn + sr::kMlpOut + i] > 0.0f)) return fail(SR_ERR_INVALID_ARG, "y_std must be > 0");
+    CUDA_TRY(cudaSetDevice(s->device));
+    CUDA_TRY(cudaMemcpy(s->norm.p, norm, sizeof(float) * sr::kMlpNorm, cudaMemcpyHostToDevice));
+    return SR_OK;
+}
+
+sr_status sr_sizer_get_state(const sr_sizer* s, float* params, float* adam_m, float* adam_v, float norm[SR_SIZER_NORM],
+                             int64_t* step) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "NULL sizer");
+    CUDA_TRY(cudaSetDevice(s->device));
+    const size_t pb = sizeof(float) * sr::kMlpParams;
+    if (params) CUDA_TRY(cudaMemcpy(params, s->master.p, pb, cudaMemcpyDeviceToHost));
+    if (adam_m) CUDA_TRY(cudaMemcpy(adam_m, s->m.p, pb, cudaMemcpyDeviceToHost));
+    if (adam_v) CUDA_TRY(cudaMemcpy(adam_v, s->v.p, pb, cudaMemcpyDeviceToHost));
+    if (norm) CUDA_TRY(cudaMemcpy(norm, s->norm.p, sizeof(float) * sr::kMlpNorm, cudaMemcpyDeviceToHost));
+    if (step) *step = s->step;
+    return SR_OK;
+}
+
+sr_status sr_sizer_set_state(sr_sizer* s, const float* params, const float* adam_m, const float* adam_v,
+                             const float norm[SR_SIZER_NORM], int64_t step) {
+    if (!s || step < 0) return fail(SR_ERR_INVALID_ARG, "bad argument");
+    CUDA_TRY(cudaSetDevice(s->device));
+    const size_t pb = sizeof(float) * sr::kMlpParams;
+    if (norm) SR_TRY(sr_sizer_set_norm(s, norm));
+    if (params) {
+        for (int i = 0; i < sr::kMlpParams; ++i)
+            if (!std::isfinite(params[i])) return fail(SR_ERR_INVALID_ARG, "parameter %d is not finite", i);
+        CUDA_TRY(cudaMemcpy(s->master.p, params, pb, cudaMemcpyHostToDevice));
+        sr::launch_to_bf16(s->master.as<float>(), s->wb.p, nullptr);
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (adam_m) CUDA_TRY(cudaMemcpy(s->m.p, adam_m, pb, cudaMemcpyHostToDevice));
+    else CUDA_TRY(cudaMemset(s->m.p, 0, pb));
+    if (adam_v) CUDA_TRY(cudaMemcpy(s->v.p, adam_v, pb, cudaMemcpyHostToDevice));
+    else CUDA_TRY(cudaMemset(s->v.p, 0, pb));
+    CUDA_TRY(cudaMemset(s->grad.p, 0, pb));
+    s->step = step;
+    CUDA_TRY(cudaDeviceSynchronize());
+    return SR_OK;
+}
+
+sr_status sr_sizer_loss_grad(sr_sizer* s, const float* d_x, const float* d_t, uint32_t n, float* h_grad,
+                             float* h_loss) {
+    if (!s || (n && (!d_x || !d_t))) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0) return fail(SR_ERR_INVALID_ARG, "no rows");
+    CUDA_TRY(cudaSetDevice(s->device));
+    const size_t pb = sizeof(float) * sr::kMlpParams;
+    CUDA_TRY(cudaMemset(s->grad.p, 0, pb));
+    CUDA_TRY(cudaMemset(s->loss.p, 0, sizeof(float)));
+    CUDA_TRY(sr::launch_mlp_grad(s->wb.p, s->master.as<float>(), s->norm.as<float>(), d_x, d_t, nullptr, n,
+                                 s->grad.as<float>(), s->loss.as<float>(), nullptr));
+    float loss = 0.0f;
+    CUDA_TRY(cudaMemcpy(&loss, s->loss.p, sizeof(float), cudaMemcpyDeviceToHost));
+    if (h_grad) CUDA_TRY(cudaMemcpy(h_grad, s->grad.p, pb, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemset(s->grad.p, 0, pb));
+    if (h_loss) *h_loss = loss / ((float)n * (float)sr::kMlpOut);
+    return SR_OK;
+}
+
+sr_status sr_sizer_train(sr_sizer* s, const float* d_x, const float* d_t, uint32_t n, const sr_sizer_train_opts* o,
+                         float* h_loss, void* stream) {
+    if (!s || (n && (!d_x || !d_t))) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    sr_sizer_train_opts d{};
+    d.struct_size = sizeof d;
+    d.batch = 4096;
+    d.epochs = 1;
+    d.shuffle = 1;
+    d.lr = 1e-3f;
+    d.beta1 = 0.9f;
+    d.beta2 = 0.999f;
+    d.eps = 1e-8f;
+    if (o) {
+        if (o->struct_size < sizeof d) return fail(SR_ERR_INVALID_ARG, "opts.struct_size too small");
+        d = *o;
+    }
+    if (n == 0 || d.batch == 0 || d.epochs == 0) return fail(SR_ERR_INVALID_ARG, "empty training run");
+    if (!(d.lr > 0.0f) || !(d.beta1 >= 0.0f && d.beta1 < 1.0f) || !(d.beta2 >= 0.0f && d.beta2 < 1.0f) ||
+        !(d.eps > 0.0f))
+        return fail(SR_ERR_INVALID_ARG, "bad optimiser settings");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaSetDevice(s->device));
+    uint32_t* idx = nullptr;
+    sr::SortPlan sp = sr::sort_plan(n, 32, nullptr);
+    if (d.shuffle) {
+        CUDA_TRY(ensure(s->keys, sizeof(uint32_t) * n));
+        CUDA_TRY(ensure(s->keys_out, sizeof(uint32_t) * n));
+        CUDA_TRY(ensure(s->perm, sizeof(uint32_t) * n));
+        CUDA_TRY(ensure(s->alt_k, sizeof(uint32_t) * n));
+        CUDA_TRY(ensure(s->alt_v, sizeof(uint32_t) * n));
+        CUDA_TRY(ensure(s->sort_scratch, sr::sort_scratch_bytes(sp)));
+        idx = s->perm.as<uint32_t>();
+    }
+    CUDA_TRY(cudaMemsetAsync(s->ctl.p, 0, sizeof(uint32_t) * 4, st));
+    const double b1 = d.beta1, b2 = d.beta2;
+    for (uint32_t ep = 0; ep < d.epochs; ++ep) {
+        CUDA_TRY(cudaMemsetAsync(s->loss.p, 0, sizeof(float), st));
+        if (d.shuffle) {
+            sr::launch_perm_keys(s->keys.as<uint32_t>(), n, d.seed * 0x100000001B3ull + ep, st);
+            sr::launch_sort_u32(sp, s->keys.as<uint32_t>(), nullptr, s->keys_out.as<uint32_t>(), idx,
+                                s->alt_k.as<uint32_t>(), s->alt_v.as<uint32_t>(), s->sort_scratch.p,
+                                s->ctl.as<uint32_t>(), st);
+        }
+        for (uint32_t b0 = 0; b0 < n; b0 += d.batch) {
+            const uint32_t nb = std::min(d.batch, n - b0);
+            CUDA_TRY(sr::launch_mlp_grad(s->wb.p, s->master.as<float>(), s->norm.as<float>(), d_x, d_t,
+                                         idx ? idx + b0 : nullptr, nb, s->grad.as<float>(), s->loss.as<float>(),
+                                         st));
+            ++s->step;
+            const float bc1 = (float)(1.0 - std::pow(b1, (double)s->step));
+            const float bc2 = (float)(1.0 - std::pow(b2, (double)s->step));
+            sr::launch_adam(s->master.as<float>(), s->wb.p, s->grad.as<float>(), s->m.as<float>(), s->v.as<float>(),
+                            d.lr, d.beta1, d.beta2, d.eps, bc1, bc2, st);
+            if (!idx) {   // unshuffled minibatches are consecutive rows
+                d_x += (size_t)nb * sr::kMlpIn;
+                d_t += (size_t)nb * sr::kMlpOut;
+            }
+        }
+        if (!idx) {
+            d_x -= (size_t)n * sr::kMlpIn;
+            d_t -= (size_t)n * sr::kMlpOut;
+        }
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(s->h_loss, s->loss.p, sizeof(float), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(s->h_loss + 1, s->ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    uint32_t status = 0;
+    std::memcpy(&status, s->h_loss + 1, sizeof status);
+    SR_TRY(check_status_word(status));
+    if (h_loss) *h_loss = s->h_loss[0] / ((float)n * (float)sr::kMlpOut);
+    return SR_OK;
+}
+
+sr_status sr_sizer_predict(const sr_sizer* s, const float* d_x, uint32_t n, float* d_y, void* stream) {
+    if (!s || (n && (!d_x || !d_y))) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    CUDA_TRY(cudaSetDevice(s->device));
+    sr::launch_mlp_predict(s->wb.p, s->master.as<float>(), s->norm.as<float>(), d_x, n, d_y, s->sm_count,
+                           static_cast<cudaStream_t>(stream));
+    CUDA_TRY(cudaGetLastError());
+    return SR_OK;
+}
+
+sr_status sr_batch_path_features(sr_batch* b, float* d_feats, void* stream) {
+    if (!b || !d_feats) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    Pipeline& p = b->p;
+    CUDA_TRY(cudaSetDevice(p.device));
+    SR_TRY(batch_path_first(b));
+    SR_TRY(p.prepare_front());
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaMemsetAsync(p.path_visible.p, 0, sizeof(int32_t) * std::max<uint32_t>(p.P, 1), st));
+    sr::launch_transform(p.pos.as<float2>(), p.pos_path.as<uint32_t>(), p.V, p.table(), p.tpos.as<float2>(),
+                         p.path_visible.as<int32_t>(), st);
+    sr::launch_path_features(p.geom(0), p.path_first.as<uint32_t>(), p.P, d_feats, st);
+    CUDA_TRY(cudaGetLastError());
+    return SR_OK;
+}
+
+// An exact frame with per-path draw counters (the exact count pass).
+static sr_status counted_frame(sr_batch* b, cudaStream_t st) {
+    Pipeline& p = b->p;
+    SR_TRY(batch_path_first(b));
+    CUDA_TRY(ensure(p.path_draw, sizeof(uint32_t) * std::max<uint32_t>(p.P, 1)));
+    p.count_paths = true;
+    sr_status s = p.frame(st, -1);
+    p.count_paths = false;
+    SR_TRY(s);
+    return p.finish(st);
+}
+
+sr_status sr_batch_path_labels(sr_batch* b, float* d_labels, void* stream) {
+    if (!b || !d_labels) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    Pipeline& p = b->p;
+    CUDA_TRY(cudaSetDevice(p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SR_TRY(counted_frame(b, st));
+    sr::launch_path_labels(p.path_first.as<uint32_t>(), p.P, p.count.as<int32_t>(), p.path_draw.as<uint32_t>(),
+                           d_labels, st);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return SR_OK;
+}
+
+sr_status sr_batch_plan(sr_batch* b, const sr_sizer* sz, const sr_sizing_margins* mg, sr_sizing_plan* plan,
+                        int64_t* scene_caps, void* stream) {
+    if (!b || !sz || !mg || !plan) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (mg->struct_size < sizeof(sr_sizing_margins)) return fail(SR_ERR_INVALID_ARG, "margins.struct_size too small");
+    const float margins[4] = {mg->path_records, mg->path_draws, mg->frame_records, mg->frame_draws};
+    for (float m : margins)
+        if (!std::isfinite(m)) return fail(SR_ERR_INVALID_ARG, "margins must be finite");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    Pipeline& p = b->p;
+    if (sz->device != p.device) return fail(SR_ERR_INVALID_ARG, "sizer and batch on different devices");
+    CUDA_TRY(cudaSetDevice(p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t p1 = std::max<uint32_t>(p.P, 1);
+    CUDA_TRY(ensure(p.feats, sizeof(float) * sr::kMlpIn * p1));
+    CUDA_TRY(ensure(p.preds, sizeof(float) * sr::kMlpOut * p1));
+    CUDA_TRY(ensure(p.allot, sizeof(uint32_t) * 2 * p1));
+    const size_t tot_words = 4 + 2 * (size_t)p.S;
+    CUDA_TRY(ensure(p.plan_tot, sizeof(unsigned long long) * tot_words));
+    SR_TRY(sr_batch_path_features(b, p.feats.as<float>(), stream));
+    SR_TRY(sr_sizer_predict(sz, p.feats.as<float>(), p.P, p.preds.as<float>(), stream));
+    CUDA_TRY(cudaMemsetAsync(p.plan_tot.p, 0, sizeof(unsigned long long) * tot_words, st));
+    unsigned long long* tot = p.plan_tot.as<unsigned long long>();
+    sr::launch_allot(p.preds.as<float>(), p.P, p.path_scene.as<uint32_t>(), margins, p.allot.as<uint32_t>(),
+                     tot + 4, tot, st);
+    CUDA_TRY(cudaGetLastError());
+    if (p.h_plan_words < tot_words) {
+        if (p.h_plan_ptr) cudaFreeHost(p.h_plan_ptr);
+        p.h_plan_ptr = nullptr;
+        p.h_plan_words = 0;
+        CUDA_TRY(cudaMallocHost(&p.h_plan_ptr, sizeof(unsigned long long) * tot_words));
+        p.h_plan_words = tot_words;
+    }
+    unsigned long long* h = p.h_plan_ptr;
+    CUDA_TRY(cudaMemcpyAsync(h, tot, sizeof(unsigned long long) * tot_words, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    plan->records = (int64_t)h[0];
+    plan->draws = (int64_t)std::min<unsigned long long>(std::max<unsigned long long>(h[1], 1), 2 * std::max(h[0], 1ull));
+    plan->path_records = (int64_t)h[2];
+    plan->path_draws = (int64_t)h[3];
+    plan->device_bytes = p.frame_bytes(plan->records, plan->draws);
+    if (scene_caps)
+        for (size_t i = 0; i < 2 * (size_t)p.S; ++i) scene_caps[i] = (int64_t)h[4 + i];
+    p.planned = true;
+    return SR_OK;
+}
+
+sr_status sr_batch_path_ranges(const sr_batch* b, uint32_t* path_begin) {
+    if (!b || !path_begin) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    const auto& info = b->h.info;
+    for (size_t i = 0; i < info.size(); ++i) path_begin[i] = info[i].path_begin;
+    path_begin[info.size()] = b->h.n_paths();
+    return SR_OK;
+}
+
+sr_status sr_batch_judge(sr_batch* b, sr_sizing_judge* out, void* stream) {
+    if (!b || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    Pipeline& p = b->p;
+    if (!b->committed || !p.planned) return fail(SR_ERR_INVALID_ARG, "sr_batch_judge needs a plan of this batch");
+    CUDA_TRY(cudaSetDevice(p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SR_TRY(counted_frame(b, st));
+    CUDA_TRY(ensure(p.judge_out, sizeof(unsigned long long) * 4));
+    CUDA_TRY(cudaMemsetAsync(p.judge_out.p, 0, sizeof(unsigned long long) * 4, st));
+    sr::launch_judge(p.path_first.as<uint32_t>(), p.P, p.count.as<int32_t>(), p.path_draw.as<uint32_t>(),
+                     p.allot.as<uint32_t>(), p.judge_out.as<unsigned long long>(), st);
+    CUDA_TRY(cudaGetLastError());
+    unsigned long long h[4];
+    CUDA_TRY(cudaMemcpyAsync(h, p.judge_out.p, sizeof h, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    std::memset(out, 0, sizeof *out);
+    out->paths = p.P;
+    out->paths_over_records = (uint32_t)h[0];
+    out->paths_over_draws = (uint32_t)h[1];
+    out->records = (int64_t)h[2];
+    out->draws = (int64_t)h[3];
+    return SR_OK;
+}
+
+sr_status sr_batch_release(sr_batch* b) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (b->inflight) return fail(SR_ERR_INVALID_ARG, "release while a frame is in flight");
+    CUDA_TRY(cudaSetDevice(b->p.device));
+    CUDA_TRY(cudaDeviceSynchronize());
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_cap = -1;
+    b->graph_dcap = -1;
+    b->p.release_post_count();
+    return SR_OK;
+}
+
+sr_status sr_batch_held_bytes(const sr_batch* b, uint64_t* bytes) {
+    if (!b || !bytes) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    *bytes = b->p.held_bytes();
+    return SR_OK;
+}
+
+sr_status sr_batch_frame_bytes(sr_batch* b, int64_t records, int64_t draws, uint64_t* bytes) {
+    if (!b || !bytes || records < 0) return fail(SR_ERR_INVALID_ARG, "bad argument");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    *bytes = b->p.frame_bytes(records, draws);
+    return SR_OK;
+}
+
+void* sr_device_alloc(int device, size_t bytes) {
+    if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 1)) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void sr_device_free(void* p) {
+    if (p) cudaFree(p);
+}
+
+sr_status sr_memcpy(void* dst, const void* src, size_t bytes) {
+    if (!bytes) return SR_OK;
+    if (!dst || !src) return fail(SR_ERR_INVALID_ARG, "NULL pointer");
+    CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
+    return SR_OK;
+}
+
 }  // extern "C"
+
+static sr_status batch_path_first(sr_batch* b) {
+    Pipeline& p = b->p;
+    if (p.path_first_valid) return SR_OK;
+    const std::vector<uint32_t>& cp = b->h.curve_path;
+    std::vector<uint32_t> first((size_t)p.P + 1);
+    uint32_t c = 0;
+    for (uint32_t i = 0; i <= p.P; ++i) {
+        while (c < p.C && cp[c] < i) ++c;
+        first[i] = c;
+    }
+    CUDA_TRY(ensure(p.path_first, sizeof(uint32_t) * first.size()));
+    CUDA_TRY(cudaMemcpy(p.path_first.p, first.data(), sizeof(uint32_t) * first.size(), cudaMemcpyHostToDevice));
+    p.path_first_valid = true;
+    return SR_OK;
+}

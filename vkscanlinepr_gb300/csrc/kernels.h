@@ -141,6 +141,7 @@ struct WindArgs {
     uint32_t* draw_row;             // [capacity] global cell row of each draw record
     uint64_t* totals;               // [2] merged fragments, spans
     uint32_t* n_draw;               // [1] merged fragments + spans
+    uint32_t* path_draw;            // [P] draw records per path (NULL unless labelling)
     // parity dumps (NULL in production)
     int32_t* dbg_wscan;             // [N+1]
     int32_t* dbg_fflag;             // [N]
@@ -173,5 +174,37 @@ void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st);
 // n_dev (optional) holds the record count; n is the capacity.
 void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,
                        cudaStream_t st);
+
+// ---- mlp.cu  (learned sizing: 6 features -> 64 -> 64 -> 2, GELU)
+constexpr int kMlpIn = 6, kMlpHidden = 64, kMlpOut = 2;
+constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
+                           kMlpOut * kMlpHidden + kMlpOut;
+constexpr int kMlpNorm = 2 * kMlpIn + 2 * kMlpOut;
+// feats[P][6] of the paths under the current transforms (tpos must be current).
+void launch_path_features(const GeomArgs& g, const uint32_t* path_first_curve, uint32_t n_paths, float* feats,
+                          cudaStream_t st);
+// labels[P][2] = log(1 + records), log(1 + draw records) per path.
+void launch_path_labels(const uint32_t* path_first_curve, uint32_t n_paths, const int32_t* count,
+                        const uint32_t* path_draw, float* labels, cudaStream_t st);
+// y[n][2] in log(1 + count) units.  wb: BF16 weights; master: FP32 copy (biases).
+void launch_mlp_predict(const void* wb, const float* master, const float* norm, const float* x, uint32_t n, float* y,
+                        int sm_count, cudaStream_t st);
+// Adds the minibatch gradient of the mean squared error into grad and the
+// sum of squared errors into loss_sum.
+cudaError_t launch_mlp_grad(const void* wb, const float* master, const float* norm, const float* x, const float* t,
+                            const uint32_t* idx, uint32_t n, float* grad, float* loss_sum, cudaStream_t st);
+void launch_adam(float* master, void* wb, float* grad, float* m, float* v, float lr, float b1, float b2, float eps,
+                 float bc1, float bc2, cudaStream_t st);
+void launch_to_bf16(const float* master, void* wb, cudaStream_t st);
+void launch_perm_keys(uint32_t* keys, uint32_t n, uint64_t seed, cudaStream_t st);
+// allot[P][2] from predictions with the path margins (margins[0..1]);
+// frame capacities with the frame margins (margins[2..3]) accumulate into
+// scene_tot[S][2] and tot[0..1], the allotments into tot[2..3] (zero them first).
+void launch_allot(const float* y, uint32_t n_paths, const uint32_t* path_scene, const float margins[4],
+                  uint32_t* allot, unsigned long long* scene_tot, unsigned long long* tot, cudaStream_t st);
+// out[4] (zeroed first): paths over their record allotment, over their draw
+// allotment, exact records, exact draw records.
+void launch_judge(const uint32_t* path_first_curve, uint32_t n_paths, const int32_t* count, const uint32_t* path_draw,
+                  const uint32_t* allot, unsigned long long* out, cudaStream_t st);
 
 }  // namespace sr

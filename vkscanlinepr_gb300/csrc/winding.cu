@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         Decoded d1 = unpack_key(a.L, S.keys[jl + 1]);
         int32_t info = (int32_t)a.fill_info[d1.path];
         const uint32_t row_base = scene_of_path(a.st, d1.path).row_base;
+        if (a.path_draw) atomicAdd(&a.path_draw[d1.path], ff[k] + sf[k]);
         int64_t o = (int64_t)(fb + sb);
         if (ff[k]) {
             if (o < a.draw_capacity) {
