@@ -62,6 +62,8 @@ def parse_args():
     ap.add_argument("--train-epochs", type=int, default=30)
     ap.add_argument("--small-batch", type=int, default=32,
                     help="scenes per batch in the learned-vs-exact sizing stream")
+    ap.add_argument("--serve-requests", type=int, default=2048, help="requests of the serving configuration")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate (requests/s)")
     return ap.parse_args()
 
 
@@ -244,12 +246,18 @@ def run_batched(sr, args, sptr, steps):
     if ctx is not None:
         ctx.close()
     plain_sps = nplain / plain_t
-    learned = None
+    n_resident = len(batches)
+    learned = serving = None
     if not args.no_learned:
-        learned = run_learned(sr, args, sptr, batches)
+        sz, margins, learned = run_learned(sr, args, sptr, batches)
+        for b in batches:
+            b.close()
+        batches = []
+        serving = run_serving(sr, args, sz, margins)
+        sz.close()
     for b in batches:
         b.close()
-    return learned, {"scenes": total, "records": int(records), "resident_batches": len(batches),
+    return learned, serving, {"scenes": total, "records": int(records), "resident_batches": n_resident,
             "scenes_per_s": round(batched_sps, 1), "ms_per_batch_of_all": round(1000 * sum(times) / len(times), 2),
             "sizing": "record capacity from the previous exact frame, frame replayed as a CUDA graph",
             "overflows": int(overflows), "plain_scenes_per_s": round(plain_sps, 1),
@@ -376,8 +384,7 @@ def run_learned(sr, args, sptr, batches):
     small_over = sum(b.stats()["overflows"] for b in objs) - o0
     for b in objs:
         b.close()
-    sz.close()
-    return {
+    return sz, margins, {
         "train_paths": int(n_train), "val_paths": int(n_val), "label_s": round(label_s, 2),
         "train_steps": int(steps), "train_s": round(train_s, 3), "train_mse": round(loss, 5),
         "val_mse": round(val_loss, 5), "margins": [round(m, 4) for m in margins],
@@ -399,6 +406,103 @@ def run_learned(sr, args, sptr, batches):
                    "scenes_per_s_learned": round(nsb * sb / t_small_learned, 1),
                    "overflowed": int(small_over)},
     }
+
+
+def _serve(sr, srv, scenes, arrivals, check_every=0):
+    """Submits scenes[i % len] at arrivals[i] (seconds from the start, None:
+    all at once) from a client thread and collects them in order; returns
+    per-request (submit, done) times on the server clock and the images of
+    every check_every-th request."""
+    import queue
+    import threading
+    q = queue.Queue()
+    n = len(arrivals)
+
+    def client():
+        t0 = time.perf_counter()
+        for i in range(n):
+            if arrivals[i] is not None:
+                d = t0 + arrivals[i] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            q.put((i, srv.submit(scenes[i % len(scenes)])))
+    th = threading.Thread(target=client)
+    th.start()
+    times, imgs = [], {}
+    for _ in range(n):
+        i, tk = q.get()
+        fetch = check_every > 0 and i % check_every == 0
+        img, info = srv.wait(tk, fetch=fetch)
+        times.append((info["submit_s"], info["done_s"], info["batch_scenes"]))
+        if fetch:
+            imgs[i] = img
+    th.join()
+    return np.array(times), imgs
+
+
+def _lat_summary(sub, done):
+    lat = 1000.0 * (done - sub)
+    span = done.max() - sub.min()
+    return {"p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
+            "scenes_per_s": round(len(lat) / span, 1)}
+
+
+def run_serving(sr, args, sz, margins):
+    """Configuration 4: requests of batch-workload sizes arriving as a
+    Poisson stream, served by the continuous-batching server (learned
+    sizing, 120 GB budget) against the exact-sizing server and the plain
+    per-request renderer; every image bit-exact."""
+    n = args.serve_requests
+    pool = [sr.synth_scene(2, 2, scene_index=i) for i in range(min(n, 1024))]
+    rng = np.random.default_rng(4)
+    arrivals = list(np.cumsum(rng.exponential(1.0 / args.serve_rate, n)))
+    out = {"requests": n, "rate_per_s": args.serve_rate, "scene_pool": len(pool), "budget_bytes": int(120e9)}
+    for name, sizer, slots in (("learned", sz, 3), ("exact", None, 1)):
+        srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=64, memory_budget=120e9, margins=margins)
+        _serve(sr, srv, pool[:64], [None] * 64)                      # warm the slots' buffers
+        t, imgs = _serve(sr, srv, pool, arrivals, check_every=64 if name == "learned" else 0)
+        res = _lat_summary(t[:, 0], t[:, 1])
+        res["mean_batch"] = round(float(t[:, 2].mean()), 1)
+        ts, _ = _serve(sr, srv, pool, [None] * n)                     # saturation: all at once
+        res["saturated_scenes_per_s"] = _lat_summary(ts[:, 0], ts[:, 1])["scenes_per_s"]
+        st = srv.stats()
+        res.update({"batches": int(st["batches"]), "overflows": int(st["overflows"]),
+                    "refits": int(st["refits"]), "peak_bytes": int(st["peak_bytes"])})
+        srv.close()
+        out[name] = res
+        if name == "learned":
+            checked = imgs
+    # the plain renderer, one request at a time in arrival order
+    ctx = None
+    done = []
+    t_free = 0.0
+    exact = 0
+    for i in range(n):
+        sc = pool[i % len(pool)]
+        if ctx is None or (ctx.width, ctx.height) != (sc.width, sc.height):
+            if ctx is not None:
+                ctx.close()
+            ctx = sr.ScanlineVGRasterizer(mode=sr.MODE_PIXEL)
+            ctx.initialize(None, sc.width, sc.height)
+            ctx.loadVG(sc)
+            ctx.render_device()
+        t1 = time.perf_counter()
+        ctx.loadVG(sc)
+        ctx.render_device()
+        svc = time.perf_counter() - t1
+        start = max(arrivals[i], t_free)
+        t_free = start + svc
+        done.append(t_free)
+        if i in checked:
+            exact += int(np.array_equal(ctx.render(), checked[i]))
+    if ctx is not None:
+        ctx.close()
+    out["plain"] = _lat_summary(np.array(arrivals), np.array(done))
+    out["bit_exact_vs_plain"] = "%d/%d" % (exact, len(checked))
+    out["speedup_vs_plain"] = round(out["learned"]["scenes_per_s"] / out["plain"]["scenes_per_s"], 2)
+    out["saturated_speedup_vs_plain"] = round(out["learned"]["saturated_scenes_per_s"] /
+                                              out["plain"]["scenes_per_s"], 2)
+    return out
 
 
 def oracle_scene(preset, seed, W, H, P):
@@ -524,8 +628,8 @@ def main():
     gpu_img = out_img.copy()
     r.close()
 
-    learned, batched = (run_batched(sr, args, sptr, max(2, min(args.steps, 5))) if args.batch_scenes > 0
-                        else (None, None))
+    learned, serving, batched = (run_batched(sr, args, sptr, max(2, min(args.steps, 5))) if args.batch_scenes > 0
+                                 else (None, None, None))
 
     # ---- roofline of the dominant stage
     peak, peak_kind = measured_peaks()
@@ -564,6 +668,8 @@ def main():
         line["batched"] = batched
     if learned is not None:
         line["learned"] = learned
+    if serving is not None:
+        line["serving"] = serving
 
     if rank == 0 and not args.no_cpu_baseline:
         so = oracle_scene(preset, seed, W, H, P)

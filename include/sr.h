@@ -396,6 +396,76 @@ sr_status sr_batch_release(sr_batch* b);
 /* Device bytes the batch holds now. */
 sr_status sr_batch_held_bytes(const sr_batch* b, uint64_t* bytes);
 
+/* ------------------------------------------------------------------ */
+/* Continuous-batching render server (no reference counterpart).       */
+/* ------------------------------------------------------------------ */
+
+/* Requests (a scene, its canvas and transform) are queued by any thread.
+ * One scheduler thread keeps up to `slots` batches in flight, each on its
+ * own stream: whenever a slot is free it takes the oldest waiting requests
+ * (at most max_batch_scenes), uploads them as one batch, sizes the frame
+ * with the sizing network and enqueues it without waiting, so a batch is
+ * assembled and uploaded while others render.  Admission keeps the device
+ * bytes of the batches in flight plus the finished, not yet collected
+ * images under memory_budget, using the predicted sizes; a frame whose
+ * records exceed the prediction is rerun with exact sizing, so every
+ * image equals the same scene rendered alone.  Without a sizer each batch
+ * is rendered with exact sizing (the scheduler waits for its count) and
+ * admission counts scenes only. */
+typedef struct sr_server sr_server;
+
+typedef struct sr_server_opts {
+    uint32_t struct_size;
+    int32_t  mode;                /* SR_MODE_* */
+    int32_t  device;
+    uint32_t slots;               /* batches in flight (default 2) */
+    uint32_t max_batch_scenes;    /* scenes per batch (default 64) */
+    uint32_t reserved;
+    uint64_t memory_budget;       /* bytes (default 120e9) */
+    sr_sizing_margins margins;    /* used with a sizer */
+} sr_server_opts;
+
+typedef struct sr_request_info {
+    double   submit_s;            /* seconds since the server started */
+    double   admit_s;             /* the request's batch was enqueued */
+    double   done_s;              /* its image is ready */
+    uint64_t predicted_bytes;     /* the request's share of its batch */
+    uint32_t batch_scenes;        /* scenes in its batch */
+    uint32_t refit;               /* its batch overflowed and was rerun exactly */
+    int32_t  status;              /* sr_status of its render */
+    uint32_t reserved;
+} sr_request_info;
+
+typedef struct sr_server_stats {
+    uint64_t submitted, completed, batches;
+    uint64_t overflows, refits;
+    uint64_t budget_waits;        /* admissions deferred by the memory budget */
+    uint64_t peak_bytes;          /* largest admitted total */
+    uint64_t rejected;            /* requests larger than the whole budget */
+} sr_server_stats;
+
+/* sizer may be NULL (exact sizing); it must outlive the server. */
+sr_status sr_server_create(const sr_server_opts* opts, const sr_sizer* sizer, sr_server** out);
+/* Copies the scene and queues it; thread-safe.  mvp may be NULL (identity). */
+sr_status sr_server_submit(sr_server* s, uint32_t width, uint32_t height, const sr_scene_view* scene,
+                           const float* mvp, uint64_t* ticket);
+/* Waits up to timeout_ms (< 0: forever) for the request, copies its image
+ * (width x height RGBA8) to rgba_out (host or device; NULL drops it) and
+ * forgets the request.  SR_ERR_TIMEOUT leaves it pending.  Thread-safe. */
+sr_status sr_server_wait(sr_server* s, uint64_t ticket, void* rgba_out, int out_is_device, sr_request_info* info,
+                         int64_t timeout_ms);
+sr_status sr_server_get_stats(sr_server* s, sr_server_stats* out);
+/* Stops the scheduler after the queued requests finish. */
+void sr_server_destroy(sr_server* s);
+
+/* Admission rule of the server (host logic, exposed for tests): the
+ * number of requests, taken in order from req_bytes[0..n), whose bytes fit
+ * with held_bytes under budget, at most max_take.  When nothing is held the
+ * first request is taken if it fits the budget alone.  *rejected is set
+ * when the first request cannot fit even an empty budget. */
+uint32_t sr_admission_take(const uint64_t* req_bytes, uint32_t n, uint64_t held_bytes, uint64_t budget,
+                           uint32_t max_take, int* rejected);
+
 /* Plain device memory for hosts without a CUDA binding of their own. */
 void* sr_device_alloc(int device, size_t bytes);
 void sr_device_free(void* p);

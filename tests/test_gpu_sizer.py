@@ -12,6 +12,8 @@ import pytest
 
 from oracle import mlp_ref as M
 
+import sizing_util
+
 pytestmark = pytest.mark.gpu
 
 
@@ -118,22 +120,7 @@ def test_state_round_trip(gpu, oracle_lib, tmp_path):
 
 
 def _train_on_batches(gpu, seeds, epochs=40):
-    xs, ts, keep = [], [], []
-    for sd in seeds:
-        b = gpu.SceneBatch(mode=1)
-        b.add_synth(2, sd, 24)
-        b.commit()
-        xs.append(b.features())
-        ts.append(b.labels())
-        keep.append(b)
-    x = gpu.concat_device(xs)
-    t = gpu.concat_device(ts)
-    sz = gpu.Sizer(seed=11)
-    sz.set_norm(gpu.sizer_norm(x.numpy(), t.numpy()))
-    losses = [sz.train(x, t, epochs=epochs // 4, batch=4096, seed=e) for e in range(4)]
-    for b in keep:
-        b.close()
-    return sz, x, t, losses
+    return sizing_util.train_sizer(gpu, seeds, epochs=epochs)
 
 
 def _overalloc(pred, exact, frac=0.01):

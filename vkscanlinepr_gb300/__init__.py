@@ -92,9 +92,27 @@ class SizingMargins(ctypes.Structure):
                 ("frame_records", ctypes.c_float), ("frame_draws", ctypes.c_float)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("mode", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("slots", ctypes.c_uint32), ("max_batch_scenes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("memory_budget", ctypes.c_uint64), ("margins", SizingMargins)]
+
+
 class SizingPlan(ctypes.Structure):
     _fields_ = [("records", ctypes.c_int64), ("draws", ctypes.c_int64), ("path_records", ctypes.c_int64),
                 ("path_draws", ctypes.c_int64), ("device_bytes", ctypes.c_uint64)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("predicted_bytes", ctypes.c_uint64), ("batch_scenes", ctypes.c_uint32), ("refit", ctypes.c_uint32),
+                ("status", ctypes.c_int32), ("reserved", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("overflows", ctypes.c_uint64), ("refits", ctypes.c_uint64), ("budget_waits", ctypes.c_uint64),
+                ("peak_bytes", ctypes.c_uint64), ("rejected", ctypes.c_uint64)]
 
 
 class SizingJudge(ctypes.Structure):
@@ -129,7 +147,9 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_sizer_set_state", "sr_sizer_loss_grad", "sr_sizer_train", "sr_sizer_predict",
            "sr_batch_path_features", "sr_batch_path_labels", "sr_batch_plan", "sr_batch_judge",
            "sr_batch_frame_bytes", "sr_device_alloc", "sr_device_free", "sr_memcpy", "sr_batch_enqueue",
-           "sr_batch_query", "sr_batch_finish", "sr_batch_release", "sr_batch_held_bytes", "sr_batch_path_ranges"]
+           "sr_batch_query", "sr_batch_finish", "sr_batch_release", "sr_batch_held_bytes", "sr_batch_path_ranges",
+           "sr_server_create", "sr_server_submit", "sr_server_wait", "sr_server_get_stats", "sr_server_destroy",
+           "sr_admission_take"]
 
 _lib = None
 
@@ -203,6 +223,16 @@ def lib():
     L.sr_batch_path_labels.argtypes = [vp, vp, vp]
     L.sr_batch_plan.argtypes = [vp, vp, ctypes.POINTER(SizingMargins), ctypes.POINTER(SizingPlan), vp, vp]
     L.sr_batch_path_ranges.argtypes = [vp, vp]
+    L.sr_server_create.argtypes = [ctypes.POINTER(ServerOpts), vp, ctypes.POINTER(vp)]
+    L.sr_server_submit.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(SceneView), vp,
+                                   ctypes.POINTER(ctypes.c_uint64)]
+    L.sr_server_wait.argtypes = [vp, ctypes.c_uint64, vp, ctypes.c_int, ctypes.POINTER(RequestInfo), ctypes.c_int64]
+    L.sr_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.sr_server_destroy.argtypes = [vp]
+    L.sr_server_destroy.restype = None
+    L.sr_admission_take.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                    ctypes.POINTER(ctypes.c_int)]
+    L.sr_admission_take.restype = ctypes.c_uint32
     L.sr_batch_judge.argtypes = [vp, ctypes.POINTER(SizingJudge), vp]
     L.sr_batch_frame_bytes.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
     L.sr_batch_release.argtypes = [vp]
@@ -802,3 +832,70 @@ def calibrate_margins(pred, labels, path_begin, path_quantile=0.995, frame_slack
             need = max(need, hi)
         out.append(float((need if np.isfinite(need) else 0.0) + frame_slack))
     return tuple(out)
+
+
+def admission_take(req_bytes, held_bytes, budget, max_take=None):
+    """The server's admission rule: (requests taken in order, rejected)."""
+    a = np.ascontiguousarray(req_bytes, np.uint64)
+    rej = ctypes.c_int()
+    k = lib().sr_admission_take(a.ctypes.data if a.size else None, int(a.size), int(held_bytes), int(budget),
+                                int(a.size if max_take is None else max_take), ctypes.byref(rej))
+    return int(k), bool(rej.value)
+
+
+class RenderServer:
+    """Continuous-batching render server (sr_server_*): submit() from any
+    thread, wait() for each ticket.  With a Sizer the batches are sized by
+    the network and kept in flight on several streams; without one every
+    batch waits for its exact count."""
+
+    def __init__(self, mode=MODE_PIXEL, device=0, slots=2, max_batch_scenes=64, memory_budget=120e9, sizer=None,
+                 margins=(0.5, 1.2, 0.05, 0.25)):
+        o = ServerOpts(ctypes.sizeof(ServerOpts), mode, device, slots, max_batch_scenes, 0, int(memory_budget),
+                       SizingMargins(ctypes.sizeof(SizingMargins), *[float(v) for v in margins]))
+        h = ctypes.c_void_p()
+        _check(lib().sr_server_create(ctypes.byref(o), sizer._h if sizer is not None else None, ctypes.byref(h)))
+        self._h = h
+        self._sizer = sizer
+        self._sizes = {}
+
+    def submit(self, container, width=None, height=None, mvp=None):
+        w = container.width if width is None else width
+        h = container.height if height is None else height
+        v = container.view()
+        m = None if mvp is None else np.ascontiguousarray(mvp, np.float32).reshape(16)
+        t = ctypes.c_uint64()
+        _check(lib().sr_server_submit(self._h, int(w), int(h), ctypes.byref(v),
+                                      m.ctypes.data if m is not None else None, ctypes.byref(t)))
+        self._sizes[t.value] = (int(w), int(h))
+        return t.value
+
+    def wait(self, ticket, fetch=True, timeout_ms=-1):
+        """(image (h, w, 4) uint8 or None, info dict)."""
+        w, h = self._sizes.pop(ticket)
+        out = np.empty((h, w, 4), np.uint8) if fetch else None
+        info = RequestInfo()
+        rc = lib().sr_server_wait(self._h, int(ticket), out.ctypes.data if fetch else None, 0, ctypes.byref(info),
+                                  int(timeout_ms))
+        d = {k: getattr(info, k) for k, _ in RequestInfo._fields_ if k != "reserved"}
+        if rc != 0:
+            if rc == 4:
+                self._sizes[ticket] = (w, h)
+            raise SRError(rc, lib().sr_last_error().decode(errors="replace"))
+        return out, d
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().sr_server_get_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().sr_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
