@@ -127,3 +127,25 @@ def test_config1_full_size(gpu, oracle_lib):
     compare_all(of, r, img, 1, stages=["curve_offset", "sorted_key", "sorted_index", "winding_scan",
                                         "draw_list", "image"])
     r.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_production_frame_equals_kept_stages_frame(gpu, oracle_lib, mode):
+    """Without SR_FLAG_KEEP_STAGES the winding bits ride above the sort key
+    (keys-only sort, no record-index gather); with it the sort carries record
+    indices.  Both must give the same draw list and image."""
+    import oracle
+    s = oracle.synth(1, 3, width=1536, height=1024, n_paths=2000)
+    d = dict(width=s.width, height=s.height, **{f: getattr(s, f) for f in oracle.Scene.FIELDS})
+    out = []
+    for keep in (True, False):
+        r = gpu.ScanlineVGRasterizer(mode=mode, keep_stages=keep)
+        r.initialize(None, d["width"], d["height"])
+        r.loadVG(scenes.to_container(d))
+        img = r.render().copy()
+        out.append((img, r.dump("draw_list").copy()))
+        r.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    want = oracle_lib.Frame(s, mode=mode).get("image")
+    assert np.array_equal(out[1][0], want)

@@ -462,9 +462,13 @@ struct Pipeline {
         fn(keys, sizeof(uint64_t) * n1);
         fn(keys_alt, sizeof(uint64_t) * n1);
         fn(skeys, sizeof(uint64_t) * n1);
-        fn(wnp, n1);
-        fn(svals, sizeof(uint32_t) * n1);
-        fn(vals_alt, sizeof(uint32_t) * n1);
+        // record indices and a separate winding-bit array only when the
+        // stages are kept (sorted-index dump); otherwise the winding bits
+        // ride in the keys
+        const bool idx = (flags & SR_FLAG_KEEP_STAGES) != 0;
+        fn(wnp, idx ? n1 : 0);
+        fn(svals, idx ? sizeof(uint32_t) * n1 : 0);
+        fn(vals_alt, idx ? sizeof(uint32_t) * n1 : 0);
         const sr::KeyLayout L = layout();
         fn(sort_scratch, sr::sort_scratch_bytes(sr::sort_plan(cap, L.pbits + L.rbits + L.xbits, nullptr)));
         fn(wind_status, sizeof(uint64_t) * sr::winding_status_words(cap));
@@ -484,6 +488,7 @@ struct Pipeline {
     uint64_t frame_bytes(int64_t cap, int64_t dcap) {
         uint64_t total = 0;
         auto add = [&](size_t b) {
+            if (!b) return;
             size_t want = std::max<size_t>(b + b / 4, 256);
             total += (want + 255) & ~(size_t)255;
         };
@@ -532,7 +537,7 @@ struct Pipeline {
     sr_status reserve(int64_t cap, int64_t dcap) {
         cudaError_t err = cudaSuccess;
         post_count_buffers(cap, dcap, [&](DevBuf& b, size_t bytes) {
-            if (err == cudaSuccess) err = ensure(b, bytes);
+            if (err == cudaSuccess && bytes) err = ensure(b, bytes);
         });
         CUDA_TRY(err);
         const size_t n1 = (size_t)std::max<int64_t>(cap, 1);
@@ -604,21 +609,23 @@ struct Pipeline {
         launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, st);
         mark(ST_MERGE, true);
         mark(ST_FRAGMENT, false);
-        launch_fragment(g, rec.as<int2>(), cap, n_dev, keys.as<uint64_t>(), wnp.as<uint8_t>(), dbg, st);
+        launch_fragment(g, rec.as<int2>(), cap, n_dev, keys.as<uint64_t>(), keep ? wnp.as<uint8_t>() : nullptr, dbg,
+                        st);
         mark(ST_FRAGMENT, true);
         const KeyLayout L = g.L;
         SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev);
         mark(ST_SORT, false);
-        launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(), svals.as<uint32_t>(),
-                        keys_alt.as<uint64_t>(), vals_alt.as<uint32_t>(), sort_scratch.p, status, st);
+        launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(), keep ? svals.as<uint32_t>() : nullptr,
+                        keys_alt.as<uint64_t>(), keep ? vals_alt.as<uint32_t>() : nullptr, sort_scratch.p, status,
+                        st);
         mark(ST_SORT, true);
         CUDA_TRY(cudaMemsetAsync(wind_status.p, 0, sizeof(uint64_t) * winding_status_words(cap), st));
         WindArgs wa;
         wa.n = cap;
         wa.n_dev = n_dev;
         wa.skeys = skeys.as<uint64_t>();
-        wa.svals = svals.as<uint32_t>();
-        wa.wnp = wnp.as<uint8_t>();
+        wa.svals = keep ? svals.as<uint32_t>() : nullptr;
+        wa.wnp = keep ? wnp.as<uint8_t>() : nullptr;
         wa.fill_rule = fill_rule.as<uint32_t>();
         wa.fill_info = fill_info.as<uint32_t>();
         wa.n_paths = P;
@@ -954,7 +961,7 @@ sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
         case SR_STAGE_FRAG_WINDING: src = p.d_fwn.p; need = 4 * N; break;
         case SR_STAGE_FRAG_LEFT: src = p.d_fleft.p; need = 4 * N; break;
         case SR_STAGE_SORTED_KEY: src = p.d_skey.p; need = 4 * N; break;
-        case SR_STAGE_SORTED_INDEX: src = p.svals.p; need = 4 * N; need_stages = false; break;
+        case SR_STAGE_SORTED_INDEX: src = p.svals.p; need = 4 * N; break;
         case SR_STAGE_WINDING_SCAN: src = p.d_wscan.p; need = 4 * (N + 1); break;
         case SR_STAGE_FRAG_FLAG: src = p.d_fflag.p; need = 4 * N; break;
         case SR_STAGE_SPAN_FLAG: src = p.d_sflag.p; need = 4 * N; break;

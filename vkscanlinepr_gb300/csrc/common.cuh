@@ -86,6 +86,17 @@ SR_DEV void st_release_u32(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Relaxed (no ordering) but coherent at GPU scope: for flag+value words
+// whose readers use nothing else the writer published.
+SR_DEV uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+SR_DEV void st_relaxed_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 SR_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
 SR_DEV uint32_t lanemask_lt() {
     uint32_t m;
@@ -126,8 +137,15 @@ struct Decoded {
     int32_t yx;     // the reference's packed key
 };
 
+// Bits of the sort key proper.  Above them a key may carry a payload (the
+// record's packed winding bits) that the sort moves but does not order by.
+__host__ __device__ __forceinline__ uint32_t key_bits(const KeyLayout& L) { return L.pbits + L.rbits + L.xbits; }
+SR_DEV uint64_t key_part(const KeyLayout& L, uint64_t k) { return k & ((1ull << key_bits(L)) - 1ull); }
+SR_DEV uint32_t payload_part(const KeyLayout& L, uint64_t k) { return (uint32_t)(k >> key_bits(L)) & 0xFu; }
+
 SR_DEV Decoded unpack_key(const KeyLayout& L, uint64_t k) {
     Decoded d;
+    k = key_part(L, k);
     uint32_t xo = (uint32_t)(k & ((1ull << L.xbits) - 1));
     uint32_t rank = (uint32_t)((k >> L.xbits) & ((1ull << L.rbits) - 1));
     d.path = (uint32_t)(k >> (L.xbits + L.rbits));

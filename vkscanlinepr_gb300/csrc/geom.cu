@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
         // only in a frame whose records overflowed their capacity (the
         // frame is reported and discarded): never index with it
         keys[i] = ~0ull;
-        wnp[i] = 0;
+        if (wnp) wnp[i] = 0;
         return;
     }
     uint32_t path = g.curve_path[c];
@@ -710,8 +710,14 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
             if (xc < __fadd_rn((float)pos_x, 0.5f)) left = wn;
         }
     }
-    keys[i] = pack_key(g.L, path, valid, pos_y, pos_x);
-    wnp[i] = (uint8_t)((wn & 3) | ((left & 3) << 2));
+    const uint32_t wbits = (uint32_t)((wn & 3) | ((left & 3) << 2));
+    const uint64_t key = pack_key(g.L, path, valid, pos_y, pos_x);
+    if (wnp) {
+        keys[i] = key;
+        wnp[i] = (uint8_t)wbits;
+    } else {
+        keys[i] = key | ((uint64_t)wbits << key_bits(g.L));   // winding bits ride above the key
+    }
     if (dbg.fkey) {
         dbg.fkey[i] = yx;
         dbg.fwn[i] = wn;

@@ -88,7 +88,9 @@ void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, i
                    cudaStream_t st);
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
                   uint32_t* status, cudaStream_t st);
-// One fragment per record: sort key + packed winding bits.
+// One fragment per record: sort key + packed winding bits (4 bits: change,
+// centre part).  With wnp NULL the bits are stored above the key bits of
+// each key instead of in wnp[].
 // n_cap launches the grid; the record count is read from n_dev (offs[C]).
 void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n_cap, const uint32_t* n_dev, uint64_t* keys,
                      uint8_t* wnp, const DebugOut& dbg, cudaStream_t st);
@@ -112,9 +114,10 @@ struct SortPlan {
 SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev = nullptr);
 // Device scratch needed by a plan (bytes).
 size_t sort_scratch_bytes(const SortPlan& p);
-// Sorts (keys, values) stably by the low key_bits of the keys.  If
-// vals_in is NULL the values are the identity 0..n-1.  Results end in
-// (keys_out, vals_out); keys_alt/vals_alt are ping-pong buffers of n items.
+// Sorts (keys, values) stably by the low key_bits of the keys; higher bits
+// travel with their key.  If vals_in is NULL the values are the identity
+// 0..n-1; if vals_out is NULL there are no values (keys only).  Results end
+// in (keys_out, vals_out); keys_alt/vals_alt are ping-pong buffers of n items.
 void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                      uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch,
                      uint32_t* status, cudaStream_t st);
@@ -127,8 +130,8 @@ struct WindArgs {
     int64_t n;                      // N records: the capacity when n_dev is set
     const uint32_t* n_dev;          // device-side record count (offs[C])
     const uint64_t* skeys;          // sorted keys
-    const uint32_t* svals;          // sorted record indices
-    const uint8_t* wnp;             // packed winding bits by record index
+    const uint32_t* svals;          // sorted record indices (NULL: winding bits ride in the keys)
+    const uint8_t* wnp;             // packed winding bits by record index (NULL likewise)
     const uint32_t* fill_rule;      // [P]
     const uint32_t* fill_info;      // [P]
     uint32_t n_paths;

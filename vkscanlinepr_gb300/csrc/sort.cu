@@ -8,8 +8,9 @@
 //
 // Per pass, each CTA (dynamic tile id) loads a 4096-key tile, ranks keys by
 // digit with warp __match_any_sync / popc, publishes its per-digit counts,
-// and looks back over earlier tiles' per-digit counts (one thread per digit,
-// bounded spin) to find where its run of each digit starts.  Keys are first
+// and looks back over earlier tiles' per-digit counts to find where its run
+// of each digit starts; the thread of a digit reads the words of 8
+// preceding tiles per step, all loads in flight together.  Keys are first
 // scattered into shared memory in digit order, then written out in runs, so
 // global stores stay mostly contiguous.  An upfront kernel histograms every
 // pass's digits in one read of the keys.
@@ -23,21 +24,42 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
+constexpr int kItems = 12;
 constexpr int kTile = kThreads * kItems;
 constexpr uint32_t kFlagA = 1u << 30;
 constexpr uint32_t kFlagP = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
 constexpr int kMaxPasses = 8;
 constexpr int kHistBlocks = 608;   // 152 SMs x 4
+constexpr int kLookWindow = 8;     // look-back words read per step
+// Lanes holding the same digit: one __match_any_sync, or one ballot per
+// digit bit (9 bits: digit 256 marks an empty slot).
+constexpr bool kMatchAny = false;
 
-template <typename K> SR_DEV uint32_t digit_of(K k, uint32_t shift) {
-    return (uint32_t)(k >> shift) & (kRadix - 1);
+SR_DEV uint32_t same_digit_lanes(uint32_t d) {
+    if (kMatchAny) return __match_any_sync(0xFFFFFFFFu, d);
+    uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+    for (int b = 0; b <= kRadixBits; ++b) {
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+        peers &= ((d >> b) & 1u) ? m : ~m;
+    }
+    return peers;
+}
+
+// Digit of a pass; bits at or above key_bits do not take part.
+template <typename K> SR_DEV uint32_t digit_of(K k, uint32_t shift, uint32_t mask) {
+    return (uint32_t)(k >> shift) & mask;
+}
+
+__host__ __device__ inline uint32_t digit_mask(uint32_t key_bits, uint32_t shift) {
+    const uint32_t left = key_bits > shift ? key_bits - shift : 0u;
+    return left >= (uint32_t)kRadixBits ? (uint32_t)(kRadix - 1) : ((1u << left) - 1u);
 }
 
 struct Scratch {
     uint32_t* hist;       // [passes][256] digit counts, then exclusive offsets
-    uint32_t* lookback;   // [passes][tiles][256]
+    uint32_t* lookback;   // [passes][tiles + 1][256]
     uint32_t* counters;   // [passes] tile counters
 };
 
@@ -66,7 +88,7 @@ SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev) {
 
 size_t sort_scratch_bytes(const SortPlan& p) {
     return sizeof(uint32_t) * (kMaxPasses * kRadix + 64) +
-           sizeof(uint32_t) * (size_t)p.passes * (size_t)(p.tiles + 1) * kRadix;
+           sizeof(uint32_t) * (size_t)p.passes * ((size_t)p.tiles + 1) * kRadix;
 }
 
 // Histogram of every pass's digits (grid-stride; warp-aggregated shared
@@ -74,7 +96,7 @@ size_t sort_scratch_bytes(const SortPlan& p) {
 template <typename K>
 __global__ void __launch_bounds__(kThreads) k_hist(const K* __restrict__ keys, int64_t n_max,
                                                    const uint32_t* __restrict__ n_dev, uint32_t passes,
-                                                   uint32_t* __restrict__ hist) {
+                                                   uint32_t key_bits, uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[kMaxPasses][kRadix];
     const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_max) : n_max;
     for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kThreads) (&sh[0][0])[i] = 0;
@@ -87,7 +109,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(const K* __restrict__ keys, i
         K k = ok ? keys[i] : (K)0;
         uint32_t am = __ballot_sync(0xFFFFFFFFu, ok);
         for (uint32_t p = 0; p < passes; ++p) {
-            uint32_t d = digit_of(k, p * kRadixBits);
+            uint32_t d = digit_of(k, p * kRadixBits, digit_mask(key_bits, p * kRadixBits));
             if (ok) {
                 uint32_t peers = __match_any_sync(am, d);
                 if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&sh[p][d], (uint32_t)__popc(peers));
@@ -129,27 +151,27 @@ __global__ void __launch_bounds__(kRadix) k_hist_scan(uint32_t* hist) {
     h[threadIdx.x] = sw[warp] + x - v;
 }
 
-template <typename K> struct OnesweepSmem {
+template <typename K, bool kVals> struct OnesweepSmem {
     uint32_t warp_hist[kWarps][kRadix];
     uint32_t digit_start[kRadix];   // tile-local exclusive start of each digit
     uint32_t digit_global[kRadix];  // global base minus digit_start
     uint32_t scan_tmp[kWarps];
     uint32_t tile;
     K keys[kTile];
-    uint32_t vals[kTile];
+    uint32_t vals[kVals ? kTile : 1];
 };
 
-template <typename K>
-__global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ keys_in,
+template <typename K, bool kVals>
+__global__ void __launch_bounds__(kThreads, kVals ? 3 : 4) k_onesweep(const K* __restrict__ keys_in,
                                                        const uint32_t* __restrict__ vals_in,
                                                        K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                        int64_t n_max, const uint32_t* __restrict__ n_dev,
-                                                       uint32_t shift,
+                                                       uint32_t shift, uint32_t dmask,
                                                        const uint32_t* __restrict__ global_off,
                                                        uint32_t* __restrict__ lookback, uint32_t* counter,
                                                        uint32_t* status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    OnesweepSmem<K>& S = *reinterpret_cast<OnesweepSmem<K>*>(smem_raw);
+    OnesweepSmem<K, kVals>& S = *reinterpret_cast<OnesweepSmem<K, kVals>*>(smem_raw);
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
     if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
@@ -162,21 +184,21 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ key
 
     // ---- load (warp-striped, coalesced) and rank within the warp
     K k[kItems];
-    uint32_t v[kItems];
+    uint32_t v[kVals ? kItems : 1];
     uint32_t rank[kItems];
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         int64_t idx = wbase + it * 32 + lane;
         bool ok = idx < n;
         k[it] = ok ? keys_in[idx] : (K)0;
-        v[it] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
+        if (kVals) v[it] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
     }
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
         int64_t idx = wbase + it * 32 + lane;
         bool ok = idx < n;
-        uint32_t d = ok ? digit_of(k[it], shift) : (uint32_t)kRadix;   // kRadix = out of range
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t d = ok ? digit_of(k[it], shift, dmask) : (uint32_t)kRadix;   // kRadix = out of range
+        uint32_t peers = same_digit_lanes(d);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t before = 0;
         if (ok && lane == leader) {
@@ -198,8 +220,8 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ key
         S.warp_hist[w][d] = cnt;
         cnt += t;
     }
-    uint32_t* lb = lookback + (size_t)tile * kRadix;
-    st_release_u32(&lb[d], (tile == 0 ? kFlagP : kFlagA) | cnt);
+    uint32_t* lb_mine = lookback + (size_t)tile * kRadix + d;
+    st_relaxed_u32(lb_mine, (tile == 0 ? kFlagP : kFlagA) | cnt);
 
     // tile-local digit starts: block exclusive scan over the 256 counts
     uint32_t x = cnt;
@@ -224,27 +246,41 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ key
     const uint32_t dstart = S.scan_tmp[warp] + x - cnt;
     S.digit_start[d] = dstart;
 
-    // ---- look-back for this digit over earlier tiles (bounded)
+    // ---- look-back for this digit: 8 preceding tiles' words per step, all
+    // loads in flight together; stop at the first inclusive prefix, wait
+    // (bounded) at the first tile that has published nothing yet
     uint32_t excl = 0;
     if (tile > 0) {
-        int64_t j = (int64_t)tile - 1;
+        const uint32_t* base = lookback + d;
+        int64_t look = (int64_t)tile - 1;
         uint32_t spins = 0;
-        while (j >= 0) {
-            uint32_t s = ld_acquire_u32(&lookback[(size_t)j * kRadix + d]);
-            uint32_t f = s & ~kCountMask;
-            if (f == 0) {
+        for (;;) {
+            uint32_t w[kLookWindow];
+#pragma unroll
+            for (int q = 0; q < kLookWindow; ++q)
+                w[q] = look - q >= 0 ? ld_relaxed_u32(base + (size_t)(look - q) * kRadix) : kFlagP;
+            int used = 0;
+            bool done = false;
+#pragma unroll
+            for (int q = 0; q < kLookWindow; ++q) {
+                if (done || used < q) continue;   // stopped at an earlier word
+                const uint32_t f = w[q] & ~kCountMask;
+                if (f == 0) continue;             // not published yet: used stays q
+                excl += w[q] & kCountMask;
+                used = q + 1;
+                done = f == kFlagP;
+            }
+            if (done) break;
+            look -= used;
+            if (used == 0) {
                 if (++spins > kSpinLimit) {
                     set_error(status, ERR_LOOKBACK_TIMEOUT);
                     break;
                 }
                 __nanosleep(32);
-                continue;
             }
-            excl += s & kCountMask;
-            if (f == kFlagP) break;
-            --j;
         }
-        st_release_u32(&lb[d], kFlagP | (excl + cnt));
+        st_relaxed_u32(lb_mine, kFlagP | (excl + cnt));
     }
     S.digit_global[d] = global_off[d] + excl - dstart;
     __syncthreads();
@@ -254,10 +290,10 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ key
     for (int it = 0; it < kItems; ++it) {
         int64_t idx = wbase + it * 32 + lane;
         if (idx < n) {
-            uint32_t dg = digit_of(k[it], shift);
+            uint32_t dg = digit_of(k[it], shift, dmask);
             uint32_t pos = S.digit_start[dg] + S.warp_hist[warp][dg] + rank[it];
             S.keys[pos] = k[it];
-            S.vals[pos] = v[it];
+            if (kVals) S.vals[pos] = v[it];
         }
     }
     __syncthreads();
@@ -267,35 +303,35 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(const K* __restrict__ key
     if (valid > kTile) valid = kTile;
     for (int j = threadIdx.x; j < valid; j += kThreads) {
         K kk = S.keys[j];
-        uint32_t dg = digit_of(kk, shift);
+        uint32_t dg = digit_of(kk, shift, dmask);
         uint32_t o = S.digit_global[dg] + (uint32_t)j;
         if ((int64_t)o < n) {
             keys_out[o] = kk;
-            vals_out[o] = S.vals[j];
+            if (kVals) vals_out[o] = S.vals[j];
         } else {
             set_error(status, ERR_BAD_INDEX);
         }
     }
 }
 
-template <typename K>
+template <typename K, bool kVals>
 static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_in, K* keys_out, uint32_t* vals_out,
                       K* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status, cudaStream_t st) {
     if (p.n <= 0) return;
     Scratch s = carve(p, scratch);
-    size_t lb_words = (size_t)p.passes * (size_t)(p.tiles + 1) * kRadix;
+    size_t lb_words = (size_t)p.passes * ((size_t)p.tiles + 1) * kRadix;
     cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + 64), st);
     cudaMemsetAsync(s.lookback, 0, sizeof(uint32_t) * lb_words, st);
     int hb = (int)((p.n + kThreads - 1) / kThreads);
     if (hb > kHistBlocks) hb = kHistBlocks;
     count_launches(1);
-    k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.n_dev, p.passes, s.hist);
+    k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.n_dev, p.passes, p.key_bits, s.hist);
     count_launches(1);
     k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
-    const size_t smem = sizeof(OnesweepSmem<K>);
+    const size_t smem = sizeof(OnesweepSmem<K, kVals>);
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_onesweep<K, kVals>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr_set = true;
     }
     const K* ksrc = keys_in;
@@ -305,10 +341,12 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
         K* kdst = to_out ? keys_out : keys_alt;
         uint32_t* vdst = to_out ? vals_out : vals_alt;
         count_launches(1);
-        k_onesweep<K><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, p.n_dev, pass * kRadixBits,
-                                                      s.hist + pass * kRadix,
-                                                      s.lookback + (size_t)pass * (p.tiles + 1) * kRadix,
-                                                      s.counters + pass, status);
+        k_onesweep<K, kVals><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, p.n_dev,
+                                                             pass * kRadixBits,
+                                                             digit_mask(p.key_bits, pass * kRadixBits),
+                                                             s.hist + pass * kRadix,
+                                                             s.lookback + (size_t)pass * (p.tiles + 1) * kRadix,
+                                                             s.counters + pass, status);
         ksrc = kdst;
         vsrc = vdst;
     }
@@ -317,13 +355,17 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
 void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                      uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
                      cudaStream_t st) {
-    sort_impl<uint64_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
+    if (vals_out) sort_impl<uint64_t, true>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch,
+                                            status, st);
+    else sort_impl<uint64_t, false>(p, keys_in, nullptr, keys_out, nullptr, keys_alt, nullptr, scratch, status, st);
 }
 
 void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, uint32_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
                      cudaStream_t st) {
-    sort_impl<uint32_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
+    if (vals_out) sort_impl<uint32_t, true>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch,
+                                            status, st);
+    else sort_impl<uint32_t, false>(p, keys_in, nullptr, keys_out, nullptr, keys_alt, nullptr, scratch, status, st);
 }
 
 }  // namespace sr

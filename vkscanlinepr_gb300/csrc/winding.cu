@@ -136,9 +136,14 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         uint8_t w = 0;
         if (i < n) {
             k = a.skeys[i];
-            uint32_t rec = a.svals[i];
-            if (rec < (uint64_t)n) w = a.wnp[rec];
-            else set_error(status, ERR_BAD_INDEX);
+            if (a.svals) {
+                uint32_t rec = a.svals[i];
+                if (rec < (uint64_t)n) w = a.wnp[rec];
+                else set_error(status, ERR_BAD_INDEX);
+            } else {
+                w = (uint8_t)payload_part(a.L, k);
+                k = key_part(a.L, k);
+            }
             if ((k >> (a.L.xbits + a.L.rbits)) >= a.n_paths) {
                 set_error(status, ERR_BAD_INDEX);
                 k = 0;
@@ -148,7 +153,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         S.wb[j] = w;
     }
     if (threadIdx.x == 0) {
-        uint64_t k0 = tbase > 0 ? a.skeys[tbase - 1] : 0ull;
+        uint64_t k0 = tbase > 0 ? key_part(a.L, a.skeys[tbase - 1]) : 0ull;
         if ((k0 >> (a.L.xbits + a.L.rbits)) >= a.n_paths) k0 = 0;
         S.keys[0] = k0;
     }
@@ -285,10 +290,14 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
                 if (jt < kTile) {
                     kj = S.keys[jt + 1];
                     lj = sx2((uint32_t)S.wb[jt] >> 2);
-                } else {
+                } else if (a.svals) {
                     kj = a.skeys[j];
                     uint32_t rec = a.svals[j];
                     lj = rec < (uint64_t)n ? sx2((uint32_t)a.wnp[rec] >> 2) : 0;
+                } else {
+                    const uint64_t kr = a.skeys[j];
+                    kj = key_part(a.L, kr);
+                    lj = sx2(payload_part(a.L, kr) >> 2);
                 }
                 if (kj != k1) break;
                 wc = wadd(wc, lj);
