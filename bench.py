@@ -204,6 +204,17 @@ def run_batched(sr, args, sptr, steps):
         b.commit()
         batches.append(b)
     build_s = time.perf_counter() - t0
+    # launch shapes for this size class: timed on the first batch, cached in
+    # JSON, applied to the batches of the same class
+    tpath = os.path.join(tempfile.mkdtemp(prefix="srtune"), "tuning.json")
+    t0 = time.perf_counter()
+    tuning = batches[0].autotune(tpath, stream=sptr)
+    tune_s = time.perf_counter() - t0
+    tclass = batches[0].tuning_class()
+    with open(tpath) as f:
+        tune_cache = json.load(f)
+    for b in batches[1:]:
+        b.set_tuning(**tuning)
     caps, records = [], 0
     for b in batches:           # exact frame: learns each batch's record count
         b.render(stream=sptr)
@@ -262,7 +273,9 @@ def run_batched(sr, args, sptr, steps):
             "sizing": "record capacity from the previous exact frame, frame replayed as a CUDA graph",
             "overflows": int(overflows), "plain_scenes_per_s": round(plain_sps, 1),
             "plain_sample": nplain, "speedup_vs_plain": round(batched_sps / plain_sps, 2),
-            "bit_exact_vs_plain": "%d/%d" % (exact, checked), "build_s": round(build_s, 2)}
+            "bit_exact_vs_plain": "%d/%d" % (exact, checked), "build_s": round(build_s, 2),
+            "autotune": {"class": tclass, "chosen": tuning, "seconds": round(tune_s, 2),
+                         "cache": tune_cache}}
 
 
 def _labels_of(sr, batches_spec, sptr):

@@ -281,6 +281,28 @@ sr_status sr_batch_get_stats(const sr_batch* b, sr_batch_stats* out);
 sr_status sr_batch_clear(sr_batch* b);
 void sr_batch_destroy(sr_batch* b);
 
+/* Launch shapes of the tunable kernels (identical images for every choice). */
+typedef struct sr_tuning {
+    uint32_t struct_size;
+    int32_t  sort_items;      /* keys per thread of a sort tile: 8, 12 (default) or 16 */
+    int32_t  resolve_warps;   /* warps per resolve CTA: 8 or 16 (default) */
+    int32_t  wind_items;      /* records per thread of a winding tile: 4 or 8 (default) */
+} sr_tuning;
+
+sr_status sr_set_tuning(sr_ctx* c, const sr_tuning* t);
+sr_status sr_batch_set_tuning(sr_batch* b, const sr_tuning* t);
+sr_status sr_batch_get_tuning(const sr_batch* b, sr_tuning* t);
+/* The batch's size class: "m<mode>/s<side>/r<log2 records>", side the
+ * largest canvas side rounded up to a power of two (256, 512, 1024, 2048,
+ * ...).  Needs a rendered frame (for the record count). */
+sr_status sr_batch_tuning_class(sr_batch* b, char* buf, size_t len);
+/* Picks the tuning of the batch's size class: from the JSON cache file
+ * cache_path (may be NULL) when it holds the class and force is 0,
+ * otherwise by timing frames of this batch for every value of each knob in
+ * turn (the others held), keeping the fastest, and storing the choice in
+ * the cache.  The batch keeps the chosen tuning. */
+sr_status sr_batch_autotune(sr_batch* b, const char* cache_path, int force, sr_tuning* chosen, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Learned buffer sizing (replaces the count read-back of              */
 /* scanline_rasterizer.cpp:337-358 and pre-sizes the fragment buffers   */

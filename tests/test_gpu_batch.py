@@ -86,3 +86,39 @@ def test_batch_synth_matches_oracle_synth(gpu, oracle_lib):
         assert b.size(first + i) == (s.width, s.height)
         assert np.array_equal(b.image(first + i), oracle_lib.Frame(s, mode=1).get("image"))
     b.close()
+
+
+@pytest.mark.parametrize("tuning", [(8, 8, 4), (16, 16, 8), (12, 8, 8), (8, 16, 4)])
+def test_every_tuning_gives_the_same_images(gpu, oracle_lib, tuning):
+    scs = _mixed_scenes(oracle_lib)
+    want = _oracle_images(oracle_lib, scs, 1)
+    b = gpu.SceneBatch(mode=1)
+    for s in scs:
+        b.add_scene(_container(gpu, s))
+    b.set_tuning(*tuning)
+    b.render()
+    for i, w in enumerate(want):
+        assert np.array_equal(b.image(i), w), (tuning, i)
+    b.render(capacity=b.stats()["n_intersections"], graph=True)
+    for i, w in enumerate(want):
+        assert np.array_equal(b.image(i), w), (tuning, i)
+    b.close()
+
+
+def test_autotune_caches_its_choice(gpu, tmp_path):
+    import json
+    path = str(tmp_path / "tuning.json")
+    b = gpu.SceneBatch(mode=1)
+    b.add_synth(2, 9, 16)
+    t1 = b.autotune(path)
+    cls = b.tuning_class()
+    with open(path) as f:
+        cache = json.load(f)
+    assert cache[cls]["sort_items"] == t1["sort_items"] and cache[cls]["frame_ms"] > 0
+    # a second batch of the same class takes the cached choice without timing
+    b2 = gpu.SceneBatch(mode=1)
+    b2.add_synth(2, 9, 16)
+    b2.set_tuning(16 if t1["sort_items"] != 16 else 8, 8 if t1["resolve_warps"] != 8 else 16, 4)
+    assert b2.autotune(path) == t1
+    b.close()
+    b2.close()

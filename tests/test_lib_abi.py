@@ -49,3 +49,10 @@ def test_cuda_sources_compile_for_sm103a_only():
     from vkscanlinepr_gb300 import builder
     assert builder.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
     assert "--fmad=false" in builder.NVCC_FLAGS
+
+
+def test_tuning_values_are_checked(srlib):
+    L = srlib.lib()
+    t = srlib.Tuning(ctypes.sizeof(srlib.Tuning), 10, 16, 8)
+    assert L.sr_set_tuning(None, ctypes.byref(t)) == 1
+    assert L.sr_batch_set_tuning(None, ctypes.byref(t)) == 1

@@ -78,6 +78,15 @@ class BatchRenderOpts(ctypes.Structure):
                 ("reserved", ctypes.c_uint32), ("draw_capacity", ctypes.c_int64)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("sort_items", ctypes.c_int32), ("resolve_warps", ctypes.c_int32),
+                ("wind_items", ctypes.c_int32)]
+
+
+def _tuning(d):
+    return Tuning(ctypes.sizeof(Tuning), int(d["sort_items"]), int(d["resolve_warps"]), int(d["wind_items"]))
+
+
 SIZER_FEATURES, SIZER_OUTPUTS, SIZER_PARAMS, SIZER_NORM = 6, 2, 4738, 16
 
 
@@ -149,7 +158,8 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_batch_frame_bytes", "sr_device_alloc", "sr_device_free", "sr_memcpy", "sr_batch_enqueue",
            "sr_batch_query", "sr_batch_finish", "sr_batch_release", "sr_batch_held_bytes", "sr_batch_path_ranges",
            "sr_server_create", "sr_server_submit", "sr_server_wait", "sr_server_get_stats", "sr_server_destroy",
-           "sr_admission_take"]
+           "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
+           "sr_batch_tuning_class", "sr_batch_autotune"]
 
 _lib = None
 
@@ -233,6 +243,11 @@ def lib():
     L.sr_admission_take.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
                                     ctypes.POINTER(ctypes.c_int)]
     L.sr_admission_take.restype = ctypes.c_uint32
+    L.sr_set_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.sr_batch_set_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.sr_batch_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.sr_batch_tuning_class.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    L.sr_batch_autotune.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(Tuning), vp]
     L.sr_batch_judge.argtypes = [vp, ctypes.POINTER(SizingJudge), vp]
     L.sr_batch_frame_bytes.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
     L.sr_batch_release.argtypes = [vp]
@@ -455,6 +470,10 @@ class ScanlineVGRasterizer:
         _check(lib().sr_render(self._ctx, ptr, 0, stream))
         return out
 
+    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8):
+        t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items})
+        _check(lib().sr_set_tuning(self._h, ctypes.byref(t)))
+
     def render_draw_list(self, records, out=None, stream=None):
         """Paints an (n, 4) int32 draw list (the reference's MOCK_DATA path)."""
         rec = np.ascontiguousarray(records, np.int32).reshape(-1, 4)
@@ -566,6 +585,27 @@ class SceneBatch:
 
     def n_paths(self):
         return self.stats()["n_paths"]
+
+    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8):
+        t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items})
+        _check(lib().sr_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def tuning(self):
+        t = Tuning()
+        _check(lib().sr_batch_get_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_ if k != "struct_size"}
+
+    def tuning_class(self):
+        buf = ctypes.create_string_buffer(64)
+        _check(lib().sr_batch_tuning_class(self._h, buf, 64))
+        return buf.value.decode()
+
+    def autotune(self, cache_path=None, force=False, stream=None):
+        """Tuning of this batch's size class, from the JSON cache or by timing."""
+        t = Tuning()
+        _check(lib().sr_batch_autotune(self._h, cache_path.encode() if cache_path else None, 1 if force else 0,
+                                       ctypes.byref(t), stream))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_ if k != "struct_size"}
 
     def features(self, out=None, stream=None):
         """Per-path sizing features under the current transforms: DeviceArray [P, 6]."""

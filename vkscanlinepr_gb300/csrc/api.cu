@@ -19,6 +19,9 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
 #include <string>
 #include <thread>
 #include <vector>
@@ -200,6 +203,7 @@ struct Pipeline {
     int32_t mode = SR_MODE_PIXEL, F = 1;
     uint32_t flags = 0;
     bool loaded = false;
+    sr_tuning tune{sizeof(sr_tuning), 12, 16, 8};
     // scenes
     uint32_t S = 0, V = 0, C = 0, P = 0;
     int32_t Wmax = 1, Hmax = 1;
@@ -300,7 +304,7 @@ struct Pipeline {
             Wmax = std::max(Wmax, si.W);
             Hmax = std::max(Hmax, si.H);
             cta_base[s] = res_ctas;
-            uint32_t rpc = sr::resolve_rows_per_cta(si.W);
+            uint32_t rpc = sr::resolve_rows_per_cta(si.W, tune.resolve_warps);
             res_ctas += (si.rows + rpc - 1) / rpc;
         }
         cta_base[S] = res_ctas;
@@ -470,8 +474,9 @@ struct Pipeline {
         fn(svals, idx ? sizeof(uint32_t) * n1 : 0);
         fn(vals_alt, idx ? sizeof(uint32_t) * n1 : 0);
         const sr::KeyLayout L = layout();
-        fn(sort_scratch, sr::sort_scratch_bytes(sr::sort_plan(cap, L.pbits + L.rbits + L.xbits, nullptr)));
-        fn(wind_status, sizeof(uint64_t) * sr::winding_status_words(cap));
+        fn(sort_scratch,
+           sr::sort_scratch_bytes(sr::sort_plan(cap, L.pbits + L.rbits + L.xbits, nullptr, tune.sort_items)));
+        fn(wind_status, sizeof(uint64_t) * sr::winding_status_words(cap, tune.wind_items));
         const size_t d1 = (size_t)draw_cap_for(cap, dcap);
         fn(draw, sizeof(int4) * d1);
         fn(draw_row, sizeof(uint32_t) * d1);
@@ -613,13 +618,13 @@ struct Pipeline {
                         st);
         mark(ST_FRAGMENT, true);
         const KeyLayout L = g.L;
-        SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev);
+        SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev, tune.sort_items);
         mark(ST_SORT, false);
         launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(), keep ? svals.as<uint32_t>() : nullptr,
                         keys_alt.as<uint64_t>(), keep ? vals_alt.as<uint32_t>() : nullptr, sort_scratch.p, status,
                         st);
         mark(ST_SORT, true);
-        CUDA_TRY(cudaMemsetAsync(wind_status.p, 0, sizeof(uint64_t) * winding_status_words(cap), st));
+        CUDA_TRY(cudaMemsetAsync(wind_status.p, 0, sizeof(uint64_t) * winding_status_words(cap, tune.wind_items), st));
         WindArgs wa;
         wa.n = cap;
         wa.n_dev = n_dev;
@@ -647,7 +652,7 @@ struct Pipeline {
         wa.dbg_sflag = keep ? d_sflag.as<int32_t>() : nullptr;
         wa.dbg_skey = keep ? d_skey.as<int32_t>() : nullptr;
         mark(ST_WINDING, false);
-        launch_winding_emit(wa, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
+        launch_winding_emit(wa, tune.wind_items, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
         mark(ST_WINDING, true);
         SortPlan rp = sort_plan(dcap, bits_for(total_rows), ctlp + CTL_NDRAW);
         mark(ST_ROWSORT, false);
@@ -664,6 +669,7 @@ struct Pipeline {
         ra.scenes = scenes_d.as<SceneInfo>();
         ra.n_scenes = S;
         ra.F = F;
+        ra.warps = tune.resolve_warps;
         ra.pixel_mode = g.pixel_mode;
         ra.image = image.as<uint32_t>();
         mark(ST_RESOLVE, false);
@@ -921,6 +927,7 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     ra.scenes = p.scenes_d.as<sr::SceneInfo>();
     ra.n_scenes = p.S;
     ra.F = p.F;
+    ra.warps = p.tune.resolve_warps;
     ra.pixel_mode = p.mode == SR_MODE_PIXEL;
     ra.image = p.image.as<uint32_t>();
     sr::launch_resolve(ra, p.res_ctas, st);
@@ -1628,6 +1635,202 @@ sr_status sr_batch_judge(sr_batch* b, sr_sizing_judge* out, void* stream) {
     out->paths_over_draws = (uint32_t)h[1];
     out->records = (int64_t)h[2];
     out->draws = (int64_t)h[3];
+    return SR_OK;
+}
+
+// ------------------------------------------------------------- tuning ---
+
+static sr_status check_tuning(const sr_tuning* t) {
+    if (!t || t->struct_size < sizeof(sr_tuning)) return fail(SR_ERR_INVALID_ARG, "bad sr_tuning");
+    if ((t->sort_items != 8 && t->sort_items != 12 && t->sort_items != 16) ||
+        (t->resolve_warps != 8 && t->resolve_warps != 16) || (t->wind_items != 4 && t->wind_items != 8))
+        return fail(SR_ERR_INVALID_ARG, "tuning values: sort_items 8/12/16, resolve_warps 8/16, wind_items 4/8");
+    return SR_OK;
+}
+
+static sr_status apply_tuning(Pipeline& p, const sr_tuning& t) {
+    const bool warps_changed = t.resolve_warps != p.tune.resolve_warps;
+    p.tune = t;
+    p.tune.struct_size = sizeof(sr_tuning);
+    if (warps_changed && p.loaded) {   // resolve CTAs per scene depend on the warps per CTA
+        CUDA_TRY(cudaSetDevice(p.device));
+        SR_TRY(p.upload_table());
+    }
+    return SR_OK;
+}
+
+static void drop_graph(sr_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_cap = -1;
+    b->graph_dcap = -1;
+}
+
+sr_status sr_set_tuning(sr_ctx* c, const sr_tuning* t) {
+    if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
+    SR_TRY(check_tuning(t));
+    return apply_tuning(c->p, *t);
+}
+
+sr_status sr_batch_set_tuning(sr_batch* b, const sr_tuning* t) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
+    if (b->inflight) return fail(SR_ERR_INVALID_ARG, "tuning while a frame is in flight");
+    SR_TRY(check_tuning(t));
+    drop_graph(b);
+    return apply_tuning(b->p, *t);
+}
+
+sr_status sr_batch_get_tuning(const sr_batch* b, sr_tuning* t) {
+    if (!b || !t) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    *t = b->p.tune;
+    return SR_OK;
+}
+
+static std::string tuning_class(const Pipeline& p) {
+    uint32_t side = 256;
+    while (side < (uint32_t)std::max(p.Wmax, p.Hmax) && side < (1u << 15)) side <<= 1;
+    uint32_t r = 0;
+    while (r < 40 && (1ll << (r + 1)) <= std::max<int64_t>(p.last_N, 1)) ++r;
+    char buf[64];
+    snprintf(buf, sizeof buf, "m%d/s%u/r%u", p.mode, side, r);
+    return buf;
+}
+
+sr_status sr_batch_tuning_class(sr_batch* b, char* buf, size_t len) {
+    if (!b || !buf || len == 0) return fail(SR_ERR_INVALID_ARG, "bad argument");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    if (b->p.last_N <= 0) SR_TRY(sr_batch_render(b, nullptr, nullptr));
+    snprintf(buf, len, "%s", tuning_class(b->p).c_str());
+    return SR_OK;
+}
+
+// The tuning cache: a JSON object with one entry per line,
+//   "<class>": {"sort_items": 12, "resolve_warps": 16, "wind_items": 8, "frame_ms": 1.234},
+// read and rewritten whole; lines it does not recognise are dropped.
+struct TuneEntry {
+    sr_tuning t;
+    double ms;
+};
+
+static std::map<std::string, TuneEntry> read_tuning_cache(const char* path) {
+    std::map<std::string, TuneEntry> m;
+    if (!path) return m;
+    std::ifstream in(path);
+    std::string line;
+    auto field = [](const std::string& l, const char* name, double* v) {
+        const std::string key = std::string("\"") + name + "\":";
+        size_t at = l.find(key);
+        if (at == std::string::npos) return false;
+        *v = std::strtod(l.c_str() + at + key.size(), nullptr);
+        return true;
+    };
+    while (std::getline(in, line)) {
+        size_t q0 = line.find('"');
+        size_t q1 = q0 == std::string::npos ? q0 : line.find('"', q0 + 1);
+        if (q1 == std::string::npos || line.find('{', q1) == std::string::npos) continue;
+        double si = 0, rw = 0, wi = 0, ms = 0;
+        if (!field(line, "sort_items", &si) || !field(line, "resolve_warps", &rw) || !field(line, "wind_items", &wi))
+            continue;
+        field(line, "frame_ms", &ms);
+        TuneEntry e{{sizeof(sr_tuning), (int32_t)si, (int32_t)rw, (int32_t)wi}, ms};
+        if (check_tuning(&e.t) == SR_OK) m[line.substr(q0 + 1, q1 - q0 - 1)] = e;
+    }
+    return m;
+}
+
+static sr_status write_tuning_cache(const char* path, const std::map<std::string, TuneEntry>& m) {
+    const std::string tmp = std::string(path) + ".tmp";
+    {
+        std::ofstream out(tmp);
+        if (!out) return fail(SR_ERR_INVALID_ARG, "cannot write tuning cache %s", path);
+        out << "{\n";
+        size_t i = 0;
+        for (const auto& kv : m) {
+            char buf[256];
+            snprintf(buf, sizeof buf,
+                     "  \"%s\": {\"sort_items\": %d, \"resolve_warps\": %d, \"wind_items\": %d, \"frame_ms\": %.4f}%s\n",
+                     kv.first.c_str(), kv.second.t.sort_items, kv.second.t.resolve_warps, kv.second.t.wind_items,
+                     kv.second.ms, ++i < m.size() ? "," : "");
+            out << buf;
+        }
+        out << "}\n";
+    }
+    if (std::rename(tmp.c_str(), path) != 0) return fail(SR_ERR_INVALID_ARG, "cannot replace %s", path);
+    return SR_OK;
+}
+
+// Device time of the batch's frame with a pre-sized capacity: the best of
+// `reps` frames (CUDA events on the stream).
+static sr_status time_frames(sr_batch* b, int64_t cap, int reps, cudaStream_t st, float* best) {
+    sr_batch_render_opts o{};
+    o.struct_size = sizeof o;
+    o.record_capacity = cap;
+    o.refit_on_overflow = 1;
+    o.draw_capacity = -1;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    *best = 1e30f;
+    sr_status s = sr_batch_render(b, &o, st);   // warm (allocations at this tuning)
+    for (int i = 0; i < reps && s == SR_OK; ++i) {
+        cudaEventRecord(e0, st);
+        s = sr_batch_render(b, &o, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *best = std::min(*best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return s;
+}
+
+sr_status sr_batch_autotune(sr_batch* b, const char* cache_path, int force, sr_tuning* chosen, void* stream) {
+    if (!b) return fail(SR_ERR_INVALID_ARG, "NULL batch");
+    if (b->inflight) return fail(SR_ERR_INVALID_ARG, "autotune while a frame is in flight");
+    if (!b->committed) SR_TRY(sr_batch_commit(b));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Pipeline& p = b->p;
+    SR_TRY(sr_batch_render(b, nullptr, stream));   // exact frame: the record count of the class
+    const std::string cls = tuning_class(p);
+    std::map<std::string, TuneEntry> cache = read_tuning_cache(cache_path);
+    auto it = cache.find(cls);
+    if (it != cache.end() && !force) {
+        SR_TRY(sr_batch_set_tuning(b, &it->second.t));
+        if (chosen) *chosen = p.tune;
+        return SR_OK;
+    }
+    const int64_t cap = p.last_N;
+    sr_tuning best = p.tune;
+    float best_ms = 0;
+    SR_TRY(time_frames(b, cap, 3, st, &best_ms));
+    const int sort_opts[] = {8, 12, 16}, warp_opts[] = {8, 16}, wind_opts[] = {4, 8};
+    for (int knob = 0; knob < 3; ++knob) {
+        const int* opts = knob == 0 ? sort_opts : knob == 1 ? warp_opts : wind_opts;
+        const int n = knob == 0 ? 3 : 2;
+        for (int i = 0; i < n; ++i) {
+            sr_tuning t = best;
+            int32_t& v = knob == 0 ? t.sort_items : knob == 1 ? t.resolve_warps : t.wind_items;
+            if (v == opts[i]) continue;
+            v = opts[i];
+            SR_TRY(sr_batch_set_tuning(b, &t));
+            float ms = 0;
+            SR_TRY(time_frames(b, cap, 3, st, &ms));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
+    }
+    SR_TRY(sr_batch_set_tuning(b, &best));
+    if (cache_path) {
+        cache[cls] = TuneEntry{best, (double)best_ms};
+        SR_TRY(write_tuning_cache(cache_path, cache));
+    }
+    if (chosen) *chosen = best;
     return SR_OK;
 }
 

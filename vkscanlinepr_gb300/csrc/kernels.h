@@ -110,8 +110,9 @@ struct SortPlan {
     uint32_t key_bits;
     uint32_t passes;
     uint32_t tiles;
+    int items;                 // keys per thread of a tile: 8, 12 or 16
 };
-SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev = nullptr);
+SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev = nullptr, int items = 12);
 // Device scratch needed by a plan (bytes).
 size_t sort_scratch_bytes(const SortPlan& p);
 // Sorts (keys, values) stably by the low key_bits of the keys; higher bits
@@ -151,9 +152,10 @@ struct WindArgs {
     int32_t* dbg_sflag;             // [N]
     int32_t* dbg_skey;              // [N]
 };
-size_t winding_status_words(int64_t n);
-void launch_winding_emit(const WindArgs& a, uint64_t* tile_status, uint32_t* tile_counter, uint32_t* status,
-                         cudaStream_t st);
+// items: records per thread of a tile (4 or 8).
+size_t winding_status_words(int64_t n, int items = 8);
+void launch_winding_emit(const WindArgs& a, int items, uint64_t* tile_status, uint32_t* tile_counter,
+                         uint32_t* status, cudaStream_t st);
 
 // ---- resolve.cu
 // Resolve work: each CTA paints rows_per_cta cell rows of one scene;
@@ -167,12 +169,12 @@ struct ResolveArgs {
     uint32_t n_scenes;
     int32_t F;
     int32_t pixel_mode;
+    int32_t warps;                    // warps per CTA: 8 or 16
     uint32_t* image;                  // all scenes' RGBA8 framebuffers
 };
-// Warps per resolve CTA and pixels per warp.
-constexpr int kResolveWarps = 16;
+// Pixels per warp of a resolve CTA.
 constexpr int kResolveSeg = 256;
-uint32_t resolve_rows_per_cta(int32_t W);
+uint32_t resolve_rows_per_cta(int32_t W, int warps);
 void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st);
 // n_dev (optional) holds the record count; n is the capacity.
 void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,

@@ -55,9 +55,9 @@ SR_DEV void blend3(float& r, float& g, float& b, const PixRec& q) {
     b = __fsub_rn(__fmaf_rn(ub, inv, kRound), kRound);
 }
 
-uint32_t resolve_rows_per_cta(int32_t W) {
+uint32_t resolve_rows_per_cta(int32_t W, int warps) {
     int32_t segs = (W + kResolveSeg - 1) / kResolveSeg;
-    return segs >= kResolveWarps ? 1u : (uint32_t)(kResolveWarps / segs);
+    return segs >= warps ? 1u : (uint32_t)(warps / segs);
 }
 
 // Which rows and segment a warp paints: a CTA holds rows_per_cta cell rows
@@ -68,7 +68,8 @@ struct ResolveWork {
     bool active;
 };
 
-SR_DEV ResolveWork resolve_work(const ResolveArgs& a) {
+template <int WARPS> SR_DEV ResolveWork resolve_work(const ResolveArgs& a) {
+    constexpr int kResolveWarps = WARPS;
     // scene of this CTA: last s with cta_base[s] <= blockIdx.x
     uint32_t lo = 0, hi = a.n_scenes;
     while (hi - lo > 1) {
@@ -96,20 +97,22 @@ SR_DEV ResolveWork resolve_work(const ResolveArgs& a) {
     return w;
 }
 
-SR_DEV int32_t resolve_seg(const ResolveWork& w, int group) {
+template <int WARPS> SR_DEV int32_t resolve_seg(const ResolveWork& w, int group) {
+    constexpr int kResolveWarps = WARPS;
     const int warp = threadIdx.x >> 5;
     return w.segs >= kResolveWarps ? group * kResolveWarps + warp : warp % w.segs;
 }
 
-__global__ void __launch_bounds__(32 * kResolveWarps) k_resolve_pixel(const ResolveArgs a) {
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs a) {
     __shared__ PixRec sq[kChunk];
-    const ResolveWork w = resolve_work(a);
+    const ResolveWork w = resolve_work<WARPS>(a);
     const int tid = threadIdx.x, lane = tid & 31;
     const int32_t W = w.W;
     const uint32_t gr0 = w.si->row_base + (uint32_t)w.r0;
     const int32_t beg = a.row_start[gr0], end = a.row_start[gr0 + (uint32_t)w.nr];
     for (int group = 0; group < w.groups; ++group) {
-        const int32_t seg = resolve_seg(w, group) * kResolveSeg;
+        const int32_t seg = resolve_seg<WARPS>(w, group) * kResolveSeg;
         const bool live = w.active && seg < W;
         float r[kK], g[kK], b[kK];
 #pragma unroll
@@ -195,15 +198,16 @@ struct RefRec {
     int32_t row;
 };
 
-__global__ void __launch_bounds__(32 * kResolveWarps) k_resolve_ref(const ResolveArgs a) {
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a) {
     __shared__ RefRec sq[kChunk];
-    const ResolveWork w = resolve_work(a);
+    const ResolveWork w = resolve_work<WARPS>(a);
     const int tid = threadIdx.x, lane = tid & 31;
     const int32_t W = w.W;
     const uint32_t gr0 = w.si->row_base + (uint32_t)w.r0;
     const int32_t beg = a.row_start[gr0], end = a.row_start[gr0 + (uint32_t)w.nr];
     for (int group = 0; group < w.groups; ++group) {
-        const int32_t seg = resolve_seg(w, group) * kResolveSeg;
+        const int32_t seg = resolve_seg<WARPS>(w, group) * kResolveSeg;
         const bool live = w.active && seg < W;
         uint32_t px[kK];
 #pragma unroll
@@ -257,8 +261,13 @@ __global__ void __launch_bounds__(32 * kResolveWarps) k_resolve_ref(const Resolv
 void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st) {
     if (n_ctas == 0) return;
     count_launches(1);
-    if (a.pixel_mode) k_resolve_pixel<<<n_ctas, 32 * kResolveWarps, 0, st>>>(a);
-    else k_resolve_ref<<<n_ctas, 32 * kResolveWarps, 0, st>>>(a);
+    if (a.warps == 8) {
+        if (a.pixel_mode) k_resolve_pixel<8><<<n_ctas, 32 * 8, 0, st>>>(a);
+        else k_resolve_ref<8><<<n_ctas, 32 * 8, 0, st>>>(a);
+    } else {
+        if (a.pixel_mode) k_resolve_pixel<16><<<n_ctas, 32 * 16, 0, st>>>(a);
+        else k_resolve_ref<16><<<n_ctas, 32 * 16, 0, st>>>(a);
+    }
 }
 
 void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,

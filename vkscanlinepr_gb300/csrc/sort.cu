@@ -24,8 +24,7 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 12;
-constexpr int kTile = kThreads * kItems;
+// Keys per thread of a tile: 8, 12 or 16 (chosen per plan; 12 by default).
 constexpr uint32_t kFlagA = 1u << 30;
 constexpr uint32_t kFlagP = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1u;
@@ -75,14 +74,15 @@ Scratch carve(const SortPlan& p, void* base) {
 }
 }  // namespace
 
-SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev) {
+SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev, int items) {
     SortPlan p;
     p.n = n;
     p.n_dev = n_dev;
     p.key_bits = key_bits;
     p.passes = (key_bits + kRadixBits - 1) / kRadixBits;
     if (p.passes == 0) p.passes = 1;
-    p.tiles = (uint32_t)((n + kTile - 1) / kTile);
+    p.items = items == 8 || items == 16 ? items : 12;
+    p.tiles = (uint32_t)((n + kThreads * p.items - 1) / (kThreads * p.items));
     return p;
 }
 
@@ -151,18 +151,24 @@ __global__ void __launch_bounds__(kRadix) k_hist_scan(uint32_t* hist) {
     h[threadIdx.x] = sw[warp] + x - v;
 }
 
-template <typename K, bool kVals> struct OnesweepSmem {
+template <typename K, bool kVals, int ITEMS> struct OnesweepSmem {
     uint32_t warp_hist[kWarps][kRadix];
     uint32_t digit_start[kRadix];   // tile-local exclusive start of each digit
     uint32_t digit_global[kRadix];  // global base minus digit_start
     uint32_t scan_tmp[kWarps];
     uint32_t tile;
-    K keys[kTile];
-    uint32_t vals[kVals ? kTile : 1];
+    K keys[kThreads * ITEMS];
+    uint32_t vals[kVals ? kThreads * ITEMS : 1];
 };
 
-template <typename K, bool kVals>
-__global__ void __launch_bounds__(kThreads, kVals ? 3 : 4) k_onesweep(const K* __restrict__ keys_in,
+// Resident CTAs per SM the register budget is set for.
+constexpr int onesweep_min_blocks(bool vals, int items) {
+    return vals ? (items <= 8 ? 4 : items <= 12 ? 3 : 2) : (items <= 8 ? 5 : items <= 12 ? 4 : 3);
+}
+
+template <typename K, bool kVals, int ITEMS>
+__global__ void __launch_bounds__(kThreads, onesweep_min_blocks(kVals, ITEMS)) k_onesweep(
+                                                       const K* __restrict__ keys_in,
                                                        const uint32_t* __restrict__ vals_in,
                                                        K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                        int64_t n_max, const uint32_t* __restrict__ n_dev,
@@ -171,7 +177,8 @@ __global__ void __launch_bounds__(kThreads, kVals ? 3 : 4) k_onesweep(const K* _
                                                        uint32_t* __restrict__ lookback, uint32_t* counter,
                                                        uint32_t* status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    OnesweepSmem<K, kVals>& S = *reinterpret_cast<OnesweepSmem<K, kVals>*>(smem_raw);
+    constexpr int kItems = ITEMS, kTile = kThreads * ITEMS;
+    OnesweepSmem<K, kVals, ITEMS>& S = *reinterpret_cast<OnesweepSmem<K, kVals, ITEMS>*>(smem_raw);
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
     if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
@@ -314,7 +321,7 @@ __global__ void __launch_bounds__(kThreads, kVals ? 3 : 4) k_onesweep(const K* _
     }
 }
 
-template <typename K, bool kVals>
+template <typename K, bool kVals, int ITEMS>
 static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_in, K* keys_out, uint32_t* vals_out,
                       K* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status, cudaStream_t st) {
     if (p.n <= 0) return;
@@ -328,10 +335,10 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
     k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.n_dev, p.passes, p.key_bits, s.hist);
     count_launches(1);
     k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
-    const size_t smem = sizeof(OnesweepSmem<K, kVals>);
+    const size_t smem = sizeof(OnesweepSmem<K, kVals, ITEMS>);
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_onesweep<K, kVals>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_onesweep<K, kVals, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr_set = true;
     }
     const K* ksrc = keys_in;
@@ -341,7 +348,7 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
         K* kdst = to_out ? keys_out : keys_alt;
         uint32_t* vdst = to_out ? vals_out : vals_alt;
         count_launches(1);
-        k_onesweep<K, kVals><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, p.n_dev,
+        k_onesweep<K, kVals, ITEMS><<<p.tiles, kThreads, smem, st>>>(ksrc, vsrc, kdst, vdst, p.n, p.n_dev,
                                                              pass * kRadixBits,
                                                              digit_mask(p.key_bits, pass * kRadixBits),
                                                              s.hist + pass * kRadix,
@@ -352,20 +359,35 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
     }
 }
 
+template <typename K>
+static void sort_dispatch(const SortPlan& p, const K* keys_in, const uint32_t* vals_in, K* keys_out, uint32_t* vals_out,
+                          K* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status, cudaStream_t st) {
+#define SR_SORT_CASE(ITEMS)                                                                                        \
+    if (p.items == ITEMS) {                                                                                        \
+        if (vals_out)                                                                                              \
+            sort_impl<K, true, ITEMS>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, \
+                                      st);                                                                         \
+        else                                                                                                       \
+            sort_impl<K, false, ITEMS>(p, keys_in, nullptr, keys_out, nullptr, keys_alt, nullptr, scratch, status,  \
+                                       st);                                                                        \
+        return;                                                                                                    \
+    }
+    SR_SORT_CASE(8)
+    SR_SORT_CASE(16)
+    SR_SORT_CASE(12)
+#undef SR_SORT_CASE
+}
+
 void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                      uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
                      cudaStream_t st) {
-    if (vals_out) sort_impl<uint64_t, true>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch,
-                                            status, st);
-    else sort_impl<uint64_t, false>(p, keys_in, nullptr, keys_out, nullptr, keys_alt, nullptr, scratch, status, st);
+    sort_dispatch<uint64_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
 }
 
 void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, uint32_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
                      cudaStream_t st) {
-    if (vals_out) sort_impl<uint32_t, true>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch,
-                                            status, st);
-    else sort_impl<uint32_t, false>(p, keys_in, nullptr, keys_out, nullptr, keys_alt, nullptr, scratch, status, st);
+    sort_dispatch<uint32_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
 }
 
 }  // namespace sr

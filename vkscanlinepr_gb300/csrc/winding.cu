@@ -24,9 +24,7 @@
 namespace sr {
 
 namespace {
-constexpr int kThreads = 256;
-constexpr int kItems = 8;
-constexpr int kTile = kThreads * kItems;
+constexpr int kThreads = 256;   // records per tile: kThreads x ITEMS (4 or 8)
 constexpr uint64_t kFlagA = 1ull << 62;
 constexpr uint64_t kFlagP = 2ull << 62;
 constexpr uint64_t kValMask = (1ull << 62) - 1;
@@ -94,7 +92,8 @@ SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
     return excl;
 }
 
-struct Smem {
+template <int ITEMS> struct Smem {
+    static constexpr int kTile = kThreads * ITEMS;
     uint32_t tile;
     int32_t warpA[kThreads / 32];
     int32_t warpAf[kThreads / 32];
@@ -106,10 +105,12 @@ struct Smem {
 };
 }  // namespace
 
+template <int ITEMS>
 __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uint64_t* __restrict__ tstatA,
                                                            uint64_t* __restrict__ tstatB, uint32_t* counter,
                                                            uint32_t* status) {
-    __shared__ Smem S;
+    constexpr int kItems = ITEMS, kTile = kThreads * ITEMS;
+    __shared__ Smem<ITEMS> S;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) S.tile = atomicAdd(counter, 1u);
     __syncthreads();
@@ -377,16 +378,22 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
     }
 }
 
-size_t winding_status_words(int64_t n) { return 2 * (size_t)((n + kTile - 1) / kTile + 1); }
+size_t winding_status_words(int64_t n, int items) {
+    const int64_t tile = (int64_t)kThreads * (items == 4 ? 4 : 8);
+    return 2 * (size_t)((n + tile - 1) / tile + 1);
+}
 
-void launch_winding_emit(const WindArgs& a, uint64_t* tile_status, uint32_t* tile_counter, uint32_t* status,
-                         cudaStream_t st) {
+void launch_winding_emit(const WindArgs& a, int items, uint64_t* tile_status, uint32_t* tile_counter,
+                         uint32_t* status, cudaStream_t st) {
     if (a.n <= 0) return;
-    int64_t tiles = (a.n + kTile - 1) / kTile;
+    items = items == 4 ? 4 : 8;
+    const int64_t tile = (int64_t)kThreads * items;
+    int64_t tiles = (a.n + tile - 1) / tile;
     uint64_t* sA = tile_status;
     uint64_t* sB = tile_status + (tiles + 1);
     count_launches(1);
-    k_winding_emit<<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
+    if (items == 4) k_winding_emit<4><<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
+    else k_winding_emit<8><<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
 }
 
 }  // namespace sr
