@@ -68,10 +68,15 @@ def parse_args():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", str(rank)))
-    return rank, world, local
+    from vkscanlinepr_gb300.replicas import dist_env as env
+    return env()
+
+
+def metric_name(workload):
+    """The metric both arms report for a workload."""
+    if workload == "frame4096":
+        return "frames/s (4096x4096, 20000 paths, 1 spp, bit-exact)"
+    return "frames/s (%s)" % workload
 
 
 def measured_peaks():
@@ -545,7 +550,7 @@ def main():
             oracle.Frame(sc, mode=oracle.MODE_PIXEL, threads=threads)
             t.append(time.perf_counter() - t0)
         v = len(t) / sum(t)
-        line = {"metric": "frames/s (%s)" % args.workload, "value": round(v, 4), "unit": "frames/s",
+        line = {"metric": metric_name(args.workload), "value": round(v, 4), "unit": "frames/s",
                 "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": round(1000 * sum(t) / len(t), 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -599,11 +604,8 @@ def main():
             stage_acc[k] += st["stage_ms"][k]
     torch.cuda.synchronize()
     clocks = clk.stop()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from vkscanlinepr_gb300 import replicas
+    total_ms = replicas.max_over_ranks(sum(step_ms))            # the slowest replica
     value = world * args.steps / (total_ms / 1000.0)
     st = r.stats()
 
@@ -631,11 +633,7 @@ def main():
     for _ in range(e2e_steps):
         r.loadVG(pscene)
         r.render(out=out_img, stream=sptr)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": round(world * e2e_steps / e2e_s, 4), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(W * H * 4)}
     gpu_img = out_img.copy()
@@ -664,8 +662,7 @@ def main():
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic}
 
-    line = {"metric": "frames/s (4096x4096, 20000 paths, 1 spp, bit-exact)" if args.workload == "frame4096"
-            else "frames/s (%s)" % args.workload,
+    line = {"metric": metric_name(args.workload),
             "value": round(value, 4), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
