@@ -166,9 +166,9 @@ def stage_bytes(st, n_curves, n_points, W, H):
         "chains": n_curves * (12 + 80 + 32) + N * 4,
         "merge": n_curves * (8 + 80) + N * (4 + 8),
         "fragment": N * (8 + 8),                       # record in, key (with winding bits) out
-        # keys only (the winding bits ride above the key): one histogram read,
-        # then per pass one read and one write of each 8-byte key
-        "sort": N * 8 + passes * N * 2 * 8,
+        # the per-path segmented sort: one read and one write of each 8-byte
+        # key (the least any sort moves; large paths' merge rounds come on top)
+        "sort": N * 2 * 8,
         # sorted keys in; draw records (16 B) and their cell rows (4 B) out
         "winding_emit": N * 8 + O * (16 + 4),
         "row_sort": O * 4 + row_passes * O * 2 * (4 + 4),

@@ -88,7 +88,7 @@ def test_batch_synth_matches_oracle_synth(gpu, oracle_lib):
     b.close()
 
 
-@pytest.mark.parametrize("tuning", [(8, 8, 4), (16, 16, 8), (12, 8, 8), (8, 16, 4)])
+@pytest.mark.parametrize("tuning", [(8, 8, 4, 1), (16, 16, 8, 1), (12, 8, 8, 0), (8, 16, 4, 0)])
 def test_every_tuning_gives_the_same_images(gpu, oracle_lib, tuning):
     scs = _mixed_scenes(oracle_lib)
     want = _oracle_images(oracle_lib, scs, 1)

@@ -149,3 +149,23 @@ def test_production_frame_equals_kept_stages_frame(gpu, oracle_lib, mode):
     assert np.array_equal(out[0][1], out[1][1])
     want = oracle_lib.Frame(s, mode=mode).get("image")
     assert np.array_equal(out[1][0], want)
+
+
+def test_segmented_sort_equals_radix_sort_at_full_size(gpu, oracle_lib):
+    """The per-path segmented sort and the radix sort give the same draw
+    list and image on the 4096x4096 20k-path frame (paths of up to ~58k
+    records, several merge rounds)."""
+    import oracle
+    s = oracle.synth(1, 1)
+    d = dict(width=s.width, height=s.height, **{f: getattr(s, f) for f in oracle.Scene.FIELDS})
+    out = []
+    for kind in (0, 1):
+        r = gpu.ScanlineVGRasterizer(mode=1)
+        r.initialize(None, d["width"], d["height"])
+        r.set_tuning(sort_kind=kind)
+        r.loadVG(scenes.to_container(d))
+        img = r.render().copy()
+        out.append((img, r.dump("draw_list").copy()))
+        r.close()
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][0], out[1][0])

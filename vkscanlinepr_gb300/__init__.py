@@ -80,11 +80,12 @@ class BatchRenderOpts(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("sort_items", ctypes.c_int32), ("resolve_warps", ctypes.c_int32),
-                ("wind_items", ctypes.c_int32)]
+                ("wind_items", ctypes.c_int32), ("sort_kind", ctypes.c_int32)]
 
 
 def _tuning(d):
-    return Tuning(ctypes.sizeof(Tuning), int(d["sort_items"]), int(d["resolve_warps"]), int(d["wind_items"]))
+    return Tuning(ctypes.sizeof(Tuning), int(d["sort_items"]), int(d["resolve_warps"]), int(d["wind_items"]),
+                  int(d.get("sort_kind", 0)))
 
 
 SIZER_FEATURES, SIZER_OUTPUTS, SIZER_PARAMS, SIZER_NORM = 6, 2, 4738, 16
@@ -470,9 +471,10 @@ class ScanlineVGRasterizer:
         _check(lib().sr_render(self._ctx, ptr, 0, stream))
         return out
 
-    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8):
-        t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items})
-        _check(lib().sr_set_tuning(self._h, ctypes.byref(t)))
+    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8, sort_kind=0):
+        t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items,
+                     "sort_kind": sort_kind})
+        _check(lib().sr_set_tuning(self._ctx, ctypes.byref(t)))
 
     def render_draw_list(self, records, out=None, stream=None):
         """Paints an (n, 4) int32 draw list (the reference's MOCK_DATA path)."""
@@ -586,8 +588,9 @@ class SceneBatch:
     def n_paths(self):
         return self.stats()["n_paths"]
 
-    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8):
-        t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items})
+    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8, sort_kind=0):
+        t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items,
+                     "sort_kind": sort_kind})
         _check(lib().sr_batch_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):

@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsr.so")
 REPO = os.path.dirname(HERE)
 
-CU_SOURCES = ["geom.cu", "scan.cu", "sort.cu", "winding.cu", "resolve.cu", "mlp.cu", "api.cu", "noalloc.cu"]
+CU_SOURCES = ["geom.cu", "scan.cu", "sort.cu", "winding.cu", "resolve.cu", "mlp.cu", "segsort.cu", "api.cu", "noalloc.cu"]
 CPP_SOURCES = ["host.cpp", "server.cpp"]
 HEADERS = ["common.cuh", "kernels.h", "synth.h"]
 

@@ -203,7 +203,11 @@ struct Pipeline {
     int32_t mode = SR_MODE_PIXEL, F = 1;
     uint32_t flags = 0;
     bool loaded = false;
-    sr_tuning tune{sizeof(sr_tuning), 12, 16, 8};
+    sr_tuning tune{sizeof(sr_tuning), 12, 16, 8, 0};
+    // segmented sort of this frame: merge rounds (-1: radix sort instead) and
+    // the largest segment the tables accept without flagging an overflow
+    int seg_levels = 0;
+    uint32_t seg_check = 0;
     // scenes
     uint32_t S = 0, V = 0, C = 0, P = 0;
     int32_t Wmax = 1, Hmax = 1;
@@ -219,7 +223,7 @@ struct Pipeline {
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
     // learned sizing: per-path curve ranges, draw counters, features,
     // predictions, allotments and their sums
-    DevBuf path_first, path_draw, feats, preds, allot, plan_tot, judge_out;
+    DevBuf path_first, path_draw, feats, preds, allot, plan_tot, judge_out, seg_scratch, seg_tiles;
     bool path_first_valid = false, count_paths = false, planned = false;
     unsigned long long* h_plan_ptr = nullptr;   // pinned plan totals
     size_t h_plan_words = 0;
@@ -242,7 +246,7 @@ struct Pipeline {
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
                          &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &image, &d_fkey,
                          &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
-                         &feats, &preds, &allot, &plan_tot, &judge_out};
+                         &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
@@ -447,8 +451,15 @@ struct Pipeline {
         CUDA_TRY(ensure(chain_sort_scratch, sr::sort_scratch_bytes(cp)));
         CUDA_TRY(ensure(totals, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(row_start, sizeof(int32_t) * ((size_t)total_rows + 1)));
+        if (segmented()) CUDA_TRY(ensure(seg_scratch, sr::segsort_scratch_bytes(std::max<uint32_t>(C, 1))));
         return SR_OK;
     }
+
+    // The production sort is the per-path segmented sort unless the tuning
+    // asks for the radix sort or the stages are kept (their sorted-index dump
+    // needs the radix sort with record indices).
+    bool segmented() const { return tune.sort_kind == 0 && !(flags & SR_FLAG_KEEP_STAGES) && C > 0; }
+    static constexpr int kSegLevelsMax = 5;
 
     // Draw-record capacity: every record gives at most one merged fragment
     // and one span, so 2 x records always suffices.
@@ -485,6 +496,7 @@ struct Pipeline {
         fn(rkeys_alt, sizeof(uint32_t) * d1);
         fn(rvals_alt, sizeof(uint32_t) * d1);
         fn(row_sort_scratch, sr::sort_scratch_bytes(sr::sort_plan((int64_t)d1, bits_for(total_rows), nullptr)));
+        fn(seg_tiles, segmented() ? sr::segsort_tile_bytes(C, std::max<int64_t>(cap, 1)) : 0);
     }
 
     // Device bytes a frame of this scene set holds with capacities (cap,
@@ -531,7 +543,7 @@ struct Pipeline {
                                &draw, &draw_row, &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt,
                                &row_sort_scratch, &row_start, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan,
                                &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
-                               &plan_tot, &judge_out};
+                               &plan_tot, &judge_out, &seg_scratch, &seg_tiles};
         uint64_t t = 0;
         for (const DevBuf* b : all) t += b->cap;
         return t;
@@ -585,6 +597,9 @@ struct Pipeline {
         mark(ST_SCAN, false);
         launch_exclusive_scan_i32(count.as<int32_t>(), offs.as<int32_t>(), C, scan_status.as<uint64_t>(),
                                   ctlp + CTL_SCAN_COUNTER, status, st);
+        if (segmented())
+            launch_segsort_tables(curve_path.as<uint32_t>(), offs.as<int32_t>(), C, seg_check, seg_scratch.p, status,
+                                  st);
         mark(ST_SCAN, true);
         CUDA_TRY(cudaGetLastError());
         return SR_OK;
@@ -620,9 +635,13 @@ struct Pipeline {
         const KeyLayout L = g.L;
         SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev, tune.sort_items);
         mark(ST_SORT, false);
-        launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(), keep ? svals.as<uint32_t>() : nullptr,
-                        keys_alt.as<uint64_t>(), keep ? vals_alt.as<uint32_t>() : nullptr, sort_scratch.p, status,
-                        st);
+        if (segmented() && seg_levels >= 0)
+            launch_segsort(keys.as<uint64_t>(), skeys.as<uint64_t>(), keys_alt.as<uint64_t>(), cap, C, L, seg_levels,
+                           seg_scratch.p, seg_tiles.p, status, st);
+        else
+            launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(),
+                            keep ? svals.as<uint32_t>() : nullptr, keys_alt.as<uint64_t>(),
+                            keep ? vals_alt.as<uint32_t>() : nullptr, sort_scratch.p, status, st);
         mark(ST_SORT, true);
         CUDA_TRY(cudaMemsetAsync(wind_status.p, 0, sizeof(uint64_t) * winding_status_words(cap, tune.wind_items), st));
         WindArgs wa;
@@ -683,8 +702,18 @@ struct Pipeline {
     sr_status read_count(cudaStream_t st, int64_t* N) {
         CUDA_TRY(cudaMemcpyAsync(&h_u32[0], offs.as<int32_t>() + C, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(&h_u32[1], ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        h_u32[2] = 0;
+        if (segmented())
+            CUDA_TRY(cudaMemcpyAsync(&h_u32[2], sr::segsort_largest(seg_scratch.p, C), sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         SR_TRY(check_status_word(h_u32[1]));
+        // merge rounds for the largest segment; past the limit the radix sort
+        seg_levels = 0;
+        const uint32_t T = (uint32_t)sr::segsort_tile();
+        uint32_t chunks = (h_u32[2] + T - 1) / T;
+        while (chunks > (1u << seg_levels)) ++seg_levels;
+        if (seg_levels > kSegLevelsMax) seg_levels = -1;
         *N = (int64_t)(int32_t)h_u32[0];
         if (*N < 0 || *N >= (1ll << 30))
             return fail(SR_ERR_OVERFLOW_REFIT, "record count %lld out of range", (long long)*N);
@@ -701,6 +730,10 @@ struct Pipeline {
         stages_valid = false;
         const uint64_t launches0 = sr::launches_so_far();
         SR_TRY(prepare_front());
+        // exact sizing reads the largest segment back; a pre-sized frame
+        // runs the most merge rounds and flags larger segments as overflow
+        seg_check = cap < 0 ? 0u : (uint32_t)sr::segsort_tile() << kSegLevelsMax;
+        seg_levels = kSegLevelsMax;
         SR_TRY(enqueue_front(st));
         if (cap < 0) {
             int64_t N = 0;
@@ -1643,8 +1676,10 @@ sr_status sr_batch_judge(sr_batch* b, sr_sizing_judge* out, void* stream) {
 static sr_status check_tuning(const sr_tuning* t) {
     if (!t || t->struct_size < sizeof(sr_tuning)) return fail(SR_ERR_INVALID_ARG, "bad sr_tuning");
     if ((t->sort_items != 8 && t->sort_items != 12 && t->sort_items != 16) ||
-        (t->resolve_warps != 8 && t->resolve_warps != 16) || (t->wind_items != 4 && t->wind_items != 8))
-        return fail(SR_ERR_INVALID_ARG, "tuning values: sort_items 8/12/16, resolve_warps 8/16, wind_items 4/8");
+        (t->resolve_warps != 8 && t->resolve_warps != 16) || (t->wind_items != 4 && t->wind_items != 8) ||
+        (t->sort_kind != 0 && t->sort_kind != 1))
+        return fail(SR_ERR_INVALID_ARG,
+                    "tuning values: sort_items 8/12/16, resolve_warps 8/16, wind_items 4/8, sort_kind 0/1");
     return SR_OK;
 }
 
@@ -1730,11 +1765,12 @@ static std::map<std::string, TuneEntry> read_tuning_cache(const char* path) {
         size_t q0 = line.find('"');
         size_t q1 = q0 == std::string::npos ? q0 : line.find('"', q0 + 1);
         if (q1 == std::string::npos || line.find('{', q1) == std::string::npos) continue;
-        double si = 0, rw = 0, wi = 0, ms = 0;
+        double si = 0, rw = 0, wi = 0, sk = 0, ms = 0;
         if (!field(line, "sort_items", &si) || !field(line, "resolve_warps", &rw) || !field(line, "wind_items", &wi))
             continue;
+        field(line, "sort_kind", &sk);
         field(line, "frame_ms", &ms);
-        TuneEntry e{{sizeof(sr_tuning), (int32_t)si, (int32_t)rw, (int32_t)wi}, ms};
+        TuneEntry e{{sizeof(sr_tuning), (int32_t)si, (int32_t)rw, (int32_t)wi, (int32_t)sk}, ms};
         if (check_tuning(&e.t) == SR_OK) m[line.substr(q0 + 1, q1 - q0 - 1)] = e;
     }
     return m;
@@ -1750,9 +1786,10 @@ static sr_status write_tuning_cache(const char* path, const std::map<std::string
         for (const auto& kv : m) {
             char buf[256];
             snprintf(buf, sizeof buf,
-                     "  \"%s\": {\"sort_items\": %d, \"resolve_warps\": %d, \"wind_items\": %d, \"frame_ms\": %.4f}%s\n",
-                     kv.first.c_str(), kv.second.t.sort_items, kv.second.t.resolve_warps, kv.second.t.wind_items,
-                     kv.second.ms, ++i < m.size() ? "," : "");
+                     "  \"%s\": {\"sort_kind\": %d, \"sort_items\": %d, \"resolve_warps\": %d, "
+                     "\"wind_items\": %d, \"frame_ms\": %.4f}%s\n",
+                     kv.first.c_str(), kv.second.t.sort_kind, kv.second.t.sort_items, kv.second.t.resolve_warps,
+                     kv.second.t.wind_items, kv.second.ms, ++i < m.size() ? "," : "");
             out << buf;
         }
         out << "}\n";
@@ -1807,13 +1844,15 @@ sr_status sr_batch_autotune(sr_batch* b, const char* cache_path, int force, sr_t
     sr_tuning best = p.tune;
     float best_ms = 0;
     SR_TRY(time_frames(b, cap, 3, st, &best_ms));
-    const int sort_opts[] = {8, 12, 16}, warp_opts[] = {8, 16}, wind_opts[] = {4, 8};
-    for (int knob = 0; knob < 3; ++knob) {
-        const int* opts = knob == 0 ? sort_opts : knob == 1 ? warp_opts : wind_opts;
-        const int n = knob == 0 ? 3 : 2;
+    const int kind_opts[] = {0, 1}, sort_opts[] = {8, 12, 16}, warp_opts[] = {8, 16}, wind_opts[] = {4, 8};
+    for (int knob = 0; knob < 4; ++knob) {
+        // the radix sort's tile only matters when the radix sort is chosen
+        if (knob == 1 && best.sort_kind == 0) continue;
+        const int* opts = knob == 0 ? kind_opts : knob == 1 ? sort_opts : knob == 2 ? warp_opts : wind_opts;
+        const int n = knob == 1 ? 3 : 2;
         for (int i = 0; i < n; ++i) {
             sr_tuning t = best;
-            int32_t& v = knob == 0 ? t.sort_items : knob == 1 ? t.resolve_warps : t.wind_items;
+            int32_t& v = knob == 0 ? t.sort_kind : knob == 1 ? t.sort_items : knob == 2 ? t.resolve_warps : t.wind_items;
             if (v == opts[i]) continue;
             v = opts[i];
             SR_TRY(sr_batch_set_tuning(b, &t));

@@ -126,6 +126,23 @@ void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t*
                      uint32_t* vals_out, uint32_t* keys_alt, uint32_t* vals_alt, void* scratch,
                      uint32_t* status, cudaStream_t st);
 
+// ---- segsort.cu  (stable sort of path-ordered keys: per-path segments)
+// Tables of the path segments from the curve offsets; max_size > 0 flags a
+// segment larger than that as a capacity overflow.
+size_t segsort_scratch_bytes(uint32_t n_curves);
+// Tile tables of a frame with capacity cap (a second buffer).
+size_t segsort_tile_bytes(uint32_t n_curves, int64_t cap);
+int segsort_tile();
+void launch_segsort_tables(const uint32_t* curve_path, const int32_t* offs, uint32_t n_curves, uint32_t max_size,
+                           void* scratch, uint32_t* status, cudaStream_t st);
+// Device word holding the largest segment of more than half a tile (0 if none).
+const uint32_t* segsort_largest(const void* scratch, uint32_t n_curves);
+// Sorts keys_in[0, N) into keys_out by their key bits (layout L; N from the
+// tables; cap bounds the grid); `levels` merge rounds launched, at least
+// ceil(log2(chunks of the largest segment)).  keys_alt is scratch.
+void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t n_curves,
+                    const KeyLayout& L, int levels, void* scratch, void* tiles, uint32_t* status, cudaStream_t st);
+
 // ---- winding.cu
 struct WindArgs {
     int64_t n;                      // N records: the capacity when n_dev is set

@@ -1,0 +1,530 @@
+// segsort.cu — the fragment sort, using the order the records arrive in.
+//
+// Records are written per curve and curves are grouped by path, so the keys
+// (path | row rank | x, see pack_key) arrive sorted by path: only the records
+// of each path need ordering.  Each path is a segment of the record array.
+//   * Segments of at most kGroup records are packed by where they start: the
+//     segments starting in [g*kGroup, (g+1)*kGroup) form one tile of at most
+//     kTile records, sorted in shared memory by one CTA.
+//   * Larger segments are cut into kTile-record chunks, each sorted the same
+//     way, then merged pairwise (merge path), as many rounds as the segment
+//     needs.
+// Both steps are stable, so the result equals a stable sort of the whole
+// array by key: the order the onesweep radix sort produces.  Keys may carry a
+// payload above the key bits; it moves with its key and takes no part in the
+// order.  Work is handed out through a table of tile descriptors built on
+// the device, one per CTA, so no CTA searches for its work.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sr {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;   // records a CTA sorts or merges
+constexpr int kGroup = kTile / 2;          // largest segment packed into a group tile
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr uint32_t kChunkBit = 1u << 31;   // descriptor .z: a chunk of a large segment
+// Lanes with the same digit: __match_any_sync (tiles hold runs of nearly
+// sorted keys, so a warp sees few distinct digits), or one ballot per bit.
+constexpr bool kMatchAny = true;
+
+// Front tables (depend on the curves only), in the segment scratch buffer.
+struct SegTables {
+    int32_t* flag;         // [C + 2] curve starts a path; then exclusive scan -> segment index
+    uint32_t* seg_start;   // [C + 2] first record of each segment, then N
+    uint64_t* scan_status;
+    uint32_t* ctl;         // [0] scan counter, [1] largest segment of more than kGroup records
+};
+
+// Back tables (depend on the record capacity), in the tile buffer.
+struct TileTables {
+    int32_t* ntiles;       // [C + 2] tiles a segment opens; then exclusive scan -> first tile
+    uint4* desc;           // [max_tiles] {start, segment size, k | rounds << 16 | chunk bit, -}
+    uint32_t* tile_end;    // [max_tiles] end of a group tile (atomic max over its segments)
+    uint64_t* scan_status;
+    uint32_t* ctl;         // [0] scan counter
+};
+
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+size_t scan_area(uint32_t C) { return round256(scan_status_words((int64_t)C + 1) * 8); }
+
+SegTables carve_front(void* base, uint32_t C) {
+    SegTables t;
+    char* b = static_cast<char*>(base);
+    const size_t ws = round256(((size_t)C + 2) * 4);
+    t.flag = reinterpret_cast<int32_t*>(b);
+    b += ws;
+    t.seg_start = reinterpret_cast<uint32_t*>(b);
+    b += ws;
+    t.scan_status = reinterpret_cast<uint64_t*>(b);
+    b += scan_area(C);
+    t.ctl = reinterpret_cast<uint32_t*>(b);
+    return t;
+}
+
+// Tiles of a frame: at most one group tile per kGroup records (a head starts
+// its own group), plus the chunks of large segments (at most one partial
+// chunk per large segment, of which there are fewer than cap / kGroup), and
+// never more than the segments plus cap / kTile.
+size_t max_tiles(uint32_t C, int64_t cap) {
+    const size_t per_tile = (size_t)((cap + kTile - 1) / kTile);
+    return std::min<size_t>((size_t)C + 2 + per_tile, 5 * per_tile + 2);
+}
+
+TileTables carve_back(void* base, uint32_t C, int64_t cap) {
+    TileTables t;
+    char* b = static_cast<char*>(base);
+    const size_t mt = max_tiles(C, cap);
+    t.ntiles = reinterpret_cast<int32_t*>(b);
+    b += round256(((size_t)C + 2) * 4);
+    t.desc = reinterpret_cast<uint4*>(b);
+    b += round256(mt * 16);
+    t.tile_end = reinterpret_cast<uint32_t*>(b);
+    b += round256(mt * 4);
+    t.scan_status = reinterpret_cast<uint64_t*>(b);
+    b += scan_area(C);
+    t.ctl = reinterpret_cast<uint32_t*>(b);
+    return t;
+}
+
+SR_DEV uint32_t n_segments(const SegTables& t, uint32_t C) { return (uint32_t)t.flag[C]; }
+
+// Merge rounds a large segment of `chunks` sorted chunks needs.
+SR_DEV uint32_t rounds_of(uint32_t chunks) {
+    uint32_t r = 0;
+    while ((1u << r) < chunks) ++r;
+    return r;
+}
+}  // namespace
+
+// ---------------------------------------------------------- segment tables
+__global__ void k_seg_flags(const uint32_t* __restrict__ curve_path, uint32_t C, int32_t* __restrict__ flag) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < C) flag[c] = (c == 0 || curve_path[c] != curve_path[c - 1]) ? 1 : 0;
+    else if (c == C) flag[c] = 0;
+}
+
+// seg_start[s] = record offset of the first curve of segment s; seg_start[S] = N.
+__global__ void k_seg_starts(const int32_t* __restrict__ offs, uint32_t C, SegTables t) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const int32_t s = t.flag[c];
+    if (t.flag[c + 1] != s) t.seg_start[s] = (uint32_t)offs[c];   // curve c starts path segment s
+    if (c == C - 1) t.seg_start[n_segments(t, C)] = (uint32_t)offs[C];
+}
+
+// The largest segment of more than kGroup records.  max_size > 0: a segment
+// larger than that is an overflow (the merge rounds of a pre-sized frame
+// cannot take it; the frame is redone with exact sizing, which chooses the
+// rounds, or the radix sort, from the largest segment).
+__global__ void k_seg_largest(uint32_t C, uint32_t max_size, SegTables t, uint32_t* status) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_segments(t, C)) return;
+    const uint32_t size = t.seg_start[s + 1] - t.seg_start[s];
+    if (size > (uint32_t)kGroup) atomicMax(&t.ctl[1], size);
+    if (max_size && size > max_size) set_error(status, ERR_CAPACITY);
+}
+
+// Tiles each segment opens: a large one its chunks, a small one that starts
+// a group (first small segment starting in its group) one tile.
+__global__ void k_seg_ntiles(uint32_t C, SegTables t, TileTables u) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t S = n_segments(t, C);
+    int32_t n = 0;
+    if (s < S) {
+        const uint32_t a = t.seg_start[s], size = t.seg_start[s + 1] - a;
+        if (size > (uint32_t)kGroup) {
+            n = (int32_t)((size + kTile - 1) / kTile);
+        } else {
+            bool head = s == 0;
+            if (!head) {
+                const uint32_t pa = t.seg_start[s - 1];
+                head = a - pa > (uint32_t)kGroup || a / (uint32_t)kGroup != pa / (uint32_t)kGroup;
+            }
+            n = head ? 1 : 0;
+        }
+    }
+    if (s <= C) u.ntiles[s] = n;
+}
+
+// Descriptors: a group tile is opened by its head and stretched to the end
+// of each small segment of the group; a large segment writes its chunks.
+// Tiles past mt exist only in a frame whose records overflowed the capacity
+// (it is redone); they are not written.
+__global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t S = n_segments(t, C);
+    if (s >= S) return;
+    const uint32_t a = t.seg_start[s], size = t.seg_start[s + 1] - a;
+    const int32_t first = u.ntiles[s];
+    const int32_t n = u.ntiles[s + 1] - first;
+    if (size > (uint32_t)kGroup) {
+        const uint32_t rounds = rounds_of((uint32_t)n);
+        for (int32_t k = 0; k < n && (uint32_t)(first + k) < mt; ++k)
+            u.desc[first + k] = make_uint4(a, size, (uint32_t)k | (rounds << 16) | kChunkBit, 0u);
+        return;
+    }
+    // a non-head small segment belongs to the tile opened just before it
+    const int32_t tile = n == 1 ? first : first - 1;
+    if (tile < 0 || (uint32_t)tile >= mt) return;
+    if (n == 1) u.desc[tile] = make_uint4(a, 0u, 0u, 0u);
+    atomicMax(&u.tile_end[tile], a + size);
+}
+
+// ----------------------------------------------------------- local sort ---
+struct LocalSmem {
+    uint64_t buf[2][kTile];
+    uint32_t warp_hist[kWarps][kRadix];
+    uint32_t digit_start[kRadix];
+    uint32_t scan_tmp[kWarps];
+    uint64_t kmin[kWarps], kmax[kWarps];
+};
+
+SR_DEV uint32_t same_digit_lanes(uint32_t d) {
+    if (kMatchAny) return __match_any_sync(0xFFFFFFFFu, d);
+    uint32_t peers = 0xFFFFFFFFu;
+#pragma unroll
+    for (int b = 0; b <= kRadixBits; ++b) {   // 9 bits: digit kRadix marks an empty slot
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+        peers &= ((d >> b) & 1u) ? m : ~m;
+    }
+    return peers;
+}
+
+// Fields of a key: path, row rank, x (payload bits above the key ignored).
+struct KeyFields {
+    uint32_t xb, rb, pb;
+    SR_DEV uint32_t x(uint64_t k) const { return (uint32_t)(k & ((1ull << xb) - 1)); }
+    SR_DEV uint32_t r(uint64_t k) const { return (uint32_t)((k >> xb) & ((1ull << rb) - 1)); }
+    SR_DEV uint32_t p(uint64_t k) const { return (uint32_t)((k >> (xb + rb)) & ((1ull << pb) - 1)); }
+};
+
+SR_DEV uint32_t block_min_max(uint32_t v, bool is_max, uint32_t* red) {
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const uint32_t u = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        v = is_max ? max(v, u) : min(v, u);
+    }
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    v = red[0];
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) v = is_max ? max(v, red[w]) : min(v, red[w]);
+    __syncthreads();
+    return v;
+}
+
+// CTA b sorts tile b (a group of small segments, or a chunk of a large one).
+// Within a tile the order is that of a compact local key, the mixed-radix
+// number (path - pmin, rank - rmin, x - xmin) over the tile's ranges, which
+// usually needs 2-3 digit passes where the whole key needs 4-6.
+__global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __restrict__ keys_in,
+                                                            uint64_t* __restrict__ keys_out,
+                                                            uint64_t* __restrict__ keys_alt, uint32_t C,
+                                                            KeyFields kf, uint32_t n_cap, TileTables u) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LocalSmem& S = *reinterpret_cast<LocalSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    if ((int32_t)blockIdx.x >= u.ntiles[C]) return;
+    const uint4 d = u.desc[blockIdx.x];
+    uint32_t a, e;
+    bool to_alt = false;
+    if (d.z & kChunkBit) {
+        const uint32_t k = d.z & 0xFFFFu, rounds = (d.z >> 16) & 0x7FFFu;
+        a = d.x + k * (uint32_t)kTile;
+        e = min(a + (uint32_t)kTile, d.x + d.y);
+        to_alt = (rounds & 1u) != 0;   // the segment's last merge round lands in keys_out
+    } else {
+        a = d.x;
+        e = u.tile_end[blockIdx.x];
+    }
+    // a frame whose records overflowed the buffers is redone: never read past them
+    a = min(a, n_cap);
+    e = min(max(e, a), n_cap);
+    const uint32_t len = e - a;
+    if (len == 0) return;
+    uint64_t* dst = to_alt ? keys_alt : keys_out;
+
+    // load (coalesced); ranges of the key fields and of the whole key
+    const uint64_t kmask = (1ull << (kf.xb + kf.rb + kf.pb)) - 1ull;
+    uint32_t pmin = ~0u, pmax = 0, rmin = ~0u, rmax = 0, xmin = ~0u, xmax = 0;
+    uint64_t lo = ~0ull, hi = 0;
+    for (uint32_t j = tid; j < len; j += kThreads) {
+        const uint64_t k = keys_in[a + j];
+        S.buf[0][j] = k;
+        pmin = min(pmin, kf.p(k)); pmax = max(pmax, kf.p(k));
+        rmin = min(rmin, kf.r(k)); rmax = max(rmax, kf.r(k));
+        xmin = min(xmin, kf.x(k)); xmax = max(xmax, kf.x(k));
+        lo = min(lo, k & kmask);
+        hi = max(hi, k & kmask);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+    }
+    if (lane == 0) {
+        S.kmin[warp] = lo;
+        S.kmax[warp] = hi;
+    }
+    uint32_t* red = S.scan_tmp;
+    pmin = block_min_max(pmin, false, red); pmax = block_min_max(pmax, true, red);
+    rmin = block_min_max(rmin, false, red); rmax = block_min_max(rmax, true, red);
+    xmin = block_min_max(xmin, false, red); xmax = block_min_max(xmax, true, red);
+    lo = S.kmin[0];
+    hi = S.kmax[0];
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) {
+        lo = min(lo, S.kmin[w]);
+        hi = max(hi, S.kmax[w]);
+    }
+    const uint64_t Rx = (uint64_t)(xmax - xmin) + 1, Rr = (uint64_t)(rmax - rmin) + 1, Rp = (uint64_t)(pmax - pmin) + 1;
+    // the compact key when the product of the ranges fits 32 bits; else the
+    // bits where the tile's keys differ
+    const bool fits = Rp * Rr <= 0xFFFFFFFFull && Rp * Rr * Rx <= 0x100000000ull;
+    const uint64_t span = fits ? Rp * Rr * Rx : 0;
+    const uint32_t bits = fits ? (span <= 1 ? 0u : 64u - (uint32_t)__clzll((long long)(span - 1)))
+                               : (lo == hi ? 0u : 64u - (uint32_t)__clzll((long long)(lo ^ hi)));
+    const uint32_t passes = (bits + kRadixBits - 1) / kRadixBits;
+    const uint32_t rr = (uint32_t)Rr, rx = (uint32_t)Rx;
+    auto digit = [&](uint64_t k, uint32_t shift) -> uint32_t {
+        if (fits) return ((((kf.p(k) - pmin) * rr + (kf.r(k) - rmin)) * rx + (kf.x(k) - xmin)) >> shift) & (kRadix - 1);
+        return (uint32_t)((k & kmask) >> shift) & (kRadix - 1);
+    };
+
+    int cur = 0;
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        const uint32_t shift = pass * kRadixBits;
+        for (int i = tid; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
+        __syncthreads();
+        // rank within the warp: warp w holds slots [w*512, w*512 + 512)
+        uint64_t k[kItems];
+        uint32_t rank[kItems], dig[kItems];
+#pragma unroll
+        for (int it = 0; it < kItems; ++it) {
+            const uint32_t j = warp * (32 * kItems) + it * 32 + lane;
+            const bool ok = j < len;
+            k[it] = ok ? S.buf[cur][j] : 0ull;
+            const uint32_t dg = ok ? digit(k[it], shift) : (uint32_t)kRadix;
+            dig[it] = dg;
+            const uint32_t peers = same_digit_lanes(dg);
+            const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+            uint32_t before = 0;
+            if (ok && lane == leader) {
+                before = S.warp_hist[warp][dg];
+                S.warp_hist[warp][dg] = before + (uint32_t)__popc(peers);
+            }
+            before = __shfl_sync(0xFFFFFFFFu, before, leader);
+            rank[it] = before + (uint32_t)__popc(peers & lanemask_lt());
+            __syncwarp();
+        }
+        __syncthreads();
+        // per digit: exclusive over warps, then over digits
+        const uint32_t dd = tid;   // kThreads == kRadix
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = S.warp_hist[w][dd];
+            S.warp_hist[w][dd] = cnt;
+            cnt += c;
+        }
+        uint32_t x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if ((int)lane >= o) x += y;
+        }
+        if (lane == 31) S.scan_tmp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = lane < kWarps ? S.scan_tmp[lane] : 0u;
+            uint32_t wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+                if ((int)lane >= o) wi += y;
+            }
+            if (lane < kWarps) S.scan_tmp[lane] = wi - w;
+        }
+        __syncthreads();
+        S.digit_start[dd] = S.scan_tmp[warp] + x - cnt;
+        __syncthreads();
+        // scatter into the other buffer (stable: digit, then warp, then slot)
+#pragma unroll
+        for (int it = 0; it < kItems; ++it) {
+            const uint32_t j = warp * (32 * kItems) + it * 32 + lane;
+            if (j < len) S.buf[cur ^ 1][S.digit_start[dig[it]] + S.warp_hist[warp][dig[it]] + rank[it]] = k[it];
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[cur][j];
+}
+
+// ---------------------------------------------------------------- merge ---
+// Round `level` of the merge of large segments: runs of width
+// W = kTile << level, pairs merged stably (A before B on equal keys).  The
+// CTA of a chunk writes that chunk's output range.  A segment needing r
+// rounds has its chunks sorted into keys_out (r even) or keys_alt (r odd),
+// and each round flips buffer, so its last round lands in keys_out; rounds
+// past r do nothing for it.
+struct MergeSmem {
+    uint64_t in[kTile];    // A part then B part of this chunk
+    uint64_t out[kTile];
+    uint32_t split[4];
+};
+
+SR_DEV uint32_t merge_split(const uint64_t* A, uint32_t na, const uint64_t* B, uint32_t nb, uint32_t d, uint64_t kmask) {
+    // number of A elements among the first d outputs
+    uint32_t lo = d > nb ? d - nb : 0u, hi = min(d, na);
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if ((A[mid] & kmask) <= (B[d - 1 - mid] & kmask)) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The same split found by a whole warp: 32 probes per step.
+SR_DEV uint32_t warp_merge_split(const uint64_t* A, uint32_t na, const uint64_t* B, uint32_t nb, uint32_t d,
+                                 uint64_t kmask) {
+    const uint32_t lane = lane_id();
+    uint32_t lo = d > nb ? d - nb : 0u, hi = min(d, na);
+    while (lo < hi) {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t m = lo + lane * step;
+        const bool valid = m < hi;
+        const bool take_a = valid && (A[m] & kmask) <= (B[d - 1 - m] & kmask);
+        const uint32_t ta = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, take_a));
+        const uint32_t tv = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, valid));
+        // the predicate holds for the first ta probes and fails from probe ta on
+        const uint32_t new_lo = ta == 0 ? lo : lo + (ta - 1) * step + 1;
+        const uint32_t new_hi = ta < tv ? lo + ta * step : hi;
+        lo = new_lo;
+        hi = new_hi;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__ keys_out,
+                                                          uint64_t* __restrict__ keys_alt, uint32_t C, uint32_t level,
+                                                          uint32_t key_bits, uint32_t n_cap, TileTables u) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MergeSmem& S = *reinterpret_cast<MergeSmem*>(smem_raw);
+    if ((int32_t)blockIdx.x >= u.ntiles[C]) return;
+    const uint4 desc = u.desc[blockIdx.x];
+    if (!(desc.z & kChunkBit)) return;
+    const uint32_t k = desc.z & 0xFFFFu, rounds = (desc.z >> 16) & 0x7FFFu;
+    if (level >= rounds) return;
+    const uint64_t* src = ((rounds - level) & 1u) ? keys_alt : keys_out;
+    uint64_t* dst = ((rounds - level) & 1u) ? keys_out : keys_alt;
+    const uint32_t s0 = desc.x, size = desc.y;
+    if ((uint64_t)s0 + size > n_cap) return;   // overflowed frame: redone
+    const uint32_t o0 = k * (uint32_t)kTile, o1 = min(o0 + (uint32_t)kTile, size);
+    const uint32_t W = (uint32_t)kTile << level;
+    const uint32_t p0 = (o0 / (2 * W)) * (2 * W);
+    const uint32_t na = min(W, size - p0);
+    const uint32_t nb = size - p0 > W ? min(W, size - p0 - W) : 0u;
+    const uint64_t* A = src + s0 + p0;
+    const uint64_t* B = A + na;
+    const uint32_t tid = threadIdx.x;
+    if (nb == 0) {   // a lone run: already in order
+        for (uint32_t j = o0 + tid; j < o1; j += kThreads) dst[s0 + j] = src[s0 + j];
+        return;
+    }
+    const uint64_t kmask = (1ull << key_bits) - 1ull;
+    const uint32_t d0 = o0 - p0, d1 = o1 - p0;
+    const uint32_t warp = tid >> 5;
+    if (warp < 2) {
+        const uint32_t sp = warp_merge_split(A, na, B, nb, warp == 0 ? d0 : d1, kmask);
+        if (lane_id() == 0) S.split[warp] = sp;
+    }
+    __syncthreads();
+    const uint32_t ia0 = S.split[0], ia1 = S.split[1];
+    const uint32_t ib0 = d0 - ia0, ib1 = d1 - ia1;
+    const uint32_t nA = ia1 - ia0, nB = ib1 - ib0, n = d1 - d0;
+    for (uint32_t j = tid; j < nA; j += kThreads) S.in[j] = A[ia0 + j];
+    for (uint32_t j = tid; j < nB; j += kThreads) S.in[nA + j] = B[ib0 + j];
+    __syncthreads();
+    // each thread merges kItems outputs from its own split
+    const uint32_t dt = min(tid * (uint32_t)kItems, n);
+    const uint64_t* sA = S.in;
+    const uint64_t* sB = S.in + nA;
+    uint32_t ia = merge_split(sA, nA, sB, nB, dt, kmask);
+    uint32_t ib = dt - ia;
+    const uint32_t e = min(dt + (uint32_t)kItems, n);
+    for (uint32_t o = dt; o < e; ++o) {
+        const bool takeA = ib >= nB || (ia < nA && (sA[ia] & kmask) <= (sB[ib] & kmask));
+        S.out[o] = takeA ? sA[ia++] : sB[ib++];
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < n; j += kThreads) dst[s0 + o0 + j] = S.out[j];
+}
+
+// ------------------------------------------------------------- launches --
+size_t segsort_scratch_bytes(uint32_t C) { return 2 * round256(((size_t)C + 2) * 4) + scan_area(C) + 256; }
+
+size_t segsort_tile_bytes(uint32_t C, int64_t cap) {
+    const size_t mt = max_tiles(C, cap);
+    return round256(((size_t)C + 2) * 4) + round256(mt * 16) + round256(mt * 4) + scan_area(C) + 256;
+}
+
+int segsort_tile() { return kTile; }
+
+void launch_segsort_tables(const uint32_t* curve_path, const int32_t* offs, uint32_t C, uint32_t max_size,
+                           void* scratch, uint32_t* status, cudaStream_t st) {
+    if (C == 0) return;
+    SegTables t = carve_front(scratch, C);
+    cudaMemsetAsync(t.scan_status, 0, scan_area(C), st);
+    cudaMemsetAsync(t.ctl, 0, 256, st);
+    const unsigned g = (C + 1 + 255) / 256;
+    count_launches(3);
+    k_seg_flags<<<g, 256, 0, st>>>(curve_path, C, t.flag);
+    launch_exclusive_scan_i32(t.flag, t.flag, C + 1, t.scan_status, t.ctl + 0, status, st);
+    k_seg_starts<<<g, 256, 0, st>>>(offs, C, t);
+    k_seg_largest<<<g, 256, 0, st>>>(C, max_size, t, status);
+}
+
+const uint32_t* segsort_largest(const void* scratch, uint32_t C) {
+    return carve_front(const_cast<void*>(scratch), C).ctl + 1;
+}
+
+void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t C,
+                    const KeyLayout& L, int levels, void* scratch, void* tiles, uint32_t* status,
+                    cudaStream_t st) {
+    if (cap <= 0 || C == 0) return;
+    SegTables t = carve_front(scratch, C);
+    TileTables u = carve_back(tiles, C, cap);
+    const size_t mt = max_tiles(C, cap);
+    cudaMemsetAsync(u.tile_end, 0, mt * 4, st);
+    cudaMemsetAsync(u.scan_status, 0, scan_area(C), st);
+    cudaMemsetAsync(u.ctl, 0, 256, st);
+    const unsigned g = (C + 1 + 255) / 256;
+    count_launches(2);
+    k_seg_ntiles<<<g, 256, 0, st>>>(C, t, u);
+    launch_exclusive_scan_i32(u.ntiles, u.ntiles, C + 1, u.scan_status, u.ctl + 0, status, st);
+    k_seg_desc<<<g, 256, 0, st>>>(C, (uint32_t)mt, t, u);
+    const uint32_t key_bits = L.pbits + L.rbits + L.xbits;
+    const KeyFields kf{L.xbits, L.rbits, L.pbits};
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_local_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LocalSmem));
+        cudaFuncSetAttribute(k_merge_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
+        attr = true;
+    }
+    count_launches(1 + (uint32_t)levels);
+    const uint32_t n_cap = (uint32_t)cap;
+    k_local_sort<<<(unsigned)mt, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap, u);
+    for (int lv = 0; lv < levels; ++lv)
+        k_merge_level<<<(unsigned)mt, kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, C, (uint32_t)lv, key_bits,
+                                                                         n_cap, u);
+}
+
+}  // namespace sr

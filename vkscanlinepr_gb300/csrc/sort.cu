@@ -32,10 +32,11 @@ constexpr int kMaxPasses = 8;
 constexpr int kHistBlocks = 608;   // 152 SMs x 4
 constexpr int kLookWindow = 8;     // look-back words read per step
 // Lanes holding the same digit: one __match_any_sync, or one ballot per
-// digit bit (9 bits: digit 256 marks an empty slot).
-constexpr bool kMatchAny = false;
-
-SR_DEV uint32_t same_digit_lanes(uint32_t d) {
+// digit bit (9 bits: digit 256 marks an empty slot).  The 64-bit fragment
+// keys are ranked by ballots (their low digits vary a lot within a warp);
+// the 32-bit keys (draw rows, chain classes) arrive in runs, where one
+// match is cheaper.
+template <bool kMatchAny> SR_DEV uint32_t same_digit_lanes(uint32_t d) {
     if (kMatchAny) return __match_any_sync(0xFFFFFFFFu, d);
     uint32_t peers = 0xFFFFFFFFu;
 #pragma unroll
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(kThreads, onesweep_min_blocks(kVals, ITEMS)) k
         int64_t idx = wbase + it * 32 + lane;
         bool ok = idx < n;
         uint32_t d = ok ? digit_of(k[it], shift, dmask) : (uint32_t)kRadix;   // kRadix = out of range
-        uint32_t peers = same_digit_lanes(d);
+        uint32_t peers = same_digit_lanes<sizeof(K) == 4>(d);
         uint32_t leader = (uint32_t)(__ffs(peers) - 1);
         uint32_t before = 0;
         if (ok && lane == leader) {
