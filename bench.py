@@ -41,6 +41,14 @@ WORKLOADS = {
     "mixed2048": (1, 1, 2048, 2048, 5000),
 }
 L2_FLUSH_BYTES = 256 << 20
+# What bounds each stage's main kernel (profiles/ncu_top_kernels_frame4096.md):
+# the HBM fraction is the roofline only for the stages that move bytes.
+LIMITS = {
+    "resolve": "FP32 instruction issue: 6.9 G pixel-blends x 9 FP32 ops, issue 80% busy, DRAM 1%",
+    "chains": "the dependent bisection steps of the longest crossing chains",
+    "sort": "shared-memory ranking latency of the tile sort and merge rounds",
+    "winding_emit": "instruction issue and two chained look-backs, DRAM 11%",
+}
 STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
                "row_sort", "resolve"]
 
@@ -663,7 +671,8 @@ def main():
     achieved = sb[dom] / (stage_ms[dom] * 1e6)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                 "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic}
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "limited_by": LIMITS.get(dom, "")}
 
     line = {"metric": metric_name(args.workload),
             "value": round(value, 4), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
