@@ -64,6 +64,8 @@ def parse_args():
     ap.add_argument("--batch-scenes", type=int, default=4096,
                     help="scenes of the batched workload (0 skips it)")
     ap.add_argument("--batch-size", type=int, default=512, help="scenes per resident batch")
+    ap.add_argument("--batch-streams", type=int, default=3,
+                    help="streams the resident batches' frames are spread over (frames in flight)")
     ap.add_argument("--plain-scenes", type=int, default=512,
                     help="scenes the plain per-scene renderer is timed on")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-sizing configuration")
@@ -72,6 +74,9 @@ def parse_args():
                     help="scenes per batch in the learned-vs-exact sizing stream")
     ap.add_argument("--serve-requests", type=int, default=2048, help="requests of the serving configuration")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-overload", type=float, default=8000.0,
+                    help="a second arrival rate above the plain renderer's capacity (0 skips it)")
+    ap.add_argument("--serve-batch", type=int, default=256, help="largest batch the server forms")
     return ap.parse_args()
 
 
@@ -239,11 +244,21 @@ def run_batched(sr, args, sptr, steps):
         records += st["n_intersections"]
     for b, c in zip(batches, caps):
         b.render(capacity=c, graph=True, stream=sptr)   # capture
+    # the batches' frames are independent: spread them over a few streams so
+    # one frame's tail (its longest bisection chains) overlaps the next ones
+    import ctypes as _ct
+    import torch
+    nst = max(1, args.batch_streams)
+    streams = [torch.cuda.Stream() for _ in range(nst)]
+    sps = [_ct.c_void_p(x.cuda_stream) for x in streams]
+    torch.cuda.synchronize()
     times = []
     for _ in range(steps):
         t1 = time.perf_counter()
-        for b, c in zip(batches, caps):
-            b.render(capacity=c, graph=True, stream=sptr)
+        for i, (b, c) in enumerate(zip(batches, caps)):
+            b.enqueue(c, graph=True, stream=sps[i % nst])
+        for b in batches:
+            b.finish()
         times.append(time.perf_counter() - t1)
     overflows = sum(b.stats()["overflows"] for b in batches)
     batched_sps = total / (sum(times) / len(times))
@@ -287,6 +302,7 @@ def run_batched(sr, args, sptr, steps):
     return learned, serving, {"scenes": total, "records": int(records), "resident_batches": n_resident,
             "scenes_per_s": round(batched_sps, 1), "ms_per_batch_of_all": round(1000 * sum(times) / len(times), 2),
             "sizing": "record capacity from the previous exact frame, frame replayed as a CUDA graph",
+            "streams": nst,
             "overflows": int(overflows), "plain_scenes_per_s": round(plain_sps, 1),
             "plain_sample": nplain, "speedup_vs_plain": round(batched_sps / plain_sps, 2),
             "bit_exact_vs_plain": "%d/%d" % (exact, checked), "build_s": round(build_s, 2),
@@ -487,13 +503,18 @@ def run_serving(sr, args, sz, margins):
     arrivals = list(np.cumsum(rng.exponential(1.0 / args.serve_rate, n)))
     out = {"requests": n, "rate_per_s": args.serve_rate, "scene_pool": len(pool), "budget_bytes": int(120e9)}
     for name, sizer, slots in (("learned", sz, 3), ("exact", None, 1)):
-        srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=64, memory_budget=120e9, margins=margins)
+        srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=args.serve_batch, memory_budget=120e9,
+                              margins=margins)
         _serve(sr, srv, pool[:64], [None] * 64)                      # warm the slots' buffers
         t, imgs = _serve(sr, srv, pool, arrivals, check_every=64 if name == "learned" else 0)
         res = _lat_summary(t[:, 0], t[:, 1])
         res["mean_batch"] = round(float(t[:, 2].mean()), 1)
         ts, _ = _serve(sr, srv, pool, [None] * n)                     # saturation: all at once
         res["saturated_scenes_per_s"] = _lat_summary(ts[:, 0], ts[:, 1])["scenes_per_s"]
+        if args.serve_overload > 0:
+            over = list(np.cumsum(np.random.default_rng(5).exponential(1.0 / args.serve_overload, n)))
+            to, _ = _serve(sr, srv, pool, over)
+            res["at_%d_per_s" % int(args.serve_overload)] = _lat_summary(to[:, 0], to[:, 1])
         st = srv.stats()
         res.update({"batches": int(st["batches"]), "overflows": int(st["overflows"]),
                     "refits": int(st["refits"]), "peak_bytes": int(st["peak_bytes"])})
