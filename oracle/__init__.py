@@ -1,7 +1,8 @@
 """CPU restatement of the VkScanlinePR scanline pipeline — test infrastructure.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-package, as the checker.  The renderer (vkscanlinepr_gb300) never imports it.
+package, to check the renderer's output.  The renderer (vkscanlinepr_gb300)
+never imports it.
 
 Parity status: unpinned by reference outputs (the reference has no tests and
 cannot run here); pinned by hand-computed known-answer scenes and by the

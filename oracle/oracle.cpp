@@ -1,7 +1,7 @@
 // oracle.cpp — CPU restatement of the VkScanlinePR scanline pipeline.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker: tests/, the smoke
-// check and bench.py's CPU-baseline leg load it; the renderer never does.
+// TEST INFRASTRUCTURE ONLY.  It checks the renderer's output: tests/, the
+// smoke check and bench.py's CPU-baseline leg load it; the renderer never does.
 //
 // Parity status: UNPINNED by the reference's own outputs.  The reference has
 // no tests, no golden images and no CPU path, and it cannot be built or run
