@@ -119,6 +119,22 @@ def degenerate(w=32, h=32):
     return b.arrays()
 
 
+def long_chains(w=2400, h=2400):
+    """Curves crossing more than 1024 grid lines of one axis in one monotone
+    piece (in both modes), which the renderer solves a warp per chain."""
+    b = Builder(w, h)
+    b.path(0, RED)
+    b.curve(CUBIC, [(15.3, 30.7), (800.2, 700.9), (1600.5, 1500.1), (2380.6, 2210.4)])
+    b.curve(CUBIC, [(2380.6, 2210.4), (2300.0, 400.0), (600.0, 100.0), (15.3, 30.7)])
+    b.path(1, BLUE)
+    b.curve(QUADRIC, [(5.5, 2390.2), (1200.3, 1190.7), (2395.1, 12.8)])
+    b.curve(LINE, [(2395.1, 12.8), (5.5, 2390.2)])
+    b.path(0, (0, 200, 0, 180))
+    b.curve(CUBIC, [(10.0, 1200.0), (800.0, -900.0), (1600.0, 3300.0), (2390.0, 1210.0)])
+    b.curve(LINE, [(2390.0, 1210.0), (10.0, 1200.0)])
+    return b.arrays()
+
+
 ALL = {
     "square": square,
     "star_nonzero": lambda: star(rule=0),
@@ -127,4 +143,5 @@ ALL = {
     "mixed_curves": mixed_curves,
     "offcanvas": offcanvas,
     "degenerate": degenerate,
+    "long_chains": long_chains,
 }

@@ -105,6 +105,7 @@ enum Ctl : int {
     CTL_CHAINS = 4,    // chain counter
     CTL_LONG = 8,      // long-piece counter
     CTL_QUEUE = 9,     // chain work-queue counter
+    CTL_WIDE = 10,     // chains solved by a whole warp
     CTL_WORDS = 16,
 };
 
@@ -430,6 +431,7 @@ struct Pipeline {
         cw.list_cap = lc;
         cw.chain_count = ctlp + CTL_CHAINS;
         cw.chain_queue = ctlp + CTL_QUEUE;
+        cw.wide_count = ctlp + CTL_WIDE;
         cw.long_list = long_list.as<uint32_t>();
         cw.long_count = ctlp + CTL_LONG;
         return cw;

@@ -137,14 +137,20 @@ SR_DEV int32_t piece_ny(uint32_t n) { return (int32_t)((n >> 16) & 0x7FFFu); }
 
 // Sort key of a chain: longest length class first (so the longest dependency
 // chains start in the first wave of k_chains), then cubic, quadric, line, so
-// that a warp runs one curve type with lengths within a factor of 2.
+// that a warp runs one curve type with lengths within a factor of 2.  A line
+// root is a closed form, about 2^5 times cheaper than a 24-step bisection, so
+// a line chain is classed 5 length classes lower.
 SR_DEV uint32_t chain_key(int32_t len, uint32_t type) {
     uint32_t lg = 31u - (uint32_t)__clz(len);
     if (lg > 14u) lg = 14u;
+    if (type != 3u && type != 4u) lg = lg > 5u ? lg - 5u : 0u;
     uint32_t cls = type == 4u ? 0u : (type == 3u ? 1u : 2u);
     return ((14u - lg) << 2) | cls;
 }
 SR_DEV bool chain_key_long(uint32_t key) { return (key >> 2) <= 14u - 5u; }   // >= 32 crossings
+// Chains of >= 1024 bisected roots are solved by a whole warp each
+// (run_chain_warp); they sort before every other chain.
+SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 10u; }
 constexpr uint32_t kChainKeyBits = 6;
 
 // get_xy_begin_end_delta + udpate_cut_range for one axis
@@ -176,6 +182,7 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
                                                int32_t* __restrict__ count, uint4* __restrict__ pieces,
                                                uint32_t* __restrict__ chain_items, uint32_t* __restrict__ chain_keys,
                                                uint32_t list_cap, uint32_t* __restrict__ chain_count,
+                                               uint32_t* __restrict__ wide_count,
                                                uint32_t* __restrict__ long_list, uint32_t* __restrict__ long_count,
                                                uint32_t* __restrict__ status) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -327,7 +334,11 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
         if (!m) break;
         uint32_t leader = (uint32_t)(__ffs(m) - 1);
         uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(chain_count, (uint32_t)__popc(m));
+        const uint32_t wm = __ballot_sync(0xFFFFFFFFu, has && chain_key_wide(my_key[k]));
+        if (lane == leader) {
+            base = atomicAdd(chain_count, (uint32_t)__popc(m));
+            if (wm) atomicAdd(wide_count, (uint32_t)__popc(wm));
+        }
         base = __shfl_sync(0xFFFFFFFFu, base, leader);
         if (has) {
             uint32_t slot = base + (uint32_t)__popc(m & lanemask_lt());
@@ -362,10 +373,15 @@ template <int kType> SR_DEV float eval_axis(const AxisPoly& a, float t) {
     return __fadd_rn(l0, __fmul_rn(t, __fsub_rn(l1, l0)));
 }
 
-// (bits(a - c) ^ bits(b - c)) >= 0 of make_intersection_1.comp:421: for
-// finite values a - c is negative exactly when a < c (x - x is +0), so the
-// test is a pair of compares.
-SR_DEV bool same_sign(float a, float c, float b) { return (a < c) == (b < c); }
+SR_DEV float mid_rn(float lo, float hi) { return __fmul_rn(__fadd_rn(lo, hi), 0.5f); }
+
+// The step test of make_intersection_1.comp:421 is
+// (bits(v - c) ^ bits(v_lo - c)) >= 0, v_lo the value at the interval's low
+// end; for finite values v - c is negative exactly when v < c (x - x is +0).
+// The low end moves only to a midpoint that passes the test, i.e. one on the
+// same side of c, so the side s0 = (value at t_min < c) holds for the whole
+// solve: a step goes right exactly when (v < c) == s0, whatever the other
+// steps did.  Both solvers below rest on that.
 
 // 24-step bisection of the reference (make_intersection_1.comp:402-434).
 // kSpec evaluates both possible next midpoints with the current one, so
@@ -373,46 +389,40 @@ SR_DEV bool same_sign(float a, float c, float b) { return (a < c) == (b < c); }
 // are exactly those of the one-step loop.
 template <int kType, bool kSpec>
 SR_DEV float bisect(const AxisPoly& a, float c, float t_min, float t_max) {
+    const float v0 = eval_axis<kType>(a, t_min);
+    const bool s0 = v0 < c;
     float ta = t_min, tb = t_max;
-    float vt0 = eval_axis<kType>(a, ta);
-    float t_solve = ta;
-    if (vt0 == c) return t_solve;
-    float last = 0.0f;
+    float t_solve = t_min, last = 0.0f;
     if (kSpec) {
 #pragma unroll 2
         for (int j = 0; j < 12; ++j) {
-            float tm = __fmul_rn(__fadd_rn(ta, tb), 0.5f);
-            float mL = __fmul_rn(__fadd_rn(ta, tm), 0.5f);
-            float mR = __fmul_rn(__fadd_rn(tm, tb), 0.5f);
-            float v = eval_axis<kType>(a, tm);
-            float vL = eval_axis<kType>(a, mL);
-            float vR = eval_axis<kType>(a, mR);
-            bool r1 = same_sign(v, c, vt0);
-            float ta1 = r1 ? tm : ta, tb1 = r1 ? tb : tm, vt1 = r1 ? v : vt0;
-            float m2 = r1 ? mR : mL, v2 = r1 ? vR : vL;
-            bool r2 = same_sign(v2, c, vt1);
-            ta = r2 ? m2 : ta1;
-            tb = r2 ? tb1 : m2;
-            vt0 = r2 ? v2 : vt1;
-            t_solve = m2;
-            last = v2;
+            const float tm = mid_rn(ta, tb);
+            const float mL = mid_rn(ta, tm), mR = mid_rn(tm, tb);
+            const float v = eval_axis<kType>(a, tm);
+            const float vL = eval_axis<kType>(a, mL);
+            const float vR = eval_axis<kType>(a, mR);
+            const bool r1 = (v < c) == s0, rL = (vL < c) == s0, rR = (vR < c) == s0;
+            t_solve = r1 ? mR : mL;
+            last = r1 ? vR : vL;
+            const float na = r1 ? (rR ? mR : tm) : (rL ? mL : ta);
+            const float nb = r1 ? (rR ? tb : mR) : (rL ? tm : mL);
+            ta = na;
+            tb = nb;
         }
     } else {
 #pragma unroll 4
         for (int j = 0; j < 24; ++j) {
-            float tm = __fmul_rn(__fadd_rn(ta, tb), 0.5f);
-            float v = eval_axis<kType>(a, tm);
+            const float tm = mid_rn(ta, tb);
+            const float v = eval_axis<kType>(a, tm);
             t_solve = tm;
             last = v;
-            if (same_sign(v, c, vt0)) {
-                ta = tm;
-                vt0 = v;
-            } else {
-                tb = tm;
-            }
+            if ((v < c) == s0) ta = tm;
+            else tb = tm;
         }
     }
-    if (fabsf(__fsub_rn(last, c)) > 1.0f) t_solve = t_min;
+    // vt0 == c returns t_min at once; a solve that ends more than one unit
+    // away from c falls back to t_min too
+    if (v0 == c || fabsf(__fsub_rn(last, c)) > 1.0f) t_solve = t_min;
     return t_solve;
 }
 
@@ -437,61 +447,200 @@ SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t
     }
 }
 
+// Warp-cooperative solve of one long chain.  By the invariant above, the 31
+// midpoints of the next five bisection steps can be evaluated at once: lane
+// l holds node l+1 of the complete binary tree of those steps in heap order
+// (node n's children are 2n and 2n+1, the right child taken when the step
+// goes right), and one ballot of the (v < c) bits gives every node's turn.
+// The leaf whose ancestors all turn toward it is on the path; it hands the
+// new interval to the warp.  Lane 31 evaluates the root's t_min in the first
+// round, which gives s0 in the same ballot.  24 steps = four 5-level rounds
+// and a last 4-level round, whose leaf midpoint is the 24th midpoint.
+struct TreeLane {
+    uint32_t dirs;    // bit j-1: turn at level j toward this lane's node
+    int32_t depth;    // node depth (lane 31: -1)
+    uint32_t anc5, want5, anc4, want4;   // path masks of the leaves of a 5- and a 4-level round
+};
+
+SR_DEV TreeLane tree_lane(uint32_t lane) {
+    TreeLane tl;
+    const uint32_t n = lane + 1u;
+    const int32_t d = lane == 31u ? -1 : 31 - __clz((int32_t)n);
+    tl.depth = d;
+    tl.dirs = 0;
+    for (int32_t j = 1; j <= d; ++j) tl.dirs |= ((n >> (d - j)) & 1u) << (j - 1);
+    tl.anc5 = tl.want5 = tl.anc4 = tl.want4 = 0;
+    for (int32_t i = 0; i < d; ++i) {   // ancestor at depth i and the turn it takes toward n
+        const uint32_t anc = n >> (d - i), dir = (n >> (d - i - 1)) & 1u;
+        const uint32_t bit = 1u << (anc - 1u);
+        if (d == 4) { tl.anc5 |= bit; tl.want5 |= dir ? bit : 0u; }
+        if (d == 3) { tl.anc4 |= bit; tl.want4 |= dir ? bit : 0u; }
+    }
+    return tl;
+}
+
+// One round of kLevels bisection steps from [ta, tb].  Returns the chosen
+// leaf's lane; its node's midpoint, value and interval are in mine/v/lb/rb.
+template <int kType, int kLevels>
+SR_DEV uint32_t tree_round(const AxisPoly& a, float c, float ta, float tb, float t_eval, const TreeLane& tl,
+                           bool& s0, bool first, float& mine, float& v, float& mlb, float& mrb) {
+    // midpoints along this lane's path: m_j = (m_{j-1} + the interval's other
+    // end) * 0.5, the other end being older than m_{j-1}
+    float lb = ta, rb = tb, m = mid_rn(ta, tb);
+    mine = m;
+    mlb = lb;
+    mrb = rb;
+#pragma unroll
+    for (int j = 1; j < kLevels; ++j) {
+        const bool dir = (tl.dirs >> (j - 1)) & 1u;
+        const float other = dir ? rb : lb;
+        lb = dir ? m : lb;
+        rb = dir ? rb : m;
+        m = __fmul_rn(__fadd_rn(m, other), 0.5f);
+        if (j == tl.depth) {
+            mine = m;
+            mlb = lb;
+            mrb = rb;
+        }
+    }
+    if (tl.depth < 0) mine = t_eval;   // lane 31: the root's t_min (used in the first round)
+    v = eval_axis<kType>(a, mine);
+    const uint32_t B = __ballot_sync(0xFFFFFFFFu, v < c);
+    if (first) s0 = (B >> 31) & 1u;
+    const uint32_t R = s0 ? B : ~B;   // bit l: node l+1 goes right
+    const bool leaf = tl.depth == kLevels - 1;
+    const uint32_t anc = kLevels == 5 ? tl.anc5 : tl.anc4, want = kLevels == 5 ? tl.want5 : tl.want4;
+    const uint32_t on = __ballot_sync(0xFFFFFFFFu, leaf && ((R ^ want) & anc) == 0u);
+    return (uint32_t)(__ffs(on) - 1);
+}
+
+template <int kType>
+SR_DEV float bisect_warp(const AxisPoly& a, float c, float t_min, float t_max, const TreeLane& tl) {
+    bool s0 = false;
+    float ta = t_min, tb = t_max;
+    float mine, v, mlb, mrb;
+    bool eq0 = false;
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r) {
+        const uint32_t leaf = tree_round<kType, 5>(a, c, ta, tb, t_min, tl, s0, r == 0, mine, v, mlb, mrb);
+        if (r == 0) eq0 = __ballot_sync(0xFFFFFFFFu, tl.depth < 0 && v == c) != 0u;
+        const bool right = (v < c) == s0;
+        const float nta = right ? mine : mlb, ntb = right ? mrb : mine;
+        ta = __shfl_sync(0xFFFFFFFFu, nta, (int)leaf);
+        tb = __shfl_sync(0xFFFFFFFFu, ntb, (int)leaf);
+    }
+    const uint32_t leaf = tree_round<kType, 4>(a, c, ta, tb, t_min, tl, s0, false, mine, v, mlb, mrb);
+    const float fin = fabsf(__fsub_rn(v, c)) > 1.0f ? t_min : mine;
+    const float t = __shfl_sync(0xFFFFFFFFu, fin, (int)leaf);
+    return eq0 ? t_min : t;
+}
+
+// A chain solved by the whole warp; lane k%32 keeps root k until 32 roots
+// are stored at once.
+template <int kType>
+SR_DEV void run_chain_warp(const AxisPoly& a, int32_t len, float x, float dx, float t_lo, float t_hi, int side,
+                           int32_t* __restrict__ out, const TreeLane& tl) {
+    const uint32_t lane = lane_id();
+    float lo = t_lo;
+    int32_t keep = 0;
+    for (int32_t k = 0; k < len; ++k) {
+        const float c = x;
+        x = __fadd_rn(x, dx);
+        const float t = bisect_warp<kType>(a, c, lo, t_hi, tl);
+        const int32_t ob = (fbits(t) & ~3) | side;
+        if ((uint32_t)(k & 31) == lane) keep = ob;
+        if ((k & 31) == 31 || k + 1 == len) {
+            const int32_t k0 = k & ~31;
+            if ((int32_t)lane <= (k - k0)) out[k0 + (int32_t)lane] = keep;
+        }
+        lo = bitsf(ob);
+    }
+}
+
+struct ChainSetup {
+    AxisPoly a;
+    uint32_t type;
+    int32_t len;
+    float x, dx, t_lo, t_hi;
+    int side;
+    int64_t base;
+};
+
+// Chain item (curve << 4 | piece << 1 | side): its polynomial, first grid
+// line and step, t range and output slot.
+SR_DEV ChainSetup chain_setup(const GeomArgs& g, const int32_t* __restrict__ offs, const uint4* __restrict__ pieces,
+                              uint32_t item) {
+    ChainSetup s;
+    const uint32_t c = item >> 4, piece = (item >> 1) & 7u;
+    s.side = (int)(item & 1u);
+    s.type = g.curve_type[c];
+    const uint4* pt = pieces + (size_t)c * kMaxPieces;
+    int64_t base = offs[c];
+    for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
+    const uint4 me = pt[piece];
+    const int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
+    s.base = base + 1 + (s.side ? nx : 0);
+    s.len = s.side ? ny : nx;
+    const bool neg = s.side ? (me.x & 0x80000000u) != 0 : (me.x & 0x8000u) != 0;
+    s.x = __uint_as_float(s.side ? me.w : me.z);
+    s.dx = neg ? -(float)g.F : (float)g.F;
+    s.t_lo = piece == 0 ? 0.0f : __uint_as_float(pt[piece - 1].y);
+    s.t_hi = __uint_as_float(me.y);
+    const float2* cp = g.tpos + g.curve_pos[c];
+    const uint32_t np = s.type & 7u;
+    float p[4];
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+        float2 v = k < np ? cp[k] : make_float2(0.0f, 0.0f);
+        p[k] = s.side ? v.y : v.x;
+    }
+    s.a.p0 = p[0]; s.a.p1 = p[1]; s.a.p2 = p[2]; s.a.p3 = p[3];
+    s.a.d01 = __fsub_rn(p[1], p[0]);
+    s.a.d12 = __fsub_rn(p[2], p[1]);
+    s.a.d23 = __fsub_rn(p[3], p[2]);
+    return s;
+}
+
 __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t* __restrict__ offs,
                                                 const uint4* __restrict__ pieces,
                                                 const uint32_t* __restrict__ items, const uint32_t* __restrict__ keys,
                                                 uint32_t list_cap, const uint32_t* __restrict__ chain_count,
+                                                const uint32_t* __restrict__ wide_count,
                                                 uint32_t* __restrict__ queue, int32_t* __restrict__ cbuf) {
     const uint32_t total = imin((int32_t)*chain_count, (int32_t)list_cap);
+    const uint32_t n_wide = imin((int32_t)*wide_count, (int32_t)total);
     const uint32_t lane = lane_id();
-    // warps take groups of 32 chains in list order, so the longest groups go
-    // to the first warp of every SM rather than to one block
+    const TreeLane tl = tree_lane(lane);
+    // tickets [0, n_wide) are the wide chains (first in the list), one per
+    // warp; later tickets are groups of 32 chains in list order, so the
+    // longest groups go to the first warp of every SM rather than to one block
     for (;;) {
-        uint32_t grp = 0;
-        if (lane == 0) grp = atomicAdd(queue, 1u);
-        grp = __shfl_sync(0xFFFFFFFFu, grp, 0);
-        const uint32_t it = grp * 32u + lane;
-        if (grp * 32u >= total) break;
-        if (it >= total) continue;
-        uint32_t item = items[it];
-        const bool spec = chain_key_long(keys[it]);
-        uint32_t c = item >> 4, piece = (item >> 1) & 7u;
-        int side = (int)(item & 1u);
-        uint32_t type = g.curve_type[c];
-        const uint4* pt = pieces + (size_t)c * kMaxPieces;
-        int64_t base = offs[c];
-        for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
-        uint4 me = pt[piece];
-        int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
-        base += 1 + (side ? nx : 0);
-        int32_t len = side ? ny : nx;
-        if (base + len > g.rec_cap) continue;   // overflow: k_merge reports it
-        bool neg = side ? (me.x & 0x80000000u) != 0 : (me.x & 0x8000u) != 0;
-        float x = __uint_as_float(side ? me.w : me.z);
-        float dx = neg ? -(float)g.F : (float)g.F;
-        float t_lo = piece == 0 ? 0.0f : __uint_as_float(pt[piece - 1].y);
-        float t_hi = __uint_as_float(me.y);
-        const float2* cp = g.tpos + g.curve_pos[c];
-        AxisPoly a;
-        uint32_t np = type & 7u;
-        float p[4];
-#pragma unroll
-        for (uint32_t k = 0; k < 4; ++k) {
-            float2 v = k < np ? cp[k] : make_float2(0.0f, 0.0f);
-            p[k] = side ? v.y : v.x;
+        uint32_t ticket = 0;
+        if (lane == 0) ticket = atomicAdd(queue, 1u);
+        ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
+        if (ticket < n_wide) {
+            const ChainSetup s = chain_setup(g, offs, pieces, items[ticket]);
+            if (s.base + s.len > g.rec_cap) continue;   // overflow: k_merge reports it
+            int32_t* out = cbuf + s.base;
+            if (s.type == 4u) run_chain_warp<4>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
+            else if (s.type == 3u) run_chain_warp<3>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
+            continue;
         }
-        a.p0 = p[0]; a.p1 = p[1]; a.p2 = p[2]; a.p3 = p[3];
-        a.d01 = __fsub_rn(p[1], p[0]);
-        a.d12 = __fsub_rn(p[2], p[1]);
-        a.d23 = __fsub_rn(p[3], p[2]);
-        int32_t* out = cbuf + base;
-        if (type == 2u) run_chain<2, false>(a, len, x, dx, t_lo, t_hi, side, out);
-        else if (type == 3u) {
-            if (spec) run_chain<3, true>(a, len, x, dx, t_lo, t_hi, side, out);
-            else run_chain<3, false>(a, len, x, dx, t_lo, t_hi, side, out);
+        const uint32_t first = n_wide + (ticket - n_wide) * 32u;
+        if (first >= total) break;
+        const uint32_t it = first + lane;
+        if (it >= total) continue;
+        const bool spec = chain_key_long(keys[it]);
+        const ChainSetup s = chain_setup(g, offs, pieces, items[it]);
+        if (s.base + s.len > g.rec_cap) continue;   // overflow: k_merge reports it
+        int32_t* out = cbuf + s.base;
+        if (s.type == 2u) run_chain<2, false>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
+        else if (s.type == 3u) {
+            if (spec) run_chain<3, true>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
+            else run_chain<3, false>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
         } else {
-            if (spec) run_chain<4, true>(a, len, x, dx, t_lo, t_hi, side, out);
-            else run_chain<4, false>(a, len, x, dx, t_lo, t_hi, side, out);
+            if (spec) run_chain<4, true>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
+            else run_chain<4, false>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
         }
     }
 }
@@ -752,7 +901,8 @@ void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const Cha
     if (g.n_curves == 0) return;
     count_launches(1);
     k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count, w.pieces, w.chain_items, w.chain_keys,
-                                                      w.list_cap, w.chain_count, w.long_list, w.long_count, status);
+                                                      w.list_cap, w.chain_count, w.wide_count, w.long_list,
+                                                      w.long_count, status);
 }
 
 uint32_t chain_key_bits() { return kChainKeyBits; }
@@ -762,7 +912,7 @@ void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, i
     if (g.n_curves == 0) return;
     count_launches(1);
     k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
-                                            w.chain_count, w.chain_queue, cbuf);
+                                            w.chain_count, w.wide_count, w.chain_queue, cbuf);
 }
 
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,

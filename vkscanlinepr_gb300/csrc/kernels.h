@@ -70,6 +70,7 @@ struct ChainWork {
     uint32_t* sorted_keys;
     uint32_t list_cap;
     uint32_t* chain_count;    // [1] zeroed before the count pass
+    uint32_t* wide_count;     // [1] chains solved by a whole warp, zeroed before the count pass
     uint32_t* chain_queue;    // [1] zeroed before the chains
     uint32_t* long_list;      // [list_cap] (curve << 3 | piece) of long pieces
     uint32_t* long_count;     // [1] zeroed before the count pass
