@@ -457,8 +457,8 @@ SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t
 // round, which gives s0 in the same ballot.  24 steps = four 5-level rounds
 // and a last 4-level round, whose leaf midpoint is the 24th midpoint.
 struct TreeLane {
-    uint32_t dirs;    // bit j-1: turn at level j toward this lane's node
-    int32_t depth;    // node depth (lane 31: -1)
+    int32_t depth;            // node depth (lane 31: -1)
+    bool d1, d2, d3, d4;      // turn at level j toward this lane's node (right = true)
     uint32_t anc5, want5, anc4, want4;   // path masks of the leaves of a 5- and a 4-level round
 };
 
@@ -467,8 +467,10 @@ SR_DEV TreeLane tree_lane(uint32_t lane) {
     const uint32_t n = lane + 1u;
     const int32_t d = lane == 31u ? -1 : 31 - __clz((int32_t)n);
     tl.depth = d;
-    tl.dirs = 0;
-    for (int32_t j = 1; j <= d; ++j) tl.dirs |= ((n >> (d - j)) & 1u) << (j - 1);
+    tl.d1 = d >= 1 && ((n >> (d - 1)) & 1u);
+    tl.d2 = d >= 2 && ((n >> (d - 2)) & 1u);
+    tl.d3 = d >= 3 && ((n >> (d - 3)) & 1u);
+    tl.d4 = d >= 4 && (n & 1u);
     tl.anc5 = tl.want5 = tl.anc4 = tl.want4 = 0;
     for (int32_t i = 0; i < d; ++i) {   // ancestor at depth i and the turn it takes toward n
         const uint32_t anc = n >> (d - i), dir = (n >> (d - i - 1)) & 1u;
@@ -479,59 +481,65 @@ SR_DEV TreeLane tree_lane(uint32_t lane) {
     return tl;
 }
 
-// One round of kLevels bisection steps from [ta, tb].  Returns the chosen
-// leaf's lane; its node's midpoint, value and interval are in mine/v/lb/rb.
-template <int kType, int kLevels>
-SR_DEV uint32_t tree_round(const AxisPoly& a, float c, float ta, float tb, float t_eval, const TreeLane& tl,
-                           bool& s0, bool first, float& mine, float& v, float& mlb, float& mrb) {
-    // midpoints along this lane's path: m_j = (m_{j-1} + the interval's other
-    // end) * 0.5, the other end being older than m_{j-1}
-    float lb = ta, rb = tb, m = mid_rn(ta, tb);
-    mine = m;
-    mlb = lb;
-    mrb = rb;
+// This lane's node of a kLevels-level tree from [ta, tb]: its midpoint,
+// and its interval in lb/rb.  m_j = (m_{j-1} + the interval's other end) *
+// 0.5, the other end being older than m_{j-1}, so a level costs one add and
+// one multiply on the dependency path.
+template <int kLevels>
+SR_DEV float tree_node(float ta, float tb, const TreeLane& tl, float& lb, float& rb) {
+    lb = ta;
+    rb = tb;
+    float m = mid_rn(ta, tb);
 #pragma unroll
     for (int j = 1; j < kLevels; ++j) {
-        const bool dir = (tl.dirs >> (j - 1)) & 1u;
-        const float other = dir ? rb : lb;
-        lb = dir ? m : lb;
-        rb = dir ? rb : m;
-        m = __fmul_rn(__fadd_rn(m, other), 0.5f);
-        if (j == tl.depth) {
-            mine = m;
-            mlb = lb;
-            mrb = rb;
+        if (j <= tl.depth) {
+            const bool dir = j == 1 ? tl.d1 : (j == 2 ? tl.d2 : (j == 3 ? tl.d3 : tl.d4));
+            const float other = dir ? rb : lb;
+            if (dir) lb = m;
+            else rb = m;
+            m = __fmul_rn(__fadd_rn(m, other), 0.5f);
         }
     }
-    if (tl.depth < 0) mine = t_eval;   // lane 31: the root's t_min (used in the first round)
-    v = eval_axis<kType>(a, mine);
-    const uint32_t B = __ballot_sync(0xFFFFFFFFu, v < c);
-    if (first) s0 = (B >> 31) & 1u;
-    const uint32_t R = s0 ? B : ~B;   // bit l: node l+1 goes right
-    const bool leaf = tl.depth == kLevels - 1;
-    const uint32_t anc = kLevels == 5 ? tl.anc5 : tl.anc4, want = kLevels == 5 ? tl.want5 : tl.want4;
-    const uint32_t on = __ballot_sync(0xFFFFFFFFu, leaf && ((R ^ want) & anc) == 0u);
-    return (uint32_t)(__ffs(on) - 1);
+    return m;
 }
 
 template <int kType>
 SR_DEV float bisect_warp(const AxisPoly& a, float c, float t_min, float t_max, const TreeLane& tl) {
-    bool s0 = false;
-    float ta = t_min, tb = t_max;
-    float mine, v, mlb, mrb;
-    bool eq0 = false;
-#pragma unroll 1
+    float lb, rb;
+    // first round; lane 31's interval is [t_min, t_min], whose midpoint is
+    // t_min itself (2t and 2t * 0.5 are exact), so its bit of the ballot is s0
+    float m = tree_node<5>(t_min, tl.depth < 0 ? t_min : t_max, tl, lb, rb);
+    float v = eval_axis<kType>(a, m);
+    uint32_t B = __ballot_sync(0xFFFFFFFFu, v < c);
+    const bool s0 = (B >> 31) & 1u;
+    const bool eq0 = (__ballot_sync(0xFFFFFFFFu, v == c) >> 31) != 0u;
+    // node l+1 goes right when bit l of B equals s0: the leaf on the path is
+    // the one with ((B ^ key) & anc) == 0, key = want ^ (s0 ? 0 : ~0)
+    const uint32_t flip = s0 ? 0u : 0xFFFFFFFFu;
+    const uint32_t key5 = tl.want5 ^ flip, key4 = tl.want4 ^ flip;
+    float ta, tb;
+#pragma unroll
     for (int r = 0; r < 4; ++r) {
-        const uint32_t leaf = tree_round<kType, 5>(a, c, ta, tb, t_min, tl, s0, r == 0, mine, v, mlb, mrb);
-        if (r == 0) eq0 = __ballot_sync(0xFFFFFFFFu, tl.depth < 0 && v == c) != 0u;
+        if (r > 0) {
+            m = tree_node<5>(ta, tb, tl, lb, rb);
+            v = eval_axis<kType>(a, m);
+            B = __ballot_sync(0xFFFFFFFFu, v < c);
+        }
+        const uint32_t on = __ballot_sync(0xFFFFFFFFu, tl.depth == 4 && ((B ^ key5) & tl.anc5) == 0u);
+        const int leaf = 31 - __clz((int32_t)on);
         const bool right = (v < c) == s0;
-        const float nta = right ? mine : mlb, ntb = right ? mrb : mine;
-        ta = __shfl_sync(0xFFFFFFFFu, nta, (int)leaf);
-        tb = __shfl_sync(0xFFFFFFFFu, ntb, (int)leaf);
+        const float nta = right ? m : lb, ntb = right ? rb : m;
+        ta = __shfl_sync(0xFFFFFFFFu, nta, leaf);
+        tb = __shfl_sync(0xFFFFFFFFu, ntb, leaf);
     }
-    const uint32_t leaf = tree_round<kType, 4>(a, c, ta, tb, t_min, tl, s0, false, mine, v, mlb, mrb);
-    const float fin = fabsf(__fsub_rn(v, c)) > 1.0f ? t_min : mine;
-    const float t = __shfl_sync(0xFFFFFFFFu, fin, (int)leaf);
+    // steps 21-24: the chosen depth-3 node's midpoint is the 24th midpoint
+    m = tree_node<4>(ta, tb, tl, lb, rb);
+    v = eval_axis<kType>(a, m);
+    B = __ballot_sync(0xFFFFFFFFu, v < c);
+    const uint32_t on = __ballot_sync(0xFFFFFFFFu, tl.depth == 3 && ((B ^ key4) & tl.anc4) == 0u);
+    const int leaf = 31 - __clz((int32_t)on);
+    const float fin = fabsf(__fsub_rn(v, c)) > 1.0f ? t_min : m;
+    const float t = __shfl_sync(0xFFFFFFFFu, fin, leaf);
     return eq0 ? t_min : t;
 }
 
