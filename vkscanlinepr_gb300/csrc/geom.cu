@@ -453,7 +453,8 @@ SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t
 // (node n's children are 2n and 2n+1, the right child taken when the step
 // goes right), and one ballot of the (v < c) bits gives every node's turn.
 // The leaf whose ancestors all turn toward it is on the path; it hands the
-// new interval to the warp.  Lane 31 evaluates the root's t_min in the first
+// new interval to the warp through a max-reduction over the lanes (every
+// other lane offers 0; t >= 0, so the bit patterns order like the values).  Lane 31 evaluates the root's t_min in the first
 // round, which gives s0 in the same ballot.  24 steps = four 5-level rounds
 // and a last 4-level round, whose leaf midpoint is the 24th midpoint.
 struct TreeLane {
@@ -525,21 +526,20 @@ SR_DEV float bisect_warp(const AxisPoly& a, float c, float t_min, float t_max, c
             v = eval_axis<kType>(a, m);
             B = __ballot_sync(0xFFFFFFFFu, v < c);
         }
-        const uint32_t on = __ballot_sync(0xFFFFFFFFu, tl.depth == 4 && ((B ^ key5) & tl.anc5) == 0u);
-        const int leaf = 31 - __clz((int32_t)on);
+        const bool on = tl.depth == 4 && ((B ^ key5) & tl.anc5) == 0u;
         const bool right = (v < c) == s0;
-        const float nta = right ? m : lb, ntb = right ? rb : m;
-        ta = __shfl_sync(0xFFFFFFFFu, nta, leaf);
-        tb = __shfl_sync(0xFFFFFFFFu, ntb, leaf);
+        const uint32_t nta = on ? __float_as_uint(right ? m : lb) : 0u;
+        const uint32_t ntb = on ? __float_as_uint(right ? rb : m) : 0u;
+        ta = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, nta));
+        tb = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, ntb));
     }
     // steps 21-24: the chosen depth-3 node's midpoint is the 24th midpoint
     m = tree_node<4>(ta, tb, tl, lb, rb);
     v = eval_axis<kType>(a, m);
     B = __ballot_sync(0xFFFFFFFFu, v < c);
-    const uint32_t on = __ballot_sync(0xFFFFFFFFu, tl.depth == 3 && ((B ^ key4) & tl.anc4) == 0u);
-    const int leaf = 31 - __clz((int32_t)on);
+    const bool on = tl.depth == 3 && ((B ^ key4) & tl.anc4) == 0u;
     const float fin = fabsf(__fsub_rn(v, c)) > 1.0f ? t_min : m;
-    const float t = __shfl_sync(0xFFFFFFFFu, fin, leaf);
+    const float t = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, on ? __float_as_uint(fin) : 0u));
     return eq0 ? t_min : t;
 }
 
