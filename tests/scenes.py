@@ -135,6 +135,20 @@ def long_chains(w=2400, h=2400):
     return b.arrays()
 
 
+def opaque_layers(w=1100, h=64):
+    """Wide opaque and translucent layers: spans that cover whole 256-pixel
+    resolve segments (the renderer skips what an opaque span hides)."""
+    b = Builder(w, h)
+    b.path(0, (200, 30, 30, 255)).polygon([(0, 0), (1100, 0), (1100, 64), (0, 64)])
+    b.path(0, (20, 40, 220, 120)).polygon([(100, 10), (900, 10), (900, 50), (100, 50)])
+    b.path(0, (10, 190, 40, 255)).polygon([(256, 0), (780, 0), (780, 40), (256, 40)])
+    b.path(1, (250, 20, 20, 90)).polygon([(0, 20), (1100, 20), (1100, 30), (0, 30)])
+    b.path(1, (240, 240, 240, 255)).polygon([(600.5, 30.25), (1099.5, 31.75), (1000, 63.5), (590, 60)])
+    b.path(0, (0, 0, 0, 200)).polygon([(5.5, 2.5), (1090.25, 8.5), (1080.75, 60.5), (12.5, 55.25)])
+    b.path(0, (90, 90, 250, 255)).polygon([(0, 44), (1100, 44), (1100, 52), (0, 52)])
+    return b.arrays()
+
+
 ALL = {
     "square": square,
     "star_nonzero": lambda: star(rule=0),
@@ -144,4 +158,5 @@ ALL = {
     "offcanvas": offcanvas,
     "degenerate": degenerate,
     "long_chains": long_chains,
+    "opaque_layers": opaque_layers,
 }

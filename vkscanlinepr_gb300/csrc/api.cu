@@ -220,7 +220,7 @@ struct Pipeline {
     // frame
     DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, chain_sort_scratch, long_list;
     DevBuf cbuf, rec, keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status, draw, draw_row, totals;
-    DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, image;
+    DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, seg_cut, image;
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
     // learned sizing: per-path curve ranges, draw counters, features,
     // predictions, allotments and their sums
@@ -245,8 +245,8 @@ struct Pipeline {
                          &scenes_d, &cta_base_d, &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status,
                          &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf, &rec, &keys, &keys_alt,
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
-                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &image, &d_fkey,
-                         &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
+                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &image,
+                         &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
                          &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : ev)
@@ -453,9 +453,15 @@ struct Pipeline {
         CUDA_TRY(ensure(chain_sort_scratch, sr::sort_scratch_bytes(cp)));
         CUDA_TRY(ensure(totals, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(row_start, sizeof(int32_t) * ((size_t)total_rows + 1)));
+        CUDA_TRY(ensure(seg_cut, sizeof(uint32_t) * std::max<size_t>(cut_words(), 1)));
         if (segmented()) CUDA_TRY(ensure(seg_scratch, sr::segsort_scratch_bytes(std::max<uint32_t>(C, 1))));
         return SR_OK;
     }
+
+    // Resolve segments per cell row (the widest scene's) and the words of
+    // the per-segment cut table.
+    uint32_t cut_segs() const { return (uint32_t)((Wmax + sr::kResolveSeg - 1) / sr::kResolveSeg); }
+    size_t cut_words() const { return (size_t)total_rows * cut_segs(); }
 
     // The production sort is the per-path segmented sort unless the tuning
     // asks for the radix sort or the stages are kept (their sorted-index dump
@@ -543,7 +549,8 @@ struct Pipeline {
                                &ctl, &scan_status, &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf,
                                &rec, &keys, &keys_alt, &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status,
                                &draw, &draw_row, &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt,
-                               &row_sort_scratch, &row_start, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan,
+                               &row_sort_scratch, &row_start, &seg_cut, &image, &d_fkey, &d_fwn, &d_fleft,
+                               &d_wscan,
                                &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
                                &plan_tot, &judge_out, &seg_scratch, &seg_tiles};
         uint64_t t = 0;
@@ -672,6 +679,10 @@ struct Pipeline {
         wa.dbg_fflag = keep ? d_fflag.as<int32_t>() : nullptr;
         wa.dbg_sflag = keep ? d_sflag.as<int32_t>() : nullptr;
         wa.dbg_skey = keep ? d_skey.as<int32_t>() : nullptr;
+        wa.seg_cut = seg_cut.as<uint32_t>();
+        wa.cut_rows = total_rows;
+        wa.cut_segs = cut_segs();
+        CUDA_TRY(cudaMemsetAsync(seg_cut.p, 0, sizeof(uint32_t) * cut_words(), st));
         mark(ST_WINDING, false);
         launch_winding_emit(wa, tune.wind_items, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
         mark(ST_WINDING, true);
@@ -693,6 +704,8 @@ struct Pipeline {
         ra.warps = tune.resolve_warps;
         ra.pixel_mode = g.pixel_mode;
         ra.image = image.as<uint32_t>();
+        ra.seg_cut = seg_cut.as<uint32_t>();
+        ra.cut_segs = cut_segs();
         mark(ST_RESOLVE, false);
         launch_resolve(ra, res_ctas, st);
         mark(ST_RESOLVE, true);
@@ -965,6 +978,8 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     ra.warps = p.tune.resolve_warps;
     ra.pixel_mode = p.mode == SR_MODE_PIXEL;
     ra.image = p.image.as<uint32_t>();
+    ra.seg_cut = nullptr;
+    ra.cut_segs = 0;
     sr::launch_resolve(ra, p.res_ctas, st);
     CUDA_TRY(cudaGetLastError());
     p.last_O = n;

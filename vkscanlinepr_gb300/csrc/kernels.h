@@ -164,6 +164,12 @@ struct WindArgs {
     uint64_t* totals;               // [2] merged fragments, spans
     uint32_t* n_draw;               // [1] merged fragments + spans
     uint32_t* path_draw;            // [P] draw records per path (NULL unless labelling)
+    // [cut_rows][cut_segs]: 1 + the last draw index of a span that covers a
+    // resolve segment (kResolveSeg pixels) entirely and leaves nothing of
+    // what was under it (opaque in pixel mode, any span in reference mode);
+    // zeroed before the emit, NULL to skip
+    uint32_t* seg_cut;
+    uint32_t cut_rows, cut_segs;
     // parity dumps (NULL in production)
     int32_t* dbg_wscan;             // [N+1]
     int32_t* dbg_fflag;             // [N]
@@ -189,6 +195,8 @@ struct ResolveArgs {
     int32_t pixel_mode;
     int32_t warps;                    // warps per CTA: 8 or 16
     uint32_t* image;                  // all scenes' RGBA8 framebuffers
+    const uint32_t* seg_cut;          // [rows][cut_segs] from the emit, or NULL
+    uint32_t cut_segs;
 };
 // Pixels per warp of a resolve CTA.
 constexpr int kResolveSeg = 256;

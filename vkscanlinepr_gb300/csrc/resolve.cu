@@ -45,6 +45,7 @@ struct PixRec {
     float ia;           // 255 - a
     float sr, sg, sb;   // s*a per channel
     int32_t row;        // cell row within the CTA
+    uint32_t idx1;      // 1 + draw index
 };
 
 SR_DEV void blend3(float& r, float& g, float& b, const PixRec& q) {
@@ -62,6 +63,10 @@ uint32_t resolve_rows_per_cta(int32_t W, int warps) {
 
 // Which rows and segment a warp paints: a CTA holds rows_per_cta cell rows
 // of one scene; small canvases give each row fewer warps than the CTA has.
+// A warp skips the records before the last one that covers its whole
+// segment and hides what is under it (seg_cut, written by the emit): source-
+// over with a = 255 gives floor((255 s + 127) / 255) = s whatever the pixel
+// held, and an overwrite leaves nothing of it either.
 struct ResolveWork {
     const SceneInfo* si;
     int32_t W, r0, nr, segs, groups, my_row;
@@ -97,6 +102,12 @@ template <int WARPS> SR_DEV ResolveWork resolve_work(const ResolveArgs& a) {
     return w;
 }
 
+SR_DEV uint32_t resolve_cut(const ResolveArgs& a, const ResolveWork& w, int32_t seg, bool live) {
+    if (!a.seg_cut || !live) return 0u;
+    return a.seg_cut[(size_t)(w.si->row_base + (uint32_t)(w.r0 + w.my_row)) * a.cut_segs +
+                     (uint32_t)(seg / kResolveSeg)];
+}
+
 template <int WARPS> SR_DEV int32_t resolve_seg(const ResolveWork& w, int group) {
     constexpr int kResolveWarps = WARPS;
     const int warp = threadIdx.x >> 5;
@@ -114,6 +125,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
     for (int group = 0; group < w.groups; ++group) {
         const int32_t seg = resolve_seg<WARPS>(w, group) * kResolveSeg;
         const bool live = w.active && seg < W;
+        const uint32_t cut = resolve_cut(a, w, seg, live);
         float r[kK], g[kK], b[kK];
 #pragma unroll
         for (int j = 0; j < kK; ++j) r[j] = g[j] = b[j] = 255.0f;
@@ -121,8 +133,10 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
             const int32_t cnt = imin(kChunk, end - c0);
             __syncthreads();
             for (int q = tid; q < cnt; q += blockDim.x) {
-                int4 d = a.draw[a.row_sorted_idx[c0 + q]];
+                const uint32_t di = a.row_sorted_idx[c0 + q];
+                int4 d = a.draw[di];
                 PixRec pr;
+                pr.idx1 = di + 1u;
                 int32_t x = d.x & 0xFFFF;
                 pr.x0 = x;
                 pr.x1 = wadd(x, d.y);
@@ -139,7 +153,9 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
             for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
                 const int32_t qi = g0 + lane;
                 bool ov = false;
-                if (qi < cnt) ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg;
+                if (qi < cnt)
+                    ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg &&
+                         sq[qi].idx1 >= cut;
                 uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
                 while (m) {
                     const int q = g0 + __ffs(m) - 1;
@@ -196,6 +212,7 @@ struct RefRec {
     int32_t x0, x1;
     uint32_t col;
     int32_t row;
+    uint32_t idx1;   // 1 + draw index
 };
 
 template <int WARPS>
@@ -209,6 +226,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
     for (int group = 0; group < w.groups; ++group) {
         const int32_t seg = resolve_seg<WARPS>(w, group) * kResolveSeg;
         const bool live = w.active && seg < W;
+        const uint32_t cut = resolve_cut(a, w, seg, live);
         uint32_t px[kK];
 #pragma unroll
         for (int j = 0; j < kK; ++j) px[j] = 0xFFFFFFFFu;
@@ -216,8 +234,10 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
             const int32_t cnt = imin(kChunk, end - c0);
             __syncthreads();
             for (int q = tid; q < cnt; q += blockDim.x) {
-                int4 d = a.draw[a.row_sorted_idx[c0 + q]];
+                const uint32_t di = a.row_sorted_idx[c0 + q];
+                int4 d = a.draw[di];
                 RefRec rr;
+                rr.idx1 = di + 1u;
                 rr.x0 = d.x & 0xFFFF;
                 rr.x1 = wadd(rr.x0, d.y);
                 rr.col = (uint32_t)d.z;
@@ -229,7 +249,9 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
             for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
                 const int32_t qi = g0 + lane;
                 bool ov = false;
-                if (qi < cnt) ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg;
+                if (qi < cnt)
+                    ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg &&
+                         sq[qi].idx1 >= cut;
                 uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
                 while (m) {
                     const int q = g0 + __ffs(m) - 1;

@@ -369,8 +369,16 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
             Decoded d0 = unpack_key(a.L, S.keys[jl]);
             int32_t x0 = imax(0, wadd(d0.x, F));
             if (o < a.draw_capacity) {
+                const uint32_t row = row_base + (uint32_t)(d0.y / F);
                 a.draw[o] = make_int4((int32_t)((uint32_t)d0.y << 16) | x0, d1.x - x0, info, 0);
-                a.draw_row[o] = row_base + (uint32_t)(d0.y / F);
+                a.draw_row[o] = row;
+                // a span that hides everything under it ends the resolve's
+                // work before it in each segment it covers whole
+                if (a.seg_cut && (!a.pixel_mode || ((uint32_t)info >> 24) == 255u) && row < a.cut_rows) {
+                    const int32_t s_hi = imin(d1.x / kResolveSeg, (int32_t)a.cut_segs);
+                    for (int32_t sg = (x0 + kResolveSeg - 1) / kResolveSeg; sg < s_hi; ++sg)
+                        atomicMax(&a.seg_cut[(size_t)row * a.cut_segs + (uint32_t)sg], (uint32_t)o + 1u);
+                }
             } else {
                 set_error(status, ERR_CAPACITY);
             }
