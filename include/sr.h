@@ -285,7 +285,7 @@ void sr_batch_destroy(sr_batch* b);
 typedef struct sr_tuning {
     uint32_t struct_size;
     int32_t  sort_items;      /* keys per thread of a sort tile: 8, 12 (default) or 16 */
-    int32_t  resolve_warps;   /* warps per resolve CTA: 8 or 16 (default) */
+    int32_t  resolve_warps;   /* warps per resolve CTA: 8 (default) or 16 */
     int32_t  wind_items;      /* records per thread of a winding tile: 4 or 8 (default) */
     int32_t  sort_kind;       /* 0: per-path segmented sort (default), 1: radix sort of the whole array */
 } sr_tuning;

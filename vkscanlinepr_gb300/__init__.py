@@ -471,7 +471,7 @@ class ScanlineVGRasterizer:
         _check(lib().sr_render(self._ctx, ptr, 0, stream))
         return out
 
-    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8, sort_kind=0):
+    def set_tuning(self, sort_items=12, resolve_warps=8, wind_items=8, sort_kind=0):
         t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items,
                      "sort_kind": sort_kind})
         _check(lib().sr_set_tuning(self._ctx, ctypes.byref(t)))
@@ -588,7 +588,7 @@ class SceneBatch:
     def n_paths(self):
         return self.stats()["n_paths"]
 
-    def set_tuning(self, sort_items=12, resolve_warps=16, wind_items=8, sort_kind=0):
+    def set_tuning(self, sort_items=12, resolve_warps=8, wind_items=8, sort_kind=0):
         t = _tuning({"sort_items": sort_items, "resolve_warps": resolve_warps, "wind_items": wind_items,
                      "sort_kind": sort_kind})
         _check(lib().sr_batch_set_tuning(self._h, ctypes.byref(t)))

@@ -204,7 +204,7 @@ struct Pipeline {
     int32_t mode = SR_MODE_PIXEL, F = 1;
     uint32_t flags = 0;
     bool loaded = false;
-    sr_tuning tune{sizeof(sr_tuning), 12, 16, 8, 0};
+    sr_tuning tune{sizeof(sr_tuning), 12, 8, 8, 0};
     // segmented sort of this frame: merge rounds (-1: radix sort instead) and
     // the largest segment the tables accept without flagging an overflow
     int seg_levels = 0;
