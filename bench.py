@@ -49,11 +49,12 @@ L2_FLUSH_BYTES = 256 << 20
 LIMITS = {
     "resolve": "FP32 instruction issue: 6.9 G pixel-blends x 9 FP32 ops, issue 80% busy, DRAM 1%",
     "chains": "the dependent bisection steps of the longest crossing chains",
+    "wide": "the longest chain's bisection rounds (lane exchange latency), beside the rest of the frame",
     "sort": "shared-memory ranking latency of the tile sort and merge rounds",
     "winding_emit": "instruction issue and two chained look-backs, DRAM 11%",
 }
 STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
-               "row_sort", "resolve"]
+               "row_sort", "resolve", "wide"]
 
 
 def parse_args():
@@ -191,6 +192,9 @@ def stage_bytes(st, n_curves, n_points, W, H):
         "winding_emit": N * 8 + O * (16 + 4),
         "row_sort": O * 4 + row_passes * O * 2 * (4 + 4),
         "resolve": O * (4 + 16) + W * H * 4,
+        # the wide chains and their curves' merge and fragments, on a second
+        # stream beside chains, merge and fragment (their bytes are counted there)
+        "wide": 0,
     }
 
 
@@ -704,13 +708,13 @@ def main():
     peak, peak_kind = measured_peaks()
     sb = stage_bytes(st, scene.n_curves, scene.n_points, W, H)
     stage_ms = {k: stage_acc[k] / args.steps for k in STAGE_NAMES}
-    dom = max(stage_ms, key=lambda k: stage_ms[k])
+    dom = max((k for k in stage_ms if sb[k]), key=lambda k: stage_ms[k])
     stages = {}
     for k in STAGE_NAMES:
         ms = stage_ms[k]
         stages[k] = {"ms": round(ms, 4), "algo_bytes": int(sb[k]),
-                     "gbs": round(sb[k] / (ms * 1e6), 1) if ms > 0 else None,
-                     "frac": round(sb[k] / (ms * 1e6) / peak, 4) if ms > 0 else None}
+                     "gbs": round(sb[k] / (ms * 1e6), 1) if ms > 0 and sb[k] else None,
+                     "frac": round(sb[k] / (ms * 1e6) / peak, 4) if ms > 0 and sb[k] else None}
     traffic = None
     tr = profile_traffic()
     if dom in tr and tr[dom][1] > 0:

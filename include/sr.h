@@ -150,7 +150,9 @@ typedef struct sr_stats {
     uint32_t reserved;
     /* with SR_FLAG_PROFILE: device time of each stage (CUDA events on the
      * render stream): transform, count, offset scan, crossing chains,
-     * record merge, fragments, sort, winding+emit, row sort, resolve */
+     * record merge, fragments, sort, winding+emit, row sort, resolve; then
+     * the wide chains with their curves' merge and fragments, which run on
+     * a second stream beside chains, merge and fragments */
     float stage_ms[12];
 } sr_stats;
 sr_status sr_get_stats(const sr_ctx* ctx, sr_stats* out);

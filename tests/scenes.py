@@ -149,6 +149,19 @@ def opaque_layers(w=1100, h=64):
     return b.arrays()
 
 
+def long_line(w=9000, h=64):
+    """A line crossing more than 8192 grid columns beside cubics of a few
+    hundred crossings: the line's chain must sort after the warp-solved ones."""
+    b = Builder(w, h)
+    b.path(0, RED)
+    b.curve(LINE, [(1.5, 10.5), (8999.5, 50.5)])
+    b.curve(CUBIC, [(8999.5, 50.5), (6000.0, 70.0), (3000.0, -10.0), (1.5, 10.5)])
+    b.path(1, BLUE)
+    b.curve(CUBIC, [(100.25, 5.5), (500.0, 60.0), (900.0, 2.0), (1300.75, 58.5)])
+    b.curve(LINE, [(1300.75, 58.5), (100.25, 5.5)])
+    return b.arrays()
+
+
 ALL = {
     "square": square,
     "star_nonzero": lambda: star(rule=0),
@@ -159,4 +172,5 @@ ALL = {
     "degenerate": degenerate,
     "long_chains": long_chains,
     "opaque_layers": opaque_layers,
+    "long_line": long_line,
 }

@@ -69,7 +69,7 @@ class Stats(ctypes.Structure):
                 ("stage_ms", ctypes.c_float * 12)]
 
 STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
-               "row_sort", "resolve"]
+               "row_sort", "resolve", "wide"]
 
 
 class BatchRenderOpts(ctypes.Structure):

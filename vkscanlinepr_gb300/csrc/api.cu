@@ -106,6 +106,8 @@ enum Ctl : int {
     CTL_LONG = 8,      // long-piece counter
     CTL_QUEUE = 9,     // chain work-queue counter
     CTL_WIDE = 10,     // chains solved by a whole warp
+    CTL_WIDE_QUEUE = 11,    // their work-queue counter
+    CTL_WIDE_CURVES = 12,   // curves with such a chain
     CTL_WORDS = 16,
 };
 
@@ -121,7 +123,7 @@ uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); 
 
 enum Stage : int {
     ST_TRANSFORM = 0, ST_COUNT, ST_SCAN, ST_CHAINS, ST_MERGE, ST_FRAGMENT, ST_SORT, ST_WINDING, ST_ROWSORT,
-    ST_RESOLVE, ST_COUNT_ALL
+    ST_RESOLVE, ST_WIDE, ST_COUNT_ALL
 };
 
 static sr_status check_status_word(uint32_t s) {
@@ -219,6 +221,7 @@ struct Pipeline {
     DevBuf pos, pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info, path_scene, scenes_d, cta_base_d;
     // frame
     DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, chain_sort_scratch, long_list;
+    DevBuf curve_wide, wide_curves;
     DevBuf cbuf, rec, keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status, draw, draw_row, totals;
     DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, seg_cut, image;
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
@@ -239,6 +242,10 @@ struct Pipeline {
     cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
     bool ev_pending = false, capturing = false;
     cudaStream_t cur = nullptr;
+    // second stream of a frame: the wide chains and their curves' merge and
+    // fragments run on it beside the rest (forked and joined by events)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_merged = nullptr, ev_join = nullptr;
 
     ~Pipeline() {
         DevBuf* all[] = {&pos, &pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info, &path_scene,
@@ -247,8 +254,12 @@ struct Pipeline {
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
                          &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &image,
                          &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
-                         &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles};
+                         &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide,
+                         &wide_curves};
         for (DevBuf* b : all) release(*b);
+        for (cudaEvent_t e : {ev_fork, ev_merged, ev_join})
+            if (e) cudaEventDestroy(e);
+        if (side) cudaStreamDestroy(side);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
         if (h_u32) cudaFreeHost(h_u32);
@@ -267,14 +278,17 @@ struct Pipeline {
         CUDA_TRY(cudaMallocHost(&h_u32, sizeof(uint32_t) * 8));
         CUDA_TRY(cudaMallocHost(&h_u64, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(ctl, sizeof(uint32_t) * CTL_WORDS));
+        CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&ev_fork, &ev_merged, &ev_join})
+            CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
         return SR_OK;
     }
 
-    void mark(int stage, bool end) {
+    void mark(int stage, bool end, cudaStream_t on = nullptr) {
         if (!(flags & SR_FLAG_PROFILE) || capturing) return;
         cudaEvent_t& e = ev[2 * stage + (end ? 1 : 0)];
         if (!e) cudaEventCreate(&e);
-        cudaEventRecord(e, cur);
+        cudaEventRecord(e, on ? on : cur);
     }
 
     sr::KeyLayout layout() const {
@@ -432,6 +446,10 @@ struct Pipeline {
         cw.chain_count = ctlp + CTL_CHAINS;
         cw.chain_queue = ctlp + CTL_QUEUE;
         cw.wide_count = ctlp + CTL_WIDE;
+        cw.wide_queue = ctlp + CTL_WIDE_QUEUE;
+        cw.curve_wide = curve_wide.as<uint8_t>();
+        cw.wide_curves = wide_curves.as<uint32_t>();
+        cw.wide_curve_count = ctlp + CTL_WIDE_CURVES;
         cw.long_list = long_list.as<uint32_t>();
         cw.long_count = ctlp + CTL_LONG;
         return cw;
@@ -449,6 +467,8 @@ struct Pipeline {
         const uint32_t lc = list_cap();
         CUDA_TRY(ensure(chain_lists, sizeof(uint32_t) * 6 * (size_t)lc));
         CUDA_TRY(ensure(long_list, sizeof(uint32_t) * (size_t)lc));
+        CUDA_TRY(ensure(curve_wide, std::max<size_t>(C, 1)));
+        CUDA_TRY(ensure(wide_curves, sizeof(uint32_t) * std::max<size_t>(C, 1)));
         sr::SortPlan cp = sr::sort_plan(lc, sr::chain_key_bits(), ctl.as<uint32_t>() + CTL_CHAINS);
         CUDA_TRY(ensure(chain_sort_scratch, sr::sort_scratch_bytes(cp)));
         CUDA_TRY(ensure(totals, sizeof(uint64_t) * 4));
@@ -552,7 +572,7 @@ struct Pipeline {
                                &row_sort_scratch, &row_start, &seg_cut, &image, &d_fkey, &d_fwn, &d_fleft,
                                &d_wscan,
                                &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
-                               &plan_tot, &judge_out, &seg_scratch, &seg_tiles};
+                               &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide, &wide_curves};
         uint64_t t = 0;
         for (const DevBuf* b : all) t += b->cap;
         return t;
@@ -631,16 +651,33 @@ struct Pipeline {
             dbg.fleft = d_fleft.as<int32_t>();
             CUDA_TRY(cudaMemsetAsync(d_wscan.p, 0, sizeof(int32_t) * ((size_t)std::max<int64_t>(cap, 1) + 1), st));
         }
+        // the wide chains and their curves' merge and fragments on the side
+        // stream, the rest on st; the side stream's merge waits for st's
+        // merge (which marks the wide curves' records pending, and covers the
+        // short chains of the wide curves), and st waits for the side stream
+        // before the sort
+        CUDA_TRY(cudaEventRecord(ev_fork, st));
+        CUDA_TRY(cudaStreamWaitEvent(side, ev_fork, 0));
+        mark(ST_WIDE, false, side);
+        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, 0, side);
         mark(ST_CHAINS, false);
-        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, st);
+        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, 1, st);
         mark(ST_CHAINS, true);
         mark(ST_MERGE, false);
-        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, st);
+        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, 0, st);
         mark(ST_MERGE, true);
+        CUDA_TRY(cudaEventRecord(ev_merged, st));
+        CUDA_TRY(cudaStreamWaitEvent(side, ev_merged, 0));
+        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, 1, side);
         mark(ST_FRAGMENT, false);
-        launch_fragment(g, rec.as<int2>(), cap, n_dev, keys.as<uint64_t>(), keep ? wnp.as<uint8_t>() : nullptr, dbg,
-                        st);
+        launch_fragment(g, rec.as<int2>(), offs.as<int32_t>(), cap, n_dev, keys.as<uint64_t>(),
+                        keep ? wnp.as<uint8_t>() : nullptr, dbg, cw, 0, st);
         mark(ST_FRAGMENT, true);
+        launch_fragment(g, rec.as<int2>(), offs.as<int32_t>(), cap, n_dev, keys.as<uint64_t>(),
+                        keep ? wnp.as<uint8_t>() : nullptr, dbg, cw, 1, side);
+        mark(ST_WIDE, true, side);
+        CUDA_TRY(cudaEventRecord(ev_join, side));
+        CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
         const KeyLayout L = g.L;
         SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev, tune.sort_items);
         mark(ST_SORT, false);

@@ -138,19 +138,20 @@ SR_DEV int32_t piece_ny(uint32_t n) { return (int32_t)((n >> 16) & 0x7FFFu); }
 // Sort key of a chain: longest length class first (so the longest dependency
 // chains start in the first wave of k_chains), then cubic, quadric, line, so
 // that a warp runs one curve type with lengths within a factor of 2.  A line
-// root is a closed form, about 2^5 times cheaper than a 24-step bisection, so
-// a line chain is classed 5 length classes lower.
+// root is a closed form, far cheaper than a 24-step bisection, so a line
+// chain is classed 7 length classes lower (at most class 7, below every
+// wide chain).
 SR_DEV uint32_t chain_key(int32_t len, uint32_t type) {
     uint32_t lg = 31u - (uint32_t)__clz(len);
     if (lg > 14u) lg = 14u;
-    if (type != 3u && type != 4u) lg = lg > 5u ? lg - 5u : 0u;
+    if (type != 3u && type != 4u) lg = lg > 7u ? lg - 7u : 0u;
     uint32_t cls = type == 4u ? 0u : (type == 3u ? 1u : 2u);
     return ((14u - lg) << 2) | cls;
 }
 SR_DEV bool chain_key_long(uint32_t key) { return (key >> 2) <= 14u - 5u; }   // >= 32 crossings
-// Chains of >= 1024 bisected roots are solved by a whole warp each
-// (run_chain_warp); they sort before every other chain.
-SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 10u; }
+// Cubic and quadric chains of >= 256 bisected roots (class >= 8) are solved
+// by a whole warp each (run_chain_warp); they sort before every other chain.
+SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 8u && (key & 3u) != 2u; }
 constexpr uint32_t kChainKeyBits = 6;
 
 // get_xy_begin_end_delta + udpate_cut_range for one axis
@@ -183,6 +184,8 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
                                                uint32_t* __restrict__ chain_items, uint32_t* __restrict__ chain_keys,
                                                uint32_t list_cap, uint32_t* __restrict__ chain_count,
                                                uint32_t* __restrict__ wide_count,
+                                               uint8_t* __restrict__ curve_wide, uint32_t* __restrict__ wide_curves,
+                                               uint32_t* __restrict__ wide_curve_count,
                                                uint32_t* __restrict__ long_list, uint32_t* __restrict__ long_count,
                                                uint32_t* __restrict__ status) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -310,6 +313,10 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
         }
         count[c] = pc;
         if (walk != pc) set_error(status, ERR_RECORD_RANGE);
+        bool wide = false;
+        for (int k = 0; k < n_chains; ++k) wide |= chain_key_wide(my_key[k]);
+        curve_wide[c] = wide ? 1 : 0;
+        if (wide) wide_curves[atomicAdd(wide_curve_count, 1u)] = c;
     }
     // append long pieces (warp-aggregated)
     const uint32_t lane = lane_id();
@@ -609,32 +616,39 @@ SR_DEV ChainSetup chain_setup(const GeomArgs& g, const int32_t* __restrict__ off
     return s;
 }
 
+// Part 0 solves the wide chains (first in the list), one per warp; part 1
+// the others in groups of 32 in list order, so the longest groups go to the
+// first warp of every SM rather than to one block.  The two parts run on two
+// streams at once.
 __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t* __restrict__ offs,
                                                 const uint4* __restrict__ pieces,
                                                 const uint32_t* __restrict__ items, const uint32_t* __restrict__ keys,
                                                 uint32_t list_cap, const uint32_t* __restrict__ chain_count,
                                                 const uint32_t* __restrict__ wide_count,
-                                                uint32_t* __restrict__ queue, int32_t* __restrict__ cbuf) {
+                                                uint32_t* __restrict__ queue, int32_t* __restrict__ cbuf, int part) {
     const uint32_t total = imin((int32_t)*chain_count, (int32_t)list_cap);
     const uint32_t n_wide = imin((int32_t)*wide_count, (int32_t)total);
     const uint32_t lane = lane_id();
-    const TreeLane tl = tree_lane(lane);
-    // tickets [0, n_wide) are the wide chains (first in the list), one per
-    // warp; later tickets are groups of 32 chains in list order, so the
-    // longest groups go to the first warp of every SM rather than to one block
-    for (;;) {
-        uint32_t ticket = 0;
-        if (lane == 0) ticket = atomicAdd(queue, 1u);
-        ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
-        if (ticket < n_wide) {
+    if (part == 0) {
+        const TreeLane tl = tree_lane(lane);
+        for (;;) {
+            uint32_t ticket = 0;
+            if (lane == 0) ticket = atomicAdd(queue, 1u);
+            ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
+            if (ticket >= n_wide) break;
             const ChainSetup s = chain_setup(g, offs, pieces, items[ticket]);
             if (s.base + s.len > g.rec_cap) continue;   // overflow: k_merge reports it
             int32_t* out = cbuf + s.base;
             if (s.type == 4u) run_chain_warp<4>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
             else if (s.type == 3u) run_chain_warp<3>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
-            continue;
         }
-        const uint32_t first = n_wide + (ticket - n_wide) * 32u;
+        return;
+    }
+    for (;;) {
+        uint32_t ticket = 0;
+        if (lane == 0) ticket = atomicAdd(queue, 1u);
+        ticket = __shfl_sync(0xFFFFFFFFu, ticket, 0);
+        const uint32_t first = n_wide + ticket * 32u;
         if (first >= total) break;
         const uint32_t it = first + lane;
         if (it >= total) continue;
@@ -659,11 +673,13 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
 // side counting as 2.0 (with its side bit); a record whose t (flag bits
 // masked) equals the previous one ORs the flags into both
 // (make_intersection_1.comp:361-375).
-__global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* __restrict__ offs,
-                                               const uint4* __restrict__ pieces, const int32_t* __restrict__ cbuf,
-                                               int2* __restrict__ rec, uint32_t* __restrict__ status) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= g.n_curves) return;
+// Records of a wide curve hold this until its merge, which runs on the other
+// stream, writes them; the record-parallel fragment pass skips them.
+constexpr int32_t kPendingCurve = -1;
+
+SR_DEV void merge_curve(const GeomArgs& g, const int32_t* __restrict__ offs, const uint4* __restrict__ pieces,
+                        const int32_t* __restrict__ cbuf, int2* __restrict__ rec, uint32_t* __restrict__ status,
+                        uint32_t c, bool pending_only) {
     int64_t pc = offs[c];
     const int64_t end = offs[c + 1];
     if (pc >= end) return;
@@ -697,6 +713,12 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
             t0 = (int32_t)me.y;
             continue;
         }
+        if (pending_only) {
+            for (int32_t k = 0; k < n_loop; ++k) rec[pc + k] = make_int2(kPendingCurve, 0);
+            pc += n_loop;
+            t0 = (int32_t)me.y;
+            continue;
+        }
         int32_t last = minus_one;
         for (int32_t k = 0; k < n_loop; ++k) {
             int32_t av = ex_x, bv = ex_y;
@@ -721,6 +743,24 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
         t0 = (int32_t)me.y;
     }
     if (pc != end) set_error(status, ERR_RECORD_RANGE);
+}
+
+// Part 0 merges every curve but the wide ones, whose records it marks
+// pending; part 1 merges the wide curves once their chains are done.
+__global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* __restrict__ offs,
+                                               const uint4* __restrict__ pieces, const int32_t* __restrict__ cbuf,
+                                               int2* __restrict__ rec, uint32_t* __restrict__ status,
+                                               const uint8_t* __restrict__ curve_wide,
+                                               const uint32_t* __restrict__ wide_curves,
+                                               const uint32_t* __restrict__ wide_curve_count, int part) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (part == 0) {
+        if (tid < g.n_curves) merge_curve(g, offs, pieces, cbuf, rec, status, tid, curve_wide[tid] != 0);
+        return;
+    }
+    const uint32_t nw = imin((int32_t)*wide_curve_count, (int32_t)g.n_curves);
+    for (uint32_t k = tid; k < nw; k += gridDim.x * blockDim.x)
+        merge_curve(g, offs, pieces, cbuf, rec, status, wide_curves[k], false);
 }
 
 // Merge of one long piece by a CTA.  The chains are non-decreasing (each
@@ -754,18 +794,25 @@ __global__ void __launch_bounds__(256) k_merge_long(const GeomArgs g, const int3
                                                     const uint4* __restrict__ pieces,
                                                     const uint32_t* __restrict__ long_list, uint32_t list_cap,
                                                     const uint32_t* __restrict__ long_count,
-                                                    int32_t* __restrict__ cbuf, int2* __restrict__ rec) {
+                                                    int32_t* __restrict__ cbuf, int2* __restrict__ rec,
+                                                    const uint8_t* __restrict__ curve_wide, int part) {
     __shared__ int32_t s_i0;
     const uint32_t n_long = imin((int32_t)*long_count, (int32_t)list_cap);
     const int tid = threadIdx.x, nt = blockDim.x;
     for (uint32_t item = blockIdx.x; item < n_long; item += gridDim.x) {
         const uint32_t c = long_list[item] >> 3, piece = long_list[item] & 7u;
+        const bool wide = curve_wide[c] != 0;   // the same for the whole CTA
+        if (part == 1 && !wide) continue;
         const uint4* pt = pieces + (size_t)c * kMaxPieces;
         int64_t base = offs[c];
         for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
         const int32_t nx = piece_nx(pt[piece].x), ny = piece_ny(pt[piece].x);
         const int32_t L = 1 + nx + ny;
         if (base + L > g.rec_cap) continue;   // overflow: k_merge reports it
+        if (part == 0 && wide) {   // merged by part 1: mark pending
+            for (int32_t k = tid; k < L; k += nt) rec[base + k] = make_int2(kPendingCurve, 0);
+            continue;
+        }
         const int32_t t0 = piece == 0 ? 0 : (int32_t)pt[piece - 1].y;
         const int32_t* X = cbuf + base + 1;
         const int32_t* Y = X + nx;
@@ -815,16 +862,12 @@ __global__ void __launch_bounds__(256) k_merge_long(const GeomArgs g, const int3
 // record's t and the next record's t (t = 1 when the next record belongs to
 // another curve), its cell, the 64-bit sort key, the winding change across
 // the sample row and (pixel mode) the part of it left of the cell centre.
-__global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* __restrict__ rec, int64_t n_cap,
-                                                  const uint32_t* __restrict__ n_dev, uint64_t* __restrict__ keys,
-                                                  uint8_t* __restrict__ wnp, DebugOut dbg) {
-    const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_cap) : n_cap;
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int2 r0 = rec[i];
-    int2 r1 = (i + 1 != n) ? rec[i + 1] : make_int2(-1, 0x3f800000);
+// Record i of curve r0.x: the piece runs to the next record's t when that
+// record belongs to the same curve (i + 1 < offs[c + 1]), else to t = 1.
+SR_DEV void fragment_record(const GeomArgs& g, const int2* __restrict__ rec, const int32_t* __restrict__ offs,
+                            int64_t n, int64_t i, int2 r0, uint64_t* __restrict__ keys, uint8_t* __restrict__ wnp,
+                            const DebugOut& dbg) {
     float t0 = gmax(bitsf(r0.y & ~3), 0.0f);
-    float t1 = gmax(bitsf(r1.y & ~3), 0.0f);
     uint32_t c = (uint32_t)r0.x;
     if (c >= g.n_curves) {
         // only in a frame whose records overflowed their capacity (the
@@ -833,8 +876,9 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
         if (wnp) wnp[i] = 0;
         return;
     }
+    float t1 = 1.0f;
+    if (i + 1 < n && i + 1 < (int64_t)offs[c + 1]) t1 = gmax(bitsf(rec[i + 1].y & ~3), 0.0f);
     uint32_t path = g.curve_path[c];
-    if (r0.x != r1.x) t1 = 1.0f;
     int32_t yx = (int32_t)0xFFFEFFFE, wn = 0, left = 0;
     bool valid = false;
     int32_t pos_x = 0, pos_y = 0;
@@ -882,6 +926,34 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
     }
 }
 
+// Part 0: every record but those of wide curves (pending, or already
+// merged by part 1); part 1: the wide curves' records, a CTA per curve.
+__global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* __restrict__ rec,
+                                                  const int32_t* __restrict__ offs, int64_t n_cap,
+                                                  const uint32_t* __restrict__ n_dev, uint64_t* __restrict__ keys,
+                                                  uint8_t* __restrict__ wnp, DebugOut dbg,
+                                                  const uint8_t* __restrict__ curve_wide,
+                                                  const uint32_t* __restrict__ wide_curves,
+                                                  const uint32_t* __restrict__ wide_curve_count, int part) {
+    const int64_t n = n_dev ? (int64_t)min((uint64_t)*n_dev, (uint64_t)n_cap) : n_cap;
+    if (part == 0) {
+        const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n) return;
+        const int2 r0 = rec[i];
+        if (r0.x == kPendingCurve) return;
+        if ((uint32_t)r0.x < g.n_curves && curve_wide[r0.x]) return;
+        fragment_record(g, rec, offs, n, i, r0, keys, wnp, dbg);
+        return;
+    }
+    const uint32_t nw = imin((int32_t)*wide_curve_count, (int32_t)g.n_curves);
+    for (uint32_t k = blockIdx.x; k < nw; k += gridDim.x) {
+        const uint32_t c = wide_curves[k];
+        const int64_t end = min((int64_t)offs[c + 1], n);
+        for (int64_t i = (int64_t)offs[c] + threadIdx.x; i < end; i += blockDim.x)
+            fragment_record(g, rec, offs, n, i, rec[i], keys, wnp, dbg);
+    }
+}
+
 // -------------------------------------------------------------- launches --
 void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const SceneTable& t,
                       float2* tpos, int32_t* path_visible, cudaStream_t st) {
@@ -909,34 +981,44 @@ void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const Cha
     if (g.n_curves == 0) return;
     count_launches(1);
     k_count<<<(g.n_curves + 255) / 256, 256, 0, st>>>(g, cut_cache, count, w.pieces, w.chain_items, w.chain_keys,
-                                                      w.list_cap, w.chain_count, w.wide_count, w.long_list,
-                                                      w.long_count, status);
+                                                      w.list_cap, w.chain_count, w.wide_count, w.curve_wide,
+                                                      w.wide_curves, w.wide_curve_count, w.long_list, w.long_count,
+                                                      status);
 }
 
 uint32_t chain_key_bits() { return kChainKeyBits; }
 
-void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
+void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count, int part,
                    cudaStream_t st) {
     if (g.n_curves == 0) return;
     count_launches(1);
-    k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
-                                            w.chain_count, w.wide_count, w.chain_queue, cbuf);
+    if (part == 0)
+        k_chains<<<sm_count * 4, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
+                                               w.chain_count, w.wide_count, w.wide_queue, cbuf, 0);
+    else
+        k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
+                                                w.chain_count, w.wide_count, w.chain_queue, cbuf, 1);
 }
 
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
-                  uint32_t* status, cudaStream_t st) {
+                  uint32_t* status, int part, cudaStream_t st) {
     if (g.n_curves == 0) return;
     count_launches(2);
-    k_merge<<<(g.n_curves + 127) / 128, 128, 0, st>>>(g, offs, w.pieces, cbuf, rec, status);
+    const unsigned grid = part == 0 ? (g.n_curves + 127) / 128 : (unsigned)sm_count_hint() / 8;
+    k_merge<<<grid, 128, 0, st>>>(g, offs, w.pieces, cbuf, rec, status, w.curve_wide, w.wide_curves,
+                                  w.wide_curve_count, part);
     k_merge_long<<<sm_count_hint(), 256, 0, st>>>(g, offs, w.pieces, w.long_list, w.list_cap, w.long_count,
-                                                  cbuf, rec);
+                                                  cbuf, rec, w.curve_wide, part);
 }
 
-void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n_cap, const uint32_t* n_dev, uint64_t* keys,
-                     uint8_t* wnp, const DebugOut& dbg, cudaStream_t st) {
-    if (n_cap <= 0) return;
+void launch_fragment(const GeomArgs& g, const int2* rec, const int32_t* offs, int64_t n_cap, const uint32_t* n_dev,
+                     uint64_t* keys, uint8_t* wnp, const DebugOut& dbg, const ChainWork& w, int part,
+                     cudaStream_t st) {
+    if (n_cap <= 0 || g.n_curves == 0) return;
     count_launches(1);
-    k_fragment<<<(unsigned)((n_cap + 255) / 256), 256, 0, st>>>(g, rec, n_cap, n_dev, keys, wnp, dbg);
+    const unsigned grid = part == 0 ? (unsigned)((n_cap + 255) / 256) : (unsigned)sm_count_hint() / 4;
+    k_fragment<<<grid, 256, 0, st>>>(g, rec, offs, n_cap, n_dev, keys, wnp, dbg, w.curve_wide, w.wide_curves,
+                                     w.wide_curve_count, part);
 }
 
 }  // namespace sr

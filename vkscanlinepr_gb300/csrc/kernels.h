@@ -71,6 +71,10 @@ struct ChainWork {
     uint32_t list_cap;
     uint32_t* chain_count;    // [1] zeroed before the count pass
     uint32_t* wide_count;     // [1] chains solved by a whole warp, zeroed before the count pass
+    uint32_t* wide_queue;     // [1] their work-queue counter, zeroed likewise
+    uint8_t* curve_wide;      // [n_curves] 1 for a curve with a wide chain (written by the count pass)
+    uint32_t* wide_curves;    // [n_curves] those curves, in no order
+    uint32_t* wide_curve_count;   // [1] zeroed before the count pass
     uint32_t* chain_queue;    // [1] zeroed before the chains
     uint32_t* long_list;      // [list_cap] (curve << 3 | piece) of long pieces
     uint32_t* long_count;     // [1] zeroed before the count pass
@@ -84,17 +88,23 @@ void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_po
 void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const ChainWork& w, uint32_t* status,
                   cudaStream_t st);
 // Crossing chains (longest first) then the per-curve merge into the
-// reference's intersection records rec[N] (curve, t bits | flags).
-void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count,
+// reference's intersection records rec[N] (curve, t bits | flags).  Each
+// runs in two parts: part 0 of the chains solves the wide chains (a warp
+// each), part 1 the others; part 0 of the merge and of the fragments covers
+// every curve but the wide ones (whose records it marks pending), part 1
+// the wide curves.  Part 1 of the merge must follow part 0 of the merge and
+// of the chains; the two parts may otherwise run on two streams at once.
+void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count, int part,
                    cudaStream_t st);
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
-                  uint32_t* status, cudaStream_t st);
+                  uint32_t* status, int part, cudaStream_t st);
 // One fragment per record: sort key + packed winding bits (4 bits: change,
 // centre part).  With wnp NULL the bits are stored above the key bits of
 // each key instead of in wnp[].
 // n_cap launches the grid; the record count is read from n_dev (offs[C]).
-void launch_fragment(const GeomArgs& g, const int2* rec, int64_t n_cap, const uint32_t* n_dev, uint64_t* keys,
-                     uint8_t* wnp, const DebugOut& dbg, cudaStream_t st);
+void launch_fragment(const GeomArgs& g, const int2* rec, const int32_t* offs, int64_t n_cap, const uint32_t* n_dev,
+                     uint64_t* keys, uint8_t* wnp, const DebugOut& dbg, const ChainWork& w, int part,
+                     cudaStream_t st);
 
 // ---- scan.cu
 // Exclusive scan of n int32 values into out[0..n] (out[n] = total), single
