@@ -253,9 +253,16 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
     int32_t wrun = fe ? ve : wadd(S.warpA[warp], ve);
 
     // ---- flags
+    // From the keys themselves: a key is (path, row rank, x + 1) with the
+    // rank of an off-canvas record Hy - 1, so two records share a cell
+    // exactly when their keys are equal, and share a row of one path when
+    // they agree above the x bits.
     uint32_t ff[kItems], sf[kItems];
     uint64_t bsum = 0;
     const int32_t F = a.F;
+    const uint32_t xbits = a.L.xbits, pshift = a.L.xbits + a.L.rbits;
+    const uint32_t xmask = (1u << xbits) - 1u, rmask = (1u << a.L.rbits) - 1u;
+    const uint32_t off_rank = (uint32_t)(a.L.Hy - 1);
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         int64_t i = ibase + k;
@@ -266,18 +273,18 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         sf[k] = 0;
         if (i >= n) continue;
         int jl = (int)(i - tbase);
-        uint64_t k1 = S.keys[jl + 1];
-        Decoded d1 = unpack_key(a.L, k1);
-        const SceneInfo& si = scene_of_path(a.st, d1.path);
-        bool on = !(d1.x < 0 || d1.y < 0 || d1.x >= si.W || d1.y >= si.H);
-        uint32_t rule = a.fill_rule[d1.path];
+        const uint64_t k1 = S.keys[jl + 1], k0 = S.keys[jl];
+        const uint32_t path1 = (uint32_t)(k1 >> pshift);
+        const uint32_t xo1 = (uint32_t)k1 & xmask, rank1 = (uint32_t)(k1 >> xbits) & rmask;
+        const int32_t Wp = a.st.n_scenes > 1 ? scene_of_path(a.st, path1).W : a.W;
+        // on the canvas: a row of it, and 0 <= x = (xo - 1) F < W
+        const bool on = rank1 != off_rank && xo1 >= 1u && (int32_t)(xo1 - 1u) * F < Wp;
+        uint32_t rule = a.fill_rule[path1];
         if (i == 0) {
             ff[k] = on ? 1u : 0u;
         } else {
-            uint64_t k0 = S.keys[jl];
-            Decoded d0 = unpack_key(a.L, k0);
-            if (on && (d0.path != d1.path || d0.yx != d1.yx)) ff[k] = 1u;
-            if (d0.y == d1.y && wadd(d0.x, F) < d1.x && d0.path == d1.path && rule_pass(rule, wscan)) sf[k] = 1u;
+            if (on && k0 != k1) ff[k] = 1u;
+            if (((k0 ^ k1) >> xbits) == 0 && ((uint32_t)k0 & xmask) + 1u < xo1 && rule_pass(rule, wscan)) sf[k] = 1u;
         }
         if (a.pixel_mode && ff[k]) {
             // centre sample of the merged cell: scan at its first record plus
@@ -310,7 +317,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
             a.dbg_wscan[i] = wscan;
             a.dbg_fflag[i] = (int32_t)ff[k];
             a.dbg_sflag[i] = (int32_t)sf[k];
-            a.dbg_skey[i] = d1.yx;
+            a.dbg_skey[i] = unpack_key(a.L, k1).yx;
         }
         bsum += ((uint64_t)ff[k] << kFragShift) | (uint64_t)sf[k];
     }
@@ -344,6 +351,8 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
     uint64_t brun = S.prefixB + S.warpB[warp] + (inclB - bsum);
 
     // ---- emit draw records (gen_merged_fragment_and_span.comp:155-196)
+    // An emitted record's cell is on the canvas: y = yy F with yy its row
+    // (rank Hy is row 0, rank r < Hy - 1 is row r + 1), x = (xo - 1) F.
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         int64_t i = ibase + k;
@@ -351,31 +360,34 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         brun += ((uint64_t)ff[k] << kFragShift) | (uint64_t)sf[k];
         if (i >= n || !(ff[k] | sf[k])) continue;
         int jl = (int)(i - tbase);
-        Decoded d1 = unpack_key(a.L, S.keys[jl + 1]);
-        int32_t info = (int32_t)a.fill_info[d1.path];
-        const uint32_t row_base = scene_of_path(a.st, d1.path).row_base;
-        if (a.path_draw) atomicAdd(&a.path_draw[d1.path], ff[k] + sf[k]);
+        const uint64_t k1 = S.keys[jl + 1];
+        const uint32_t path1 = (uint32_t)(k1 >> pshift);
+        const uint32_t rank1 = (uint32_t)(k1 >> xbits) & rmask;
+        const int32_t yy = rank1 == (uint32_t)a.L.Hy ? 0 : (int32_t)rank1 + 1;
+        const int32_t y = yy * F, x1 = ((int32_t)((uint32_t)k1 & xmask) - 1) * F;
+        int32_t info = (int32_t)a.fill_info[path1];
+        const uint32_t row = (a.st.n_scenes > 1 ? scene_of_path(a.st, path1).row_base : 0u) + (uint32_t)yy;
+        if (a.path_draw) atomicAdd(&a.path_draw[path1], ff[k] + sf[k]);
         int64_t o = (int64_t)(fb + sb);
         if (ff[k]) {
             if (o < a.draw_capacity) {
-                a.draw[o] = make_int4((int32_t)((uint32_t)d1.y << 16) | d1.x, F, info, (int32_t)(fb + 1));
-                a.draw_row[o] = row_base + (uint32_t)(d1.y / F);
+                a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x1, F, info, (int32_t)(fb + 1));
+                a.draw_row[o] = row;
             } else {
                 set_error(status, ERR_CAPACITY);
             }
             ++o;
         }
         if (sf[k]) {
-            Decoded d0 = unpack_key(a.L, S.keys[jl]);
-            int32_t x0 = imax(0, wadd(d0.x, F));
+            // the span's left cell is in the same row: x0 = its x + F
+            const int32_t x0 = imax(0, wadd(((int32_t)((uint32_t)S.keys[jl] & xmask) - 1) * F, F));
             if (o < a.draw_capacity) {
-                const uint32_t row = row_base + (uint32_t)(d0.y / F);
-                a.draw[o] = make_int4((int32_t)((uint32_t)d0.y << 16) | x0, d1.x - x0, info, 0);
+                a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x0, x1 - x0, info, 0);
                 a.draw_row[o] = row;
                 // a span that hides everything under it ends the resolve's
                 // work before it in each segment it covers whole
                 if (a.seg_cut && (!a.pixel_mode || ((uint32_t)info >> 24) == 255u) && row < a.cut_rows) {
-                    const int32_t s_hi = imin(d1.x / kResolveSeg, (int32_t)a.cut_segs);
+                    const int32_t s_hi = imin(x1 / kResolveSeg, (int32_t)a.cut_segs);
                     for (int32_t sg = (x0 + kResolveSeg - 1) / kResolveSeg; sg < s_hi; ++sg)
                         atomicMax(&a.seg_cut[(size_t)row * a.cut_segs + (uint32_t)sg], (uint32_t)o + 1u);
                 }
