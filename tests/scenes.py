@@ -162,6 +162,16 @@ def long_line(w=9000, h=64):
     return b.arrays()
 
 
+def very_long_piece(w=16000, h=16):
+    """One monotone cubic piece crossing about 16,000 grid columns (more
+    than the long-piece merge keeps in shared memory) and a line back."""
+    b = Builder(w, h)
+    b.path(0, (30, 160, 90, 220))
+    b.curve(CUBIC, [(1.5, 3.5), (5000.25, 5.5), (11000.75, 10.5), (15998.5, 12.5)])
+    b.curve(LINE, [(15998.5, 12.5), (1.5, 3.5)])
+    return b.arrays()
+
+
 ALL = {
     "square": square,
     "star_nonzero": lambda: star(rule=0),
@@ -173,4 +183,5 @@ ALL = {
     "long_chains": long_chains,
     "opaque_layers": opaque_layers,
     "long_line": long_line,
+    "very_long_piece": very_long_piece,
 }

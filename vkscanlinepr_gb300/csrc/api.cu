@@ -278,6 +278,7 @@ struct Pipeline {
         CUDA_TRY(cudaMallocHost(&h_u32, sizeof(uint32_t) * 8));
         CUDA_TRY(cudaMallocHost(&h_u64, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(ctl, sizeof(uint32_t) * CTL_WORDS));
+        CUDA_TRY(sr::geom_init());
         CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
         for (cudaEvent_t* e : {&ev_fork, &ev_merged, &ev_join})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));

@@ -790,70 +790,157 @@ SR_DEV int32_t count_lt(const int32_t* a, int32_t n, float v) {   // elements < 
     return lo;
 }
 
+// A long piece merged by the CTA.  When its two chains fit in shared memory
+// (cap elements) they are merged there: each thread writes one stretch of
+// the output, its start found by a merge-path search (x first on ties), and
+// the flag-OR reads shared memory.  Larger pieces use binary-search ranks in
+// global memory.  Every thread of the CTA calls it with the same piece.
+SR_DEV void merge_long_piece(uint32_t c, int32_t t0, int64_t base, int32_t nx, int32_t ny,
+                             int32_t* __restrict__ cbuf, int2* __restrict__ rec, int32_t* sm, int32_t cap,
+                             int32_t* s_i0) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int32_t L = 1 + nx + ny;
+    const int32_t* X = cbuf + base + 1;
+    const int32_t* Y = X + nx;
+    int2* R = rec + base;
+    if (nx + ny <= cap) {
+        int32_t* sin = sm;
+        int32_t* sout = sm + cap;
+        for (int32_t k = tid; k < nx + ny; k += nt) sin[k] = X[k];
+        __syncthreads();
+        const int32_t* sx = sin;
+        const int32_t* sy = sin + nx;
+        if (nx == 0 || ny == 0) {
+            for (int32_t k = tid; k < L; k += nt) sout[k] = k == 0 ? t0 : sin[k - 1];
+        } else {
+            const int32_t i0 = count_le(sx, nx, bitsf(t0));
+            for (int32_t k = tid; k < i0; k += nt) sout[k] = sx[k];
+            if (tid == 0) sout[i0] = t0;
+            // the merge of sx[i0..nx) with sy: this thread's stretch [d, d_end)
+            const int32_t* xr = sx + i0;
+            const int32_t nxr = nx - i0, M = nxr + ny;
+            const int32_t per = (M + nt - 1) / nt;
+            const int32_t d = imin(tid * per, M), d_end = imin(d + per, M);
+            int32_t lo = imax(0, d - ny), hi = imin(d, nxr);
+            while (lo < hi) {
+                const int32_t mid = (lo + hi) >> 1;
+                if (bitsf(xr[mid]) <= bitsf(sy[d - mid - 1])) lo = mid + 1;
+                else hi = mid;
+            }
+            int32_t ia = lo, ib = d - lo;
+            int32_t* o = sout + i0 + 1;
+            for (int32_t k = d; k < d_end; ++k) {
+                const bool take_x = ia < nxr && (ib >= ny || bitsf(xr[ia]) <= bitsf(sy[ib]));
+                o[k] = take_x ? xr[ia++] : sy[ib++];
+            }
+        }
+        __syncthreads();
+        for (int32_t k = tid; k < L; k += nt) {
+            const int32_t v = sout[k];
+            int32_t acc = v;
+            for (int32_t s2 = k - 1; s2 >= 0; --s2) {
+                const int32_t u = sout[s2];
+                if ((u & ~3) != (v & ~3)) break;
+                acc |= u;
+            }
+            if (k + 1 < L) {
+                const int32_t u = sout[k + 1];
+                if ((u & ~3) == (v & ~3)) acc |= u;
+            }
+            R[k] = make_int2((int32_t)c, acc);
+        }
+        __syncthreads();
+        return;
+    }
+    if (nx == 0 || ny == 0) {
+        const int32_t* S = nx == 0 ? Y : X;
+        for (int32_t k = tid; k < L; k += nt) R[k] = make_int2((int32_t)c, k == 0 ? t0 : S[k - 1]);
+    } else {
+        if (tid == 0) *s_i0 = count_le(X, nx, bitsf(t0));
+        __syncthreads();
+        const int32_t i0 = *s_i0;
+        for (int32_t i = tid; i < nx; i += nt) {
+            int32_t v = X[i];
+            int32_t pos = i < i0 ? i : i0 + 1 + (i - i0) + count_lt(Y, ny, bitsf(v));
+            R[pos] = make_int2((int32_t)c, v);
+        }
+        if (tid == 0) R[i0] = make_int2((int32_t)c, t0);
+        for (int32_t j = tid; j < ny; j += nt) {
+            int32_t v = Y[j];
+            int32_t pos = i0 + 1 + j + count_le(X + i0, nx - i0, bitsf(v));
+            R[pos] = make_int2((int32_t)c, v);
+        }
+    }
+    __syncthreads();
+    int32_t* T = cbuf + base;   // the chains are consumed: reuse as scratch
+    for (int32_t k = tid; k < L; k += nt) {
+        int32_t v = R[k].y, acc = v;
+        for (int32_t s2 = k - 1; s2 >= 0; --s2) {
+            int32_t u = R[s2].y;
+            if ((u & ~3) != (v & ~3)) break;
+            acc |= u;
+        }
+        if (k + 1 < L) {
+            int32_t u = R[k + 1].y;
+            if ((u & ~3) == (v & ~3)) acc |= u;
+        }
+        T[k] = acc;
+    }
+    __syncthreads();
+    for (int32_t k = tid; k < L; k += nt) R[k].y = T[k];
+    __syncthreads();
+}
+
+// Part 0: the long pieces of the list, a CTA each; those of wide curves are
+// marked pending.  Part 1: the wide curves, a CTA each, merging their long
+// pieces.
 __global__ void __launch_bounds__(256) k_merge_long(const GeomArgs g, const int32_t* __restrict__ offs,
                                                     const uint4* __restrict__ pieces,
                                                     const uint32_t* __restrict__ long_list, uint32_t list_cap,
                                                     const uint32_t* __restrict__ long_count,
                                                     int32_t* __restrict__ cbuf, int2* __restrict__ rec,
-                                                    const uint8_t* __restrict__ curve_wide, int part) {
+                                                    const uint8_t* __restrict__ curve_wide,
+                                                    const uint32_t* __restrict__ wide_curves,
+                                                    const uint32_t* __restrict__ wide_curve_count, int part,
+                                                    int32_t cap) {
+    extern __shared__ int32_t sm_long[];   // [cap] chains in, [cap + 1] records out
     __shared__ int32_t s_i0;
-    const uint32_t n_long = imin((int32_t)*long_count, (int32_t)list_cap);
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (uint32_t item = blockIdx.x; item < n_long; item += gridDim.x) {
-        const uint32_t c = long_list[item] >> 3, piece = long_list[item] & 7u;
-        const bool wide = curve_wide[c] != 0;   // the same for the whole CTA
-        if (part == 1 && !wide) continue;
+    if (part == 0) {
+        const uint32_t n_long = imin((int32_t)*long_count, (int32_t)list_cap);
+        for (uint32_t item = blockIdx.x; item < n_long; item += gridDim.x) {
+            const uint32_t c = long_list[item] >> 3, piece = long_list[item] & 7u;
+            const uint4* pt = pieces + (size_t)c * kMaxPieces;
+            int64_t base = offs[c];
+            for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
+            const int32_t nx = piece_nx(pt[piece].x), ny = piece_ny(pt[piece].x);
+            const int32_t L = 1 + nx + ny;
+            if (base + L > g.rec_cap) continue;   // overflow: k_merge reports it
+            if (curve_wide[c]) {   // merged by part 1: mark pending
+                for (int32_t k = tid; k < L; k += nt) rec[base + k] = make_int2(kPendingCurve, 0);
+                continue;
+            }
+            merge_long_piece(c, piece == 0 ? 0 : (int32_t)pt[piece - 1].y, base, nx, ny, cbuf, rec, sm_long, cap,
+                             &s_i0);
+        }
+        return;
+    }
+    const uint32_t nw = imin((int32_t)*wide_curve_count, (int32_t)g.n_curves);
+    for (uint32_t k = blockIdx.x; k < nw; k += gridDim.x) {
+        const uint32_t c = wide_curves[k];
         const uint4* pt = pieces + (size_t)c * kMaxPieces;
         int64_t base = offs[c];
-        for (uint32_t j = 0; j < piece; ++j) base += 1 + piece_nx(pt[j].x) + piece_ny(pt[j].x);
-        const int32_t nx = piece_nx(pt[piece].x), ny = piece_ny(pt[piece].x);
-        const int32_t L = 1 + nx + ny;
-        if (base + L > g.rec_cap) continue;   // overflow: k_merge reports it
-        if (part == 0 && wide) {   // merged by part 1: mark pending
-            for (int32_t k = tid; k < L; k += nt) rec[base + k] = make_int2(kPendingCurve, 0);
-            continue;
+        const int64_t end = offs[c + 1];
+        if (end > g.rec_cap) continue;   // overflow: k_merge reports it
+        for (int j = 0; j < kMaxPieces && base < end; ++j) {
+            const int32_t nx = piece_nx(pt[j].x), ny = piece_ny(pt[j].x);
+            const int32_t L = 1 + nx + ny;
+            if (base + L > end) break;   // k_merge reports the range error
+            if (L >= kLongPiece)
+                merge_long_piece(c, j == 0 ? 0 : (int32_t)pt[j - 1].y, base, nx, ny, cbuf, rec, sm_long, cap,
+                                 &s_i0);
+            base += L;
         }
-        const int32_t t0 = piece == 0 ? 0 : (int32_t)pt[piece - 1].y;
-        const int32_t* X = cbuf + base + 1;
-        const int32_t* Y = X + nx;
-        int2* R = rec + base;
-        if (nx == 0 || ny == 0) {
-            const int32_t* S = nx == 0 ? Y : X;
-            for (int32_t k = tid; k < L; k += nt) R[k] = make_int2((int32_t)c, k == 0 ? t0 : S[k - 1]);
-        } else {
-            if (tid == 0) s_i0 = count_le(X, nx, bitsf(t0));
-            __syncthreads();
-            const int32_t i0 = s_i0;
-            for (int32_t i = tid; i < nx; i += nt) {
-                int32_t v = X[i];
-                int32_t pos = i < i0 ? i : i0 + 1 + (i - i0) + count_lt(Y, ny, bitsf(v));
-                R[pos] = make_int2((int32_t)c, v);
-            }
-            if (tid == 0) R[i0] = make_int2((int32_t)c, t0);
-            for (int32_t j = tid; j < ny; j += nt) {
-                int32_t v = Y[j];
-                int32_t pos = i0 + 1 + j + count_le(X + i0, nx - i0, bitsf(v));
-                R[pos] = make_int2((int32_t)c, v);
-            }
-        }
-        __syncthreads();
-        int32_t* T = cbuf + base;   // the chains are consumed: reuse as scratch
-        for (int32_t k = tid; k < L; k += nt) {
-            int32_t v = R[k].y, acc = v;
-            for (int32_t s = k - 1; s >= 0; --s) {
-                int32_t u = R[s].y;
-                if ((u & ~3) != (v & ~3)) break;
-                acc |= u;
-            }
-            if (k + 1 < L) {
-                int32_t u = R[k + 1].y;
-                if ((u & ~3) == (v & ~3)) acc |= u;
-            }
-            T[k] = acc;
-        }
-        __syncthreads();
-        for (int32_t k = tid; k < L; k += nt) R[k].y = T[k];
-        __syncthreads();
     }
 }
 
@@ -1000,6 +1087,13 @@ void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, i
                                                 w.chain_count, w.wide_count, w.chain_queue, cbuf, 1);
 }
 
+constexpr int32_t kLongCapMain = 3072, kLongCapSide = 12288;
+
+cudaError_t geom_init() {
+    return cudaFuncSetAttribute(k_merge_long, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(int32_t) * (2 * (size_t)kLongCapSide + 1)));
+}
+
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
                   uint32_t* status, int part, cudaStream_t st) {
     if (g.n_curves == 0) return;
@@ -1007,8 +1101,14 @@ void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, in
     const unsigned grid = part == 0 ? (g.n_curves + 127) / 128 : (unsigned)sm_count_hint() / 8;
     k_merge<<<grid, 128, 0, st>>>(g, offs, w.pieces, cbuf, rec, status, w.curve_wide, w.wide_curves,
                                   w.wide_curve_count, part);
-    k_merge_long<<<sm_count_hint(), 256, 0, st>>>(g, offs, w.pieces, w.long_list, w.list_cap, w.long_count,
-                                                  cbuf, rec, w.curve_wide, part);
+    // chains of up to 3 K elements in 25 KB of shared memory (eight CTAs an
+    // SM) on the main stream; up to 12 K on the second stream, whose few
+    // pieces are the longest
+    const int32_t cap = part == 0 ? kLongCapMain : kLongCapSide;
+    const size_t smem = sizeof(int32_t) * (2 * (size_t)cap + 1);
+    k_merge_long<<<part == 0 ? sm_count_hint() : sm_count_hint() / 4, 256, smem, st>>>(
+        g, offs, w.pieces, w.long_list, w.list_cap, w.long_count, cbuf, rec, w.curve_wide, w.wide_curves,
+        w.wide_curve_count, part, cap);
 }
 
 void launch_fragment(const GeomArgs& g, const int2* rec, const int32_t* offs, int64_t n_cap, const uint32_t* n_dev,

@@ -94,6 +94,9 @@ void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const Cha
 // every curve but the wide ones (whose records it marks pending), part 1
 // the wide curves.  Part 1 of the merge must follow part 0 of the merge and
 // of the chains; the two parts may otherwise run on two streams at once.
+// Kernel attributes of the geometry kernels (the long-piece merge's shared
+// memory); once per device before the first frame.
+cudaError_t geom_init();
 void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int sm_count, int part,
                    cudaStream_t st);
 void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, int32_t* cbuf, int2* rec,
