@@ -677,76 +677,74 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
 // stream, writes them; the record-parallel fragment pass skips them.
 constexpr int32_t kPendingCurve = -1;
 
-SR_DEV void merge_curve(const GeomArgs& g, const int32_t* __restrict__ offs, const uint4* __restrict__ pieces,
+// Piece j of curve c, a thread each (pieces are merged independently: each
+// starts from its own t0 and flag state).  The piece-0 thread also checks
+// that the pieces cover the curve's records exactly.
+SR_DEV void merge_piece(const GeomArgs& g, const int32_t* __restrict__ offs, const uint4* __restrict__ pieces,
                         const int32_t* __restrict__ cbuf, int2* __restrict__ rec, uint32_t* __restrict__ status,
-                        uint32_t c, bool pending_only) {
-    int64_t pc = offs[c];
-    const int64_t end = offs[c + 1];
-    if (pc >= end) return;
+                        uint32_t c, int j, bool pending_only) {
+    const int64_t start = offs[c], end = offs[c + 1];
+    if (start >= end) return;
     if (end > g.rec_cap) {
-        set_error(status, ERR_CAPACITY);
+        if (j == 0) set_error(status, ERR_CAPACITY);
         return;
     }
     const uint4* pt = pieces + (size_t)c * kMaxPieces;
+    if (j == 0) {
+        int64_t tot = start;
+        for (int i = 0; i < kMaxPieces && tot < end; ++i) tot += 1 + piece_nx(pt[i].x) + piece_ny(pt[i].x);
+        if (tot != end) set_error(status, ERR_RECORD_RANGE);
+    }
+    int64_t pc = start;
+    for (int i = 0; i < j; ++i) pc += 1 + piece_nx(pt[i].x) + piece_ny(pt[i].x);
+    if (pc >= end) return;   // the curve has fewer pieces
+    const uint4 me = pt[j];
+    const int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
+    const int32_t n_loop = nx + ny + 1;
+    if (pc + n_loop > end) return;   // reported by the piece-0 thread
+    if (n_loop >= kLongPiece) return;   // k_merge_long
+    if (pending_only) {
+        for (int32_t k = 0; k < n_loop; ++k) rec[pc + k] = make_int2(kPendingCurve, 0);
+        return;
+    }
+    const int32_t t0 = j == 0 ? 0 : (int32_t)pt[j - 1].y;   // bits of 0.0f for the first piece
     const int32_t minus_one = fbits(-1.0f);
     const int32_t ex_x = fbits(2.0f), ex_y = fbits(2.0f) | 1;
-    int32_t t0 = 0;   // bits of 0.0f
-    for (int i = 0; i < kMaxPieces && pc < end; ++i) {
-        uint4 me = pt[i];
-        int32_t nx = piece_nx(me.x), ny = piece_ny(me.x);
-        const int32_t* X = cbuf + pc + 1;
-        const int32_t* Y = X + nx;
-        // heads: A = x side, B = y side (make_intersection_1.comp:321-359)
-        int32_t ia = 0, ib = 0;
-        // both sides cross: A = x chain, B = [t0, y chain]; no x crossing:
-        // A empty, B = [t0, y chain]; no y crossing: A = [t0, x chain], B empty
-        const bool a_has_t0 = (nx > 0 && ny == 0);
-        const int32_t lenA = nx + (a_has_t0 ? 1 : 0);
-        const int32_t lenB = a_has_t0 ? 0 : ny + 1;
-        int32_t n_loop = nx + ny + 1;
-        if (pc + n_loop > end) {
-            set_error(status, ERR_RECORD_RANGE);
-            return;
+    const int32_t* X = cbuf + pc + 1;
+    const int32_t* Y = X + nx;
+    // heads: A = x side, B = y side (make_intersection_1.comp:321-359)
+    int32_t ia = 0, ib = 0;
+    // both sides cross: A = x chain, B = [t0, y chain]; no x crossing:
+    // A empty, B = [t0, y chain]; no y crossing: A = [t0, x chain], B empty
+    const bool a_has_t0 = (nx > 0 && ny == 0);
+    const int32_t lenA = nx + (a_has_t0 ? 1 : 0);
+    const int32_t lenB = a_has_t0 ? 0 : ny + 1;
+    int32_t last = minus_one;
+    for (int32_t k = 0; k < n_loop; ++k) {
+        int32_t av = ex_x, bv = ex_y;
+        if (ia < lenA) av = a_has_t0 ? (ia == 0 ? t0 : X[ia - 1]) : X[ia];
+        if (ib < lenB) bv = ib == 0 ? t0 : Y[ib - 1];
+        int32_t out;
+        if (bitsf(av) <= bitsf(bv)) {
+            out = av;
+            ++ia;
+        } else {
+            out = bv;
+            ++ib;
         }
-        if (n_loop >= kLongPiece) {   // k_merge_long
-            pc += n_loop;
-            t0 = (int32_t)me.y;
-            continue;
+        if ((out & ~3) == (last & ~3)) {
+            out |= last;
+            rec[pc - 1] = make_int2((int32_t)c, out);
         }
-        if (pending_only) {
-            for (int32_t k = 0; k < n_loop; ++k) rec[pc + k] = make_int2(kPendingCurve, 0);
-            pc += n_loop;
-            t0 = (int32_t)me.y;
-            continue;
-        }
-        int32_t last = minus_one;
-        for (int32_t k = 0; k < n_loop; ++k) {
-            int32_t av = ex_x, bv = ex_y;
-            if (ia < lenA) av = a_has_t0 ? (ia == 0 ? t0 : X[ia - 1]) : X[ia];
-            if (ib < lenB) bv = ib == 0 ? t0 : Y[ib - 1];
-            int32_t out;
-            if (bitsf(av) <= bitsf(bv)) {
-                out = av;
-                ++ia;
-            } else {
-                out = bv;
-                ++ib;
-            }
-            if ((out & ~3) == (last & ~3)) {
-                out |= last;
-                rec[pc - 1] = make_int2((int32_t)c, out);
-            }
-            rec[pc] = make_int2((int32_t)c, out);
-            last = out;
-            ++pc;
-        }
-        t0 = (int32_t)me.y;
+        rec[pc] = make_int2((int32_t)c, out);
+        last = out;
+        ++pc;
     }
-    if (pc != end) set_error(status, ERR_RECORD_RANGE);
 }
 
 // Part 0 merges every curve but the wide ones, whose records it marks
-// pending; part 1 merges the wide curves once their chains are done.
+// pending; part 1 merges the wide curves once their chains are done.  A
+// thread per (curve, piece).
 __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* __restrict__ offs,
                                                const uint4* __restrict__ pieces, const int32_t* __restrict__ cbuf,
                                                int2* __restrict__ rec, uint32_t* __restrict__ status,
@@ -755,12 +753,14 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
                                                const uint32_t* __restrict__ wide_curve_count, int part) {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (part == 0) {
-        if (tid < g.n_curves) merge_curve(g, offs, pieces, cbuf, rec, status, tid, curve_wide[tid] != 0);
+        const uint32_t c = tid / kMaxPieces;
+        if (c < g.n_curves)
+            merge_piece(g, offs, pieces, cbuf, rec, status, c, (int)(tid % kMaxPieces), curve_wide[c] != 0);
         return;
     }
     const uint32_t nw = imin((int32_t)*wide_curve_count, (int32_t)g.n_curves);
-    for (uint32_t k = tid; k < nw; k += gridDim.x * blockDim.x)
-        merge_curve(g, offs, pieces, cbuf, rec, status, wide_curves[k], false);
+    for (uint32_t k = tid; k < nw * kMaxPieces; k += gridDim.x * blockDim.x)
+        merge_piece(g, offs, pieces, cbuf, rec, status, wide_curves[k / kMaxPieces], (int)(k % kMaxPieces), false);
 }
 
 // Merge of one long piece by a CTA.  The chains are non-decreasing (each
@@ -768,9 +768,9 @@ __global__ void __launch_bounds__(128) k_merge(const GeomArgs g, const int32_t* 
 // piece start t0 may exceed the first roots by less than 4 ulp, so the
 // sequential merge is: the x roots <= t0, then t0, then the stable merge
 // (x first on ties) of the remaining x roots with the y roots.  Each
-// element's slot is its index plus a binary-search rank in the other
-// chain.  The flag-OR of equal t values is then applied per element:
-// record k of a run [s, e] of equal masked t ends as OR(v_s .. v_min(k+1,e)).
+// element's slot is its index plus its rank in the other chain.  The
+// flag-OR of equal t values is then applied per element: record k of a
+// run [s, e] of equal masked t ends as OR(v_s .. v_min(k+1,e)).
 SR_DEV int32_t count_le(const int32_t* a, int32_t n, float v) {   // elements <= v
     int32_t lo = 0, hi = n;
     while (lo < hi) {
@@ -1098,7 +1098,8 @@ void launch_merge(const GeomArgs& g, const int32_t* offs, const ChainWork& w, in
                   uint32_t* status, int part, cudaStream_t st) {
     if (g.n_curves == 0) return;
     count_launches(2);
-    const unsigned grid = part == 0 ? (g.n_curves + 127) / 128 : (unsigned)sm_count_hint() / 8;
+    const unsigned grid = part == 0 ? (unsigned)(((size_t)g.n_curves * kMaxPieces + 127) / 128)
+                                    : (unsigned)sm_count_hint() / 8;
     k_merge<<<grid, 128, 0, st>>>(g, offs, w.pieces, cbuf, rec, status, w.curve_wide, w.wide_curves,
                                   w.wide_curve_count, part);
     // chains of up to 3 K elements in 25 KB of shared memory (eight CTAs an
