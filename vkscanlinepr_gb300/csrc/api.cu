@@ -108,6 +108,7 @@ enum Ctl : int {
     CTL_WIDE = 10,     // chains solved by a whole warp
     CTL_WIDE_QUEUE = 11,    // their work-queue counter
     CTL_WIDE_CURVES = 12,   // curves with such a chain
+    CTL_ROW_SCAN = 13,      // row-start scan's tile counter
     CTL_WORDS = 16,
 };
 
@@ -223,7 +224,7 @@ struct Pipeline {
     DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, chain_sort_scratch, long_list;
     DevBuf curve_wide, wide_curves;
     DevBuf cbuf, rec, keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status, draw, draw_row, totals;
-    DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, seg_cut, image;
+    DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, seg_cut, row_count, row_scan, image;
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
     // learned sizing: per-path curve ranges, draw counters, features,
     // predictions, allotments and their sums
@@ -252,8 +253,8 @@ struct Pipeline {
                          &scenes_d, &cta_base_d, &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status,
                          &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf, &rec, &keys, &keys_alt,
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
-                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &image,
-                         &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
+                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &row_count,
+                         &row_scan, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
                          &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide,
                          &wide_curves};
         for (DevBuf* b : all) release(*b);
@@ -475,6 +476,8 @@ struct Pipeline {
         CUDA_TRY(ensure(totals, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(row_start, sizeof(int32_t) * ((size_t)total_rows + 1)));
         CUDA_TRY(ensure(seg_cut, sizeof(uint32_t) * std::max<size_t>(cut_words(), 1)));
+        CUDA_TRY(ensure(row_count, sizeof(uint32_t) * std::max<size_t>(total_rows, 1)));
+        CUDA_TRY(ensure(row_scan, sizeof(uint64_t) * sr::scan_status_words(total_rows)));
         if (segmented()) CUDA_TRY(ensure(seg_scratch, sr::segsort_scratch_bytes(std::max<uint32_t>(C, 1))));
         return SR_OK;
     }
@@ -570,7 +573,8 @@ struct Pipeline {
                                &ctl, &scan_status, &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf,
                                &rec, &keys, &keys_alt, &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status,
                                &draw, &draw_row, &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt,
-                               &row_sort_scratch, &row_start, &seg_cut, &image, &d_fkey, &d_fwn, &d_fleft,
+                               &row_sort_scratch, &row_start, &seg_cut, &row_count, &row_scan, &image, &d_fkey,
+                               &d_fwn, &d_fleft,
                                &d_wscan,
                                &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
                                &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide, &wide_curves};
@@ -720,16 +724,23 @@ struct Pipeline {
         wa.seg_cut = seg_cut.as<uint32_t>();
         wa.cut_rows = total_rows;
         wa.cut_segs = cut_segs();
+        wa.row_count = row_count.as<uint32_t>();
         CUDA_TRY(cudaMemsetAsync(seg_cut.p, 0, sizeof(uint32_t) * cut_words(), st));
+        CUDA_TRY(cudaMemsetAsync(row_count.p, 0, sizeof(uint32_t) * total_rows, st));
+        CUDA_TRY(cudaMemsetAsync(row_scan.p, 0, sizeof(uint64_t) * sr::scan_status_words(total_rows), st));
         mark(ST_WINDING, false);
         launch_winding_emit(wa, tune.wind_items, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
         mark(ST_WINDING, true);
         SortPlan rp = sort_plan(dcap, bits_for(total_rows), ctlp + CTL_NDRAW);
         mark(ST_ROWSORT, false);
+        // the emit counted the records of every row: their exclusive scan is
+        // each row's start in the row order, and their digits the sort's
+        // histogram
+        launch_exclusive_scan_i32(row_count.as<int32_t>(), row_start.as<int32_t>(), total_rows, row_scan.as<uint64_t>(),
+                                  ctlp + CTL_ROW_SCAN, status, st);
+        sort_hist_from_counts(rp, row_count.as<uint32_t>(), total_rows, row_sort_scratch.p, st);
         launch_sort_u32(rp, draw_row.as<uint32_t>(), nullptr, rkeys.as<uint32_t>(), rvals.as<uint32_t>(),
                         rkeys_alt.as<uint32_t>(), rvals_alt.as<uint32_t>(), row_sort_scratch.p, status, st);
-        launch_row_bounds(rkeys.as<uint32_t>(), dcap, ctlp + CTL_NDRAW, (int32_t)total_rows, row_start.as<int32_t>(),
-                          st);
         mark(ST_ROWSORT, true);
         ResolveArgs ra;
         ra.draw = draw.as<int4>();

@@ -125,6 +125,7 @@ struct SortPlan {
     uint32_t passes;
     uint32_t tiles;
     int items;                 // keys per thread of a tile: 8, 12 or 16
+    int hist_given = 0;        // 1: the digit counts are already in the scratch (sort_hist_from_counts)
 };
 SortPlan sort_plan(int64_t n, uint32_t key_bits, const uint32_t* n_dev = nullptr, int items = 12);
 // Device scratch needed by a plan (bytes).
@@ -136,6 +137,10 @@ size_t sort_scratch_bytes(const SortPlan& p);
 void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                      uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch,
                      uint32_t* status, cudaStream_t st);
+// For keys that are bin indices 0..n_bins-1 whose counts are known: writes
+// each pass's digit counts into the plan's scratch (and sets hist_given on
+// the plan), so the sort skips its own histogram pass over the keys.
+void sort_hist_from_counts(SortPlan& p, const uint32_t* counts, uint32_t n_bins, void* scratch, cudaStream_t st);
 void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, uint32_t* keys_alt, uint32_t* vals_alt, void* scratch,
                      uint32_t* status, cudaStream_t st);
@@ -183,6 +188,7 @@ struct WindArgs {
     // zeroed before the emit, NULL to skip
     uint32_t* seg_cut;
     uint32_t cut_rows, cut_segs;
+    uint32_t* row_count;            // [cut_rows] draw records per global cell row (zeroed before), or NULL
     // parity dumps (NULL in production)
     int32_t* dbg_wscan;             // [N+1]
     int32_t* dbg_fflag;             // [N]

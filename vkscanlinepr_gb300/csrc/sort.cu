@@ -124,6 +124,26 @@ __global__ void __launch_bounds__(kThreads) k_hist(const K* __restrict__ keys, i
     }
 }
 
+// Digit counts of every pass for the keys 0..n_bins-1 with the given counts.
+__global__ void __launch_bounds__(kThreads) k_hist_from_counts(const uint32_t* __restrict__ counts, uint32_t n_bins,
+                                                               uint32_t passes, uint32_t key_bits,
+                                                               uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kMaxPasses][kRadix];
+    for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kThreads) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t b = blockIdx.x * kThreads + threadIdx.x; b < n_bins; b += gridDim.x * kThreads) {
+        const uint32_t c = counts[b];
+        if (!c) continue;
+        for (uint32_t p = 0; p < passes; ++p)
+            atomicAdd(&sh[p][digit_of(b, p * kRadixBits, digit_mask(key_bits, p * kRadixBits))], c);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < passes * kRadix; i += kThreads) {
+        const uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
 // In-place exclusive scan of each pass's 256 digit counts (one CTA per pass).
 __global__ void __launch_bounds__(kRadix) k_hist_scan(uint32_t* hist) {
     __shared__ uint32_t sw[kRadix / 32];
@@ -328,12 +348,18 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
     if (p.n <= 0) return;
     Scratch s = carve(p, scratch);
     size_t lb_words = (size_t)p.passes * ((size_t)p.tiles + 1) * kRadix;
-    cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + 64), st);
+    if (p.hist_given) {
+        cudaMemsetAsync(s.counters, 0, sizeof(uint32_t) * 64, st);
+    } else {
+        cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * (kMaxPasses * kRadix + 64), st);
+    }
     cudaMemsetAsync(s.lookback, 0, sizeof(uint32_t) * lb_words, st);
-    int hb = (int)((p.n + kThreads - 1) / kThreads);
-    if (hb > kHistBlocks) hb = kHistBlocks;
-    count_launches(1);
-    k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.n_dev, p.passes, p.key_bits, s.hist);
+    if (!p.hist_given) {
+        int hb = (int)((p.n + kThreads - 1) / kThreads);
+        if (hb > kHistBlocks) hb = kHistBlocks;
+        count_launches(1);
+        k_hist<K><<<hb, kThreads, 0, st>>>(keys_in, p.n, p.n_dev, p.passes, p.key_bits, s.hist);
+    }
     count_launches(1);
     k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
     const size_t smem = sizeof(OnesweepSmem<K, kVals, ITEMS>);
@@ -383,6 +409,17 @@ void launch_sort_u64(const SortPlan& p, const uint64_t* keys_in, const uint32_t*
                      uint32_t* vals_out, uint64_t* keys_alt, uint32_t* vals_alt, void* scratch, uint32_t* status,
                      cudaStream_t st) {
     sort_dispatch<uint64_t>(p, keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, scratch, status, st);
+}
+
+void sort_hist_from_counts(SortPlan& p, const uint32_t* counts, uint32_t n_bins, void* scratch, cudaStream_t st) {
+    Scratch s = carve(p, scratch);
+    cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, st);
+    int blocks = (int)((n_bins + kThreads - 1) / kThreads);
+    if (blocks > kHistBlocks) blocks = kHistBlocks;
+    if (blocks < 1) blocks = 1;
+    count_launches(1);
+    k_hist_from_counts<<<blocks, kThreads, 0, st>>>(counts, n_bins, p.passes, p.key_bits, s.hist);
+    p.hist_given = 1;
 }
 
 void launch_sort_u32(const SortPlan& p, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,

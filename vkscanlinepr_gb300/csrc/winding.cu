@@ -353,49 +353,65 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
     // ---- emit draw records (gen_merged_fragment_and_span.comp:155-196)
     // An emitted record's cell is on the canvas: y = yy F with yy its row
     // (rank Hy is row 0, rank r < Hy - 1 is row r + 1), x = (xo - 1) F.
+    // The records written per cell row are counted for the row sort; a
+    // thread's records are consecutive, so it adds a run of one row at once.
+    uint32_t run_row = 0, run_cnt = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         int64_t i = ibase + k;
         uint64_t fb = brun >> kFragShift, sb = brun & kSpanMask;
         brun += ((uint64_t)ff[k] << kFragShift) | (uint64_t)sf[k];
-        if (i >= n || !(ff[k] | sf[k])) continue;
-        int jl = (int)(i - tbase);
-        const uint64_t k1 = S.keys[jl + 1];
-        const uint32_t path1 = (uint32_t)(k1 >> pshift);
-        const uint32_t rank1 = (uint32_t)(k1 >> xbits) & rmask;
-        const int32_t yy = rank1 == (uint32_t)a.L.Hy ? 0 : (int32_t)rank1 + 1;
-        const int32_t y = yy * F, x1 = ((int32_t)((uint32_t)k1 & xmask) - 1) * F;
-        int32_t info = (int32_t)a.fill_info[path1];
-        const uint32_t row = (a.st.n_scenes > 1 ? scene_of_path(a.st, path1).row_base : 0u) + (uint32_t)yy;
-        if (a.path_draw) atomicAdd(&a.path_draw[path1], ff[k] + sf[k]);
-        int64_t o = (int64_t)(fb + sb);
-        if (ff[k]) {
-            if (o < a.draw_capacity) {
-                a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x1, F, info, (int32_t)(fb + 1));
-                a.draw_row[o] = row;
-            } else {
-                set_error(status, ERR_CAPACITY);
-            }
-            ++o;
-        }
-        if (sf[k]) {
-            // the span's left cell is in the same row: x0 = its x + F
-            const int32_t x0 = imax(0, wadd(((int32_t)((uint32_t)S.keys[jl] & xmask) - 1) * F, F));
-            if (o < a.draw_capacity) {
-                a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x0, x1 - x0, info, 0);
-                a.draw_row[o] = row;
-                // a span that hides everything under it ends the resolve's
-                // work before it in each segment it covers whole
-                if (a.seg_cut && (!a.pixel_mode || ((uint32_t)info >> 24) == 255u) && row < a.cut_rows) {
-                    const int32_t s_hi = imin(x1 / kResolveSeg, (int32_t)a.cut_segs);
-                    for (int32_t sg = (x0 + kResolveSeg - 1) / kResolveSeg; sg < s_hi; ++sg)
-                        atomicMax(&a.seg_cut[(size_t)row * a.cut_segs + (uint32_t)sg], (uint32_t)o + 1u);
+        uint32_t row = 0, written = 0;
+        if (i < n && (ff[k] | sf[k])) {
+            int jl = (int)(i - tbase);
+            const uint64_t k1 = S.keys[jl + 1];
+            const uint32_t path1 = (uint32_t)(k1 >> pshift);
+            const uint32_t rank1 = (uint32_t)(k1 >> xbits) & rmask;
+            const int32_t yy = rank1 == (uint32_t)a.L.Hy ? 0 : (int32_t)rank1 + 1;
+            const int32_t y = yy * F, x1 = ((int32_t)((uint32_t)k1 & xmask) - 1) * F;
+            int32_t info = (int32_t)a.fill_info[path1];
+            row = (a.st.n_scenes > 1 ? scene_of_path(a.st, path1).row_base : 0u) + (uint32_t)yy;
+            if (a.path_draw) atomicAdd(&a.path_draw[path1], ff[k] + sf[k]);
+            int64_t o = (int64_t)(fb + sb);
+            if (ff[k]) {
+                if (o < a.draw_capacity) {
+                    a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x1, F, info, (int32_t)(fb + 1));
+                    a.draw_row[o] = row;
+                    ++written;
+                } else {
+                    set_error(status, ERR_CAPACITY);
                 }
-            } else {
-                set_error(status, ERR_CAPACITY);
+                ++o;
             }
+            if (sf[k]) {
+                // the span's left cell is in the same row: x0 = its x + F
+                const int32_t x0 = imax(0, wadd(((int32_t)((uint32_t)S.keys[jl] & xmask) - 1) * F, F));
+                if (o < a.draw_capacity) {
+                    a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x0, x1 - x0, info, 0);
+                    a.draw_row[o] = row;
+                    ++written;
+                    // a span that hides everything under it ends the resolve's
+                    // work before it in each segment it covers whole
+                    if (a.seg_cut && (!a.pixel_mode || ((uint32_t)info >> 24) == 255u) && row < a.cut_rows) {
+                        const int32_t s_hi = imin(x1 / kResolveSeg, (int32_t)a.cut_segs);
+                        for (int32_t sg = (x0 + kResolveSeg - 1) / kResolveSeg; sg < s_hi; ++sg)
+                            atomicMax(&a.seg_cut[(size_t)row * a.cut_segs + (uint32_t)sg], (uint32_t)o + 1u);
+                    }
+                } else {
+                    set_error(status, ERR_CAPACITY);
+                }
+            }
+        }
+        if (a.row_count && written != 0 && row < a.cut_rows) {
+            if (run_cnt != 0 && row != run_row) {
+                atomicAdd(&a.row_count[run_row], run_cnt);
+                run_cnt = 0;
+            }
+            run_row = row;
+            run_cnt += written;
         }
     }
+    if (run_cnt != 0) atomicAdd(&a.row_count[run_row], run_cnt);
 }
 
 size_t winding_status_words(int64_t n, int items) {
