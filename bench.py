@@ -9,10 +9,10 @@ winding -> spans/fragments -> RGBA8) on one GB300.  Prints ONE JSON line.
               between timed frames.
   e2e         frames/s through the C ABI with host buffers: every step copies
               the scene from pinned host memory (sr_load_scene) and reads the
-              RGBA8 frame back into pinned host memory (sr_render).  Two
-              renderer contexts on two streams, each driven by its own host
-              thread, keep two frames in flight, so one frame's copies and
-              its chain stage's idle tail overlap the other frame's kernels.
+              RGBA8 frame back into pinned host memory (sr_render).  Three
+              renderer contexts on three streams, each driven by its own host
+              thread, keep three frames in flight, so one frame's copies and
+              its chain stage's idle tail overlap the other frames' kernels.
   roofline    the dominant stage's algorithmic bytes / its CUDA-event time
               against the measured HBM copy bandwidth.
   cpu_baseline  the C++ oracle (the CPU restatement of the reference shaders)
@@ -65,7 +65,7 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="frame4096", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-streams", type=int, default=2,
+    ap.add_argument("--e2e-streams", type=int, default=3,
                     help="frames in flight in the end-to-end leg (one context, stream and host thread each)")
     ap.add_argument("--batch-scenes", type=int, default=4096,
                     help="scenes of the batched workload (0 skips it)")
