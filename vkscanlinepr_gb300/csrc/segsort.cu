@@ -375,9 +375,11 @@ __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __re
 // rounds has its chunks sorted into keys_out (r even) or keys_alt (r odd),
 // and each round flips buffer, so its last round lands in keys_out; rounds
 // past r do nothing for it.
+constexpr int kMergeOut = kTile / 2;   // outputs a merge CTA writes (half a chunk)
+constexpr int kMergeItems = kMergeOut / kThreads;
 struct MergeSmem {
-    uint64_t in[kTile];    // A part then B part of this chunk
-    uint64_t out[kTile];
+    uint64_t in[kMergeOut];    // A part then B part of this half chunk
+    uint64_t out[kMergeOut];
     uint32_t split[4];
 };
 
@@ -418,8 +420,8 @@ __global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__
                                                           uint32_t key_bits, uint32_t n_cap, TileTables u) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MergeSmem& S = *reinterpret_cast<MergeSmem*>(smem_raw);
-    if ((int32_t)blockIdx.x >= u.ntiles[C]) return;
-    const uint4 desc = u.desc[blockIdx.x];
+    if ((int32_t)(blockIdx.x >> 1) >= u.ntiles[C]) return;
+    const uint4 desc = u.desc[blockIdx.x >> 1];
     if (!(desc.z & kChunkBit)) return;
     const uint32_t k = desc.z & 0xFFFFu, rounds = (desc.z >> 16) & 0x7FFFu;
     if (level >= rounds) return;
@@ -427,7 +429,9 @@ __global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__
     uint64_t* dst = ((rounds - level) & 1u) ? keys_out : keys_alt;
     const uint32_t s0 = desc.x, size = desc.y;
     if ((uint64_t)s0 + size > n_cap) return;   // overflowed frame: redone
-    const uint32_t o0 = k * (uint32_t)kTile, o1 = min(o0 + (uint32_t)kTile, size);
+    const uint32_t o0 = k * (uint32_t)kTile + (blockIdx.x & 1u) * (uint32_t)kMergeOut;
+    if (o0 >= size) return;
+    const uint32_t o1 = min(o0 + (uint32_t)kMergeOut, size);
     const uint32_t W = (uint32_t)kTile << level;
     const uint32_t p0 = (o0 / (2 * W)) * (2 * W);
     const uint32_t na = min(W, size - p0);
@@ -454,12 +458,12 @@ __global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__
     for (uint32_t j = tid; j < nB; j += kThreads) S.in[nA + j] = B[ib0 + j];
     __syncthreads();
     // each thread merges kItems outputs from its own split
-    const uint32_t dt = min(tid * (uint32_t)kItems, n);
+    const uint32_t dt = min(tid * (uint32_t)kMergeItems, n);
     const uint64_t* sA = S.in;
     const uint64_t* sB = S.in + nA;
     uint32_t ia = merge_split(sA, nA, sB, nB, dt, kmask);
     uint32_t ib = dt - ia;
-    const uint32_t e = min(dt + (uint32_t)kItems, n);
+    const uint32_t e = min(dt + (uint32_t)kMergeItems, n);
     for (uint32_t o = dt; o < e; ++o) {
         const bool takeA = ib >= nB || (ia < nA && (sA[ia] & kmask) <= (sB[ib] & kmask));
         S.out[o] = takeA ? sA[ia++] : sB[ib++];
@@ -523,7 +527,7 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     const uint32_t n_cap = (uint32_t)cap;
     k_local_sort<<<(unsigned)mt, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap, u);
     for (int lv = 0; lv < levels; ++lv)
-        k_merge_level<<<(unsigned)mt, kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, C, (uint32_t)lv, key_bits,
+        k_merge_level<<<(unsigned)(2 * mt), kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, C, (uint32_t)lv, key_bits,
                                                                          n_cap, u);
 }
 
