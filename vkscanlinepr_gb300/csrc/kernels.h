@@ -1,6 +1,7 @@
 // kernels.h — launch interface between the host orchestration and the
 // device kernels of the scanline renderer.
 #pragma once
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -11,6 +12,18 @@ namespace sr {
 
 // Number of kernels this library has launched in this process.
 void count_launches(uint32_t n);
+// Runs fn (setting a kernel attribute) unless it has already run for
+// `flags` on the current device (one bit per device, up to 32 devices).
+// The bit is set after fn, so no thread skips it before it has taken
+// effect; two threads may both run it, which is harmless.
+template <typename Fn> void once_per_device(std::atomic<uint32_t>& flags, Fn&& fn) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint32_t bit = 1u << (dev & 31);
+    if (flags.load(std::memory_order_acquire) & bit) return;
+    fn();
+    flags.fetch_or(bit, std::memory_order_release);
+}
 uint64_t launches_so_far();
 
 struct Mvp {

@@ -517,12 +517,11 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     k_seg_desc<<<g, 256, 0, st>>>(C, (uint32_t)mt, t, u);
     const uint32_t key_bits = L.pbits + L.rbits + L.xbits;
     const KeyFields kf{L.xbits, L.rbits, L.pbits};
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint32_t> attr{0};
+    once_per_device(attr, [] {
         cudaFuncSetAttribute(k_local_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LocalSmem));
         cudaFuncSetAttribute(k_merge_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
-        attr = true;
-    }
+    });
     count_launches(1 + (uint32_t)levels);
     const uint32_t n_cap = (uint32_t)cap;
     k_local_sort<<<(unsigned)mt, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap, u);

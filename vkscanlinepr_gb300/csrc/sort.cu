@@ -363,11 +363,10 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
     count_launches(1);
     k_hist_scan<<<p.passes, kRadix, 0, st>>>(s.hist);
     const size_t smem = sizeof(OnesweepSmem<K, kVals, ITEMS>);
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<uint32_t> attr_set{0};
+    once_per_device(attr_set, [&] {
         cudaFuncSetAttribute(k_onesweep<K, kVals, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
+    });
     const K* ksrc = keys_in;
     const uint32_t* vsrc = vals_in;
     for (uint32_t pass = 0; pass < p.passes; ++pass) {
