@@ -29,6 +29,33 @@ def test_packed_div255_identity():
     assert np.array_equal((x + 1 + (x >> 8)) >> 8, x // 255)
 
 
+def _perm_4341(x):
+    # __byte_perm(x, 0, 0x4341): bytes 1 and 3 of x to bytes 0 and 2, zeros elsewhere
+    return ((x >> 8) & 0xFF) | (((x >> 24) & 0xFF) << 16)
+
+
+def test_packed_red_blue_blend_equals_source_over():
+    # red in bits 0-7 and blue in bits 16-23 of one word:
+    # u = rb * (255 - a) + ((sr*a + 128) | (sb*a + 128) << 16);
+    # rb' = perm(u + perm(u)) with perm(x) = (x >> 8) & 0x00FF00FF
+    u = np.arange(0, 65026, dtype=np.int64)   # every reachable c*(255-a) + s*a
+    v = u + 128
+    assert (v + (v >> 8)).max() < 2 ** 16      # no half carries into the other
+    assert np.array_equal((v + (v >> 8)) >> 8, (u + 127) // 255)
+    rng = np.random.default_rng(1)
+    n = 200000
+    c_r, c_b, s_r, s_b, a = (rng.integers(0, 256, n) for _ in range(5))
+    a[:256] = np.arange(256)
+    c_r[:256] = 255
+    s_b[:256] = 255
+    rb = c_r | (c_b << 16)
+    uu = rb * (255 - a) + ((s_r * a + 128) | ((s_b * a + 128) << 16))
+    assert uu.max() < 2 ** 32
+    out = _perm_4341(uu + _perm_4341(uu))
+    assert np.array_equal(out & 0xFF, (s_r * a + c_r * (255 - a) + 127) // 255)
+    assert np.array_equal(out >> 16, (s_b * a + c_b * (255 - a) + 127) // 255)
+
+
 def test_oracle_blend_matches_formula_and_keeps_alpha():
     rng = np.random.default_rng(0)
     for _ in range(2000):

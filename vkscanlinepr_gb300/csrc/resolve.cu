@@ -31,11 +31,16 @@ __global__ void k_row_bounds(const uint32_t* __restrict__ srows, int64_t n_cap, 
 
 // ----------------------------------------------------------- pixel mode --
 // Source-over in path order over opaque white: for R, G, B
-//   c' = floor((s*a + c*(255-a) + 127) / 255) = round((s*a + c*(255-a)) / 255),
-// computed on the FMA pipe: u = c*ia + s*a is an exact float (<= 65025),
-// and fma(u, 1/255, 1.5*2^23) - 1.5*2^23 rounds u/255 to the nearest
-// integer exactly for every reachable u (checked exhaustively by the CPU
-// tests).  Alpha stays 255: (255*a + 255*(255-a) + 127) / 255 = 255.
+//   c' = floor((s*a + c*(255-a) + 127) / 255) = round((s*a + c*(255-a)) / 255).
+// Red and blue share one 32-bit word (r in bits 0-7, b in bits 16-23) and
+// blend with integer operations: u = c*ia + s*a + 128 fits each 16-bit
+// half (<= 65153), and c' = (u + (u >> 8)) >> 8 per half, the two shifts
+// being byte permutes (bytes 1 and 3 to 0 and 2); no half carries into the
+// other.  Green blends on the FMA pipe: u = c*ia + s*a is an exact float
+// (<= 65025), and fma(u, 1/255, 1.5*2^23) - 1.5*2^23 rounds u/255 to the
+// nearest integer.  Both forms equal the formula for every reachable u
+// (checked exhaustively by the CPU tests).  Alpha stays 255:
+// (255*a + 255*(255-a) + 127) / 255 = 255.
 constexpr float kRound = 12582912.0f;   // 1.5 * 2^23
 constexpr int kK = kResolveSeg / 32;   // pixels per lane; a warp owns kResolveSeg pixels
 constexpr int kChunk = 512;
@@ -43,17 +48,18 @@ constexpr int kChunk = 512;
 struct PixRec {
     int32_t x0, x1;     // [x0, x1) clipped to >= 0
     float ia;           // 255 - a
-    float sr, sg, sb;   // s*a per channel
+    float sg;           // s*a of green
+    uint32_t iau;       // 255 - a
+    uint32_t sab;       // (s*a + 128) of red | of blue << 16
     int32_t row;        // cell row within the CTA
     uint32_t idx1;      // 1 + draw index
 };
 
-SR_DEV void blend3(float& r, float& g, float& b, const PixRec& q) {
-    const float inv = 1.0f / 255.0f;
-    float ur = __fmaf_rn(r, q.ia, q.sr), ug = __fmaf_rn(g, q.ia, q.sg), ub = __fmaf_rn(b, q.ia, q.sb);
-    r = __fsub_rn(__fmaf_rn(ur, inv, kRound), kRound);
-    g = __fsub_rn(__fmaf_rn(ug, inv, kRound), kRound);
-    b = __fsub_rn(__fmaf_rn(ub, inv, kRound), kRound);
+SR_DEV void blend3(uint32_t& rb, float& g, const PixRec& q) {
+    const uint32_t u = rb * q.iau + q.sab;
+    rb = __byte_perm(u + __byte_perm(u, 0u, 0x4341u), 0u, 0x4341u);
+    const float ug = __fmaf_rn(g, q.ia, q.sg);
+    g = __fsub_rn(__fmaf_rn(ug, 1.0f / 255.0f, kRound), kRound);
 }
 
 uint32_t resolve_rows_per_cta(int32_t W, int warps) {
@@ -126,9 +132,13 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
         const int32_t seg = resolve_seg<WARPS>(w, group) * kResolveSeg;
         const bool live = w.active && seg < W;
         const uint32_t cut = resolve_cut(a, w, seg, live);
-        float r[kK], g[kK], b[kK];
+        uint32_t rb[kK];
+        float g[kK];
 #pragma unroll
-        for (int j = 0; j < kK; ++j) r[j] = g[j] = b[j] = 255.0f;
+        for (int j = 0; j < kK; ++j) {
+            rb[j] = 0x00FF00FFu;
+            g[j] = 255.0f;
+        }
         for (int32_t c0 = beg; c0 < end; c0 += kChunk) {
             const int32_t cnt = imin(kChunk, end - c0);
             __syncthreads();
@@ -142,9 +152,9 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
                 pr.x1 = wadd(x, d.y);
                 uint32_t col = (uint32_t)d.z, al = col >> 24;
                 pr.ia = (float)(255u - al);
-                pr.sr = (float)((col & 0xFFu) * al);
                 pr.sg = (float)(((col >> 8) & 0xFFu) * al);
-                pr.sb = (float)(((col >> 16) & 0xFFu) * al);
+                pr.iau = 255u - al;
+                pr.sab = ((col & 0xFFu) * al + 128u) | ((((col >> 16) & 0xFFu) * al + 128u) << 16);
                 pr.row = (d.x >> 16) / a.F - w.r0;
                 sq[q] = pr;
             }
@@ -167,24 +177,24 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
                         const int j = off >> 5;
                         if (lane == (off & 31)) {
                             switch (j) {
-                                case 0: blend3(r[0], g[0], b[0], pr); break;
-                                case 1: blend3(r[1], g[1], b[1], pr); break;
-                                case 2: blend3(r[2], g[2], b[2], pr); break;
-                                case 3: blend3(r[3], g[3], b[3], pr); break;
-                                case 4: blend3(r[4], g[4], b[4], pr); break;
-                                case 5: blend3(r[5], g[5], b[5], pr); break;
-                                case 6: blend3(r[6], g[6], b[6], pr); break;
-                                default: blend3(r[7], g[7], b[7], pr); break;
+                                case 0: blend3(rb[0], g[0], pr); break;
+                                case 1: blend3(rb[1], g[1], pr); break;
+                                case 2: blend3(rb[2], g[2], pr); break;
+                                case 3: blend3(rb[3], g[3], pr); break;
+                                case 4: blend3(rb[4], g[4], pr); break;
+                                case 5: blend3(rb[5], g[5], pr); break;
+                                case 6: blend3(rb[6], g[6], pr); break;
+                                default: blend3(rb[7], g[7], pr); break;
                             }
                         }
                     } else if (pr.x0 <= seg && pr.x1 >= seg + kResolveSeg) {
 #pragma unroll
-                        for (int j = 0; j < kK; ++j) blend3(r[j], g[j], b[j], pr);
+                        for (int j = 0; j < kK; ++j) blend3(rb[j], g[j], pr);
                     } else {
 #pragma unroll
                         for (int j = 0; j < kK; ++j) {
                             int32_t p = seg + lane + 32 * j;
-                            if (p >= pr.x0 && p < pr.x1) blend3(r[j], g[j], b[j], pr);
+                            if (p >= pr.x0 && p < pr.x1) blend3(rb[j], g[j], pr);
                         }
                     }
                 }
@@ -196,8 +206,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
             for (int j = 0; j < kK; ++j) {
                 int32_t p = seg + lane + 32 * j;
                 if (p < W) {
-                    uint32_t v = (uint32_t)__float2int_rn(r[j]) | ((uint32_t)__float2int_rn(g[j]) << 8) |
-                                 ((uint32_t)__float2int_rn(b[j]) << 16) | 0xFF000000u;
+                    uint32_t v = rb[j] | ((uint32_t)__float2int_rn(g[j]) << 8) | 0xFF000000u;
                     out[p] = v;
                 }
             }
