@@ -219,7 +219,10 @@ struct Pipeline {
     uint64_t total_pixels = 0;
     std::vector<sr::SceneInfo> info;
     std::vector<uint32_t> cta_base;
+    std::vector<uint8_t> cta_narrow;
+    bool any_narrow = false;
     DevBuf pos, pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info, path_scene, scenes_d, cta_base_d;
+    DevBuf cta_narrow_d;
     // frame
     DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, chain_sort_scratch, long_list;
     DevBuf curve_wide, wide_curves;
@@ -256,7 +259,7 @@ struct Pipeline {
                          &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &row_count,
                          &row_scan, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
                          &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide,
-                         &wide_curves};
+                         &wide_curves, &cta_narrow_d};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : {ev_fork, ev_merged, ev_join})
             if (e) cudaEventDestroy(e);
@@ -315,6 +318,8 @@ struct Pipeline {
         Wmax = 1;
         Hmax = 1;
         cta_base.assign(S + 1, 0);
+        cta_narrow.clear();
+        any_narrow = false;
         for (uint32_t s = 0; s < S; ++s) {
             sr::SceneInfo& si = info[s];
             si.rows = (uint32_t)((si.H + F - 1) / F);
@@ -327,6 +332,8 @@ struct Pipeline {
             cta_base[s] = res_ctas;
             uint32_t rpc = sr::resolve_rows_per_cta(si.W, tune.resolve_warps);
             res_ctas += (si.rows + rpc - 1) / rpc;
+            cta_narrow.resize(res_ctas, rpc > 1 ? 1 : 0);
+            any_narrow = any_narrow || rpc > 1;
         }
         cta_base[S] = res_ctas;
         CUDA_TRY(ensure(scenes_d, sizeof(sr::SceneInfo) * std::max<uint32_t>(S, 1)));
@@ -334,6 +341,8 @@ struct Pipeline {
         CUDA_TRY(ensure(image, 4 * std::max<uint64_t>(total_pixels, 1)));
         if (S) CUDA_TRY(cudaMemcpy(scenes_d.p, info.data(), sizeof(sr::SceneInfo) * S, cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMemcpy(cta_base_d.p, cta_base.data(), sizeof(uint32_t) * (S + 1), cudaMemcpyHostToDevice));
+        CUDA_TRY(ensure(cta_narrow_d, std::max<size_t>(res_ctas, 1)));
+        if (res_ctas) CUDA_TRY(cudaMemcpy(cta_narrow_d.p, cta_narrow.data(), res_ctas, cudaMemcpyHostToDevice));
         return SR_OK;
     }
 
@@ -577,7 +586,8 @@ struct Pipeline {
                                &d_fwn, &d_fleft,
                                &d_wscan,
                                &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
-                               &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide, &wide_curves};
+                               &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide, &wide_curves,
+                               &cta_narrow_d};
         uint64_t t = 0;
         for (const DevBuf* b : all) t += b->cap;
         return t;
@@ -755,6 +765,8 @@ struct Pipeline {
         ra.image = image.as<uint32_t>();
         ra.seg_cut = seg_cut.as<uint32_t>();
         ra.cut_segs = cut_segs();
+        ra.cta_narrow = cta_narrow_d.as<uint8_t>();
+        ra.any_narrow = any_narrow ? 1 : 0;
         mark(ST_RESOLVE, false);
         launch_resolve(ra, res_ctas, st);
         mark(ST_RESOLVE, true);
@@ -1029,6 +1041,8 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     ra.image = p.image.as<uint32_t>();
     ra.seg_cut = nullptr;
     ra.cut_segs = 0;
+    ra.cta_narrow = p.cta_narrow_d.as<uint8_t>();
+    ra.any_narrow = p.any_narrow ? 1 : 0;
     sr::launch_resolve(ra, p.res_ctas, st);
     CUDA_TRY(cudaGetLastError());
     p.last_O = n;

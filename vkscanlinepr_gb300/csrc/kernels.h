@@ -229,6 +229,8 @@ struct ResolveArgs {
     uint32_t* image;                  // all scenes' RGBA8 framebuffers
     const uint32_t* seg_cut;          // [rows][cut_segs] from the emit, or NULL
     uint32_t cut_segs;
+    const uint8_t* cta_narrow;        // [CTAs] 1 for a CTA of several rows
+    int any_narrow;                   // some CTA is (then pixel mode runs a second kernel for them)
 };
 // Pixels per warp of a resolve CTA.
 constexpr int kResolveSeg = 256;

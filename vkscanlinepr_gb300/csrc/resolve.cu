@@ -120,8 +120,110 @@ template <int WARPS> SR_DEV int32_t resolve_seg(const ResolveWork& w, int group)
     return w.segs >= kResolveWarps ? group * kResolveWarps + warp : warp % w.segs;
 }
 
+SR_DEV PixRec pix_rec(const int4 d, uint32_t di) {
+    PixRec pr;
+    pr.idx1 = di + 1u;
+    const int32_t x = d.x & 0xFFFF;
+    pr.x0 = x;
+    pr.x1 = wadd(x, d.y);
+    const uint32_t col = (uint32_t)d.z, al = col >> 24;
+    pr.ia = (float)(255u - al);
+    pr.sg = (float)(((col >> 8) & 0xFFu) * al);
+    pr.iau = 255u - al;
+    pr.sab = ((col & 0xFFu) * al + 128u) | ((((col >> 16) & 0xFFu) * al + 128u) << 16);
+    pr.row = 0;
+    return pr;
+}
+
+// A record on this warp's segment: a one-pixel record is a uniform branch on
+// its register slot; a record over the whole segment blends every slot;
+// otherwise each lane tests its pixels.
+SR_DEV void apply_pix(const PixRec& pr, int32_t seg, int lane, uint32_t (&rb)[kK], float (&g)[kK]) {
+    if (pr.x1 - pr.x0 == 1) {
+        const int32_t off = pr.x0 - seg;
+        const int j = off >> 5;
+        if (lane == (off & 31)) {
+            switch (j) {
+                case 0: blend3(rb[0], g[0], pr); break;
+                case 1: blend3(rb[1], g[1], pr); break;
+                case 2: blend3(rb[2], g[2], pr); break;
+                case 3: blend3(rb[3], g[3], pr); break;
+                case 4: blend3(rb[4], g[4], pr); break;
+                case 5: blend3(rb[5], g[5], pr); break;
+                case 6: blend3(rb[6], g[6], pr); break;
+                default: blend3(rb[7], g[7], pr); break;
+            }
+        }
+    } else if (pr.x0 <= seg && pr.x1 >= seg + kResolveSeg) {
+#pragma unroll
+        for (int j = 0; j < kK; ++j) blend3(rb[j], g[j], pr);
+    } else {
+#pragma unroll
+        for (int j = 0; j < kK; ++j) {
+            int32_t p = seg + lane + 32 * j;
+            if (p >= pr.x0 && p < pr.x1) blend3(rb[j], g[j], pr);
+        }
+    }
+}
+
+// A CTA of several short rows (a canvas narrower than WARPS segments): each
+// warp streams its own row's records 32 at a time through its own
+// shared-memory slots, without waiting for the other warps.
+template <int WARPS>
+SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, PixRec* sq) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int32_t seg = resolve_seg<WARPS>(w, 0) * kResolveSeg;
+    if (!w.active || seg >= w.W) return;
+    const uint32_t cut = resolve_cut(a, w, seg, true);
+    uint32_t rb[kK];
+    float g[kK];
+#pragma unroll
+    for (int j = 0; j < kK; ++j) {
+        rb[j] = 0x00FF00FFu;
+        g[j] = 255.0f;
+    }
+    PixRec* my = sq + warp * 32;
+    const uint32_t r = w.si->row_base + (uint32_t)(w.r0 + w.my_row);
+    const int32_t beg = a.row_start[r], end = a.row_start[r + 1];
+    for (int32_t c0 = beg; c0 < end; c0 += 32) {
+        const int32_t q = c0 + lane;
+        bool ov = false;
+        if (q < end) {
+            const uint32_t di = a.row_sorted_idx[q];
+            const PixRec pr = pix_rec(a.draw[di], di);
+            ov = pr.x0 < seg + kResolveSeg && pr.x1 > seg && pr.idx1 >= cut;
+            if (ov) my[lane] = pr;
+        }
+        uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
+        __syncwarp();
+        while (m) {
+            const PixRec pr = my[__ffs(m) - 1];
+            m &= m - 1;
+            apply_pix(pr, seg, lane, rb, g);
+        }
+        __syncwarp();
+    }
+    uint32_t* out = a.image + w.si->image_off + (size_t)(w.r0 + w.my_row) * w.W;
+#pragma unroll
+    for (int j = 0; j < kK; ++j) {
+        int32_t p = seg + lane + 32 * j;
+        if (p < w.W) out[p] = rb[j] | ((uint32_t)__float2int_rn(g[j]) << 8) | 0xFF000000u;
+    }
+}
+
+// The CTAs of several rows (canvases narrower than WARPS segments); the
+// row-per-CTA kernel below skips them.  The two kernels run one after the
+// other over the same grid.
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel_rows(const ResolveArgs a) {
+    __shared__ PixRec sq[WARPS * 32];
+    if (!a.cta_narrow[blockIdx.x]) return;
+    resolve_pixel_rows<WARPS>(a, resolve_work<WARPS>(a), sq);
+}
+
 template <int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs a) {
+    if (a.any_narrow && a.cta_narrow[blockIdx.x]) return;   // k_resolve_pixel_rows
     __shared__ PixRec sq[kChunk];
     const ResolveWork w = resolve_work<WARPS>(a);
     const int tid = threadIdx.x, lane = tid & 31;
@@ -292,12 +394,21 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
 void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st) {
     if (n_ctas == 0) return;
     count_launches(1);
+    if (a.pixel_mode && a.any_narrow) count_launches(1);
     if (a.warps == 8) {
-        if (a.pixel_mode) k_resolve_pixel<8><<<n_ctas, 32 * 8, 0, st>>>(a);
-        else k_resolve_ref<8><<<n_ctas, 32 * 8, 0, st>>>(a);
+        if (a.pixel_mode) {
+            k_resolve_pixel<8><<<n_ctas, 32 * 8, 0, st>>>(a);
+            if (a.any_narrow) k_resolve_pixel_rows<8><<<n_ctas, 32 * 8, 0, st>>>(a);
+        } else {
+            k_resolve_ref<8><<<n_ctas, 32 * 8, 0, st>>>(a);
+        }
     } else {
-        if (a.pixel_mode) k_resolve_pixel<16><<<n_ctas, 32 * 16, 0, st>>>(a);
-        else k_resolve_ref<16><<<n_ctas, 32 * 16, 0, st>>>(a);
+        if (a.pixel_mode) {
+            k_resolve_pixel<16><<<n_ctas, 32 * 16, 0, st>>>(a);
+            if (a.any_narrow) k_resolve_pixel_rows<16><<<n_ctas, 32 * 16, 0, st>>>(a);
+        } else {
+            k_resolve_ref<16><<<n_ctas, 32 * 16, 0, st>>>(a);
+        }
     }
 }
 
