@@ -149,9 +149,9 @@ SR_DEV uint32_t chain_key(int32_t len, uint32_t type) {
     return ((14u - lg) << 2) | cls;
 }
 SR_DEV bool chain_key_long(uint32_t key) { return (key >> 2) <= 14u - 5u; }   // >= 32 crossings
-// Cubic and quadric chains of >= 256 bisected roots (class >= 8) are solved
+// Cubic and quadric chains of >= 512 bisected roots (class >= 9) are solved
 // by a whole warp each (run_chain_warp); they sort before every other chain.
-SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 8u && (key & 3u) != 2u; }
+SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 9u && (key & 3u) != 2u; }
 constexpr uint32_t kChainKeyBits = 6;
 
 // get_xy_begin_end_delta + udpate_cut_range for one axis
