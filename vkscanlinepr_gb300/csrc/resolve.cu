@@ -43,7 +43,7 @@ __global__ void k_row_bounds(const uint32_t* __restrict__ srows, int64_t n_cap, 
 // (255*a + 255*(255-a) + 127) / 255 = 255.
 constexpr float kRound = 12582912.0f;   // 1.5 * 2^23
 constexpr int kK = kResolveSeg / 32;   // pixels per lane; a warp owns kResolveSeg pixels
-constexpr int kChunk = 512;
+constexpr int kChunk = 1024;
 
 struct PixRec {
     int32_t x0, x1;     // [x0, x1) clipped to >= 0
