@@ -148,7 +148,6 @@ SR_DEV uint32_t chain_key(int32_t len, uint32_t type) {
     uint32_t cls = type == 4u ? 0u : (type == 3u ? 1u : 2u);
     return ((14u - lg) << 2) | cls;
 }
-SR_DEV bool chain_key_long(uint32_t key) { return (key >> 2) <= 14u - 5u; }   // >= 32 crossings
 // Cubic and quadric chains of >= 512 bisected roots (class >= 9) are solved
 // by a whole warp each (run_chain_warp); they sort before every other chain.
 SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 9u && (key & 3u) != 2u; }
@@ -390,42 +389,24 @@ SR_DEV float mid_rn(float lo, float hi) { return __fmul_rn(__fadd_rn(lo, hi), 0.
 // solve: a step goes right exactly when (v < c) == s0, whatever the other
 // steps did.  Both solvers below rest on that.
 
-// 24-step bisection of the reference (make_intersection_1.comp:402-434).
-// kSpec evaluates both possible next midpoints with the current one, so
-// two steps cost one dependent curve evaluation; the values and decisions
-// are exactly those of the one-step loop.
-template <int kType, bool kSpec>
+// 24-step bisection of the reference (make_intersection_1.comp:402-434), a
+// thread per chain.  (Evaluating both possible next midpoints with each one
+// halves the dependent depth, but the chains left to this solver are
+// throughput-bound, and the extra evaluations made the frame slower.)
+template <int kType>
 SR_DEV float bisect(const AxisPoly& a, float c, float t_min, float t_max) {
     const float v0 = eval_axis<kType>(a, t_min);
     const bool s0 = v0 < c;
     float ta = t_min, tb = t_max;
     float t_solve = t_min, last = 0.0f;
-    if (kSpec) {
-#pragma unroll 2
-        for (int j = 0; j < 12; ++j) {
-            const float tm = mid_rn(ta, tb);
-            const float mL = mid_rn(ta, tm), mR = mid_rn(tm, tb);
-            const float v = eval_axis<kType>(a, tm);
-            const float vL = eval_axis<kType>(a, mL);
-            const float vR = eval_axis<kType>(a, mR);
-            const bool r1 = (v < c) == s0, rL = (vL < c) == s0, rR = (vR < c) == s0;
-            t_solve = r1 ? mR : mL;
-            last = r1 ? vR : vL;
-            const float na = r1 ? (rR ? mR : tm) : (rL ? mL : ta);
-            const float nb = r1 ? (rR ? tb : mR) : (rL ? tm : mL);
-            ta = na;
-            tb = nb;
-        }
-    } else {
 #pragma unroll 4
-        for (int j = 0; j < 24; ++j) {
-            const float tm = mid_rn(ta, tb);
-            const float v = eval_axis<kType>(a, tm);
-            t_solve = tm;
-            last = v;
-            if ((v < c) == s0) ta = tm;
-            else tb = tm;
-        }
+    for (int j = 0; j < 24; ++j) {
+        const float tm = mid_rn(ta, tb);
+        const float v = eval_axis<kType>(a, tm);
+        t_solve = tm;
+        last = v;
+        if ((v < c) == s0) ta = tm;
+        else tb = tm;
     }
     // vt0 == c returns t_min at once; a solve that ends more than one unit
     // away from c falls back to t_min too
@@ -433,7 +414,7 @@ SR_DEV float bisect(const AxisPoly& a, float c, float t_min, float t_max) {
     return t_solve;
 }
 
-template <int kType, bool kSpec>
+template <int kType>
 SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t_lo, float t_hi, int side,
                       int32_t* __restrict__ out) {
     float lo = t_lo;
@@ -447,7 +428,7 @@ SR_DEV void run_chain(const AxisPoly& a, int32_t len, float x, float dx, float t
         x = __fadd_rn(x, dx);
         float t;
         if (kType == 2) t = gmin(gmax(__fmul_rn(__fsub_rn(c, a.p0), inv), lo), t_hi);
-        else t = bisect<kType, kSpec>(a, c, lo, t_hi);
+        else t = bisect<kType>(a, c, lo, t_hi);
         int32_t ob = (fbits(t) & ~3) | side;
         out[k] = ob;
         lo = bitsf(ob);
@@ -652,18 +633,12 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
         if (first >= total) break;
         const uint32_t it = first + lane;
         if (it >= total) continue;
-        const bool spec = chain_key_long(keys[it]);
         const ChainSetup s = chain_setup(g, offs, pieces, items[it]);
         if (s.base + s.len > g.rec_cap) continue;   // overflow: k_merge reports it
         int32_t* out = cbuf + s.base;
-        if (s.type == 2u) run_chain<2, false>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
-        else if (s.type == 3u) {
-            if (spec) run_chain<3, true>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
-            else run_chain<3, false>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
-        } else {
-            if (spec) run_chain<4, true>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
-            else run_chain<4, false>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
-        }
+        if (s.type == 2u) run_chain<2>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
+        else if (s.type == 3u) run_chain<3>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
+        else run_chain<4>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
     }
 }
 
