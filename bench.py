@@ -47,7 +47,7 @@ L2_FLUSH_BYTES = 256 << 20
 # What bounds each stage's main kernel (profiles/ncu_top_kernels_frame4096.md):
 # the HBM fraction is the roofline only for the stages that move bytes.
 LIMITS = {
-    "resolve": "instruction issue: 6.3 G pixel-blends x 7 integer and FP32 ops, DRAM 1%",
+    "resolve": "latency of each segment's walk back to its collapse cut and of the record gathers",
     "chains": "the dependent bisection steps of the longest crossing chains",
     "wide": "the longest chain's bisection rounds (lane exchange latency), beside the rest of the frame",
     "sort": "shared-memory ranking latency of the tile sort and merge rounds",

@@ -172,6 +172,52 @@ def very_long_piece(w=16000, h=16):
     return b.arrays()
 
 
+def translucent_layers(w=1300, h=48):
+    """Runs of translucent layers over whole 256-pixel resolve segments between
+    shapes that cover part of a segment.  A run whose composed blend sends
+    every colour to one (a few layers of alpha 0.4 and more) lets the
+    renderer start painting there; runs of alpha 1-3 never do; one run is
+    longer than the 32 records a warp holds, and the last segment is 20
+    pixels wide."""
+    rng = np.random.default_rng(11)
+    b = Builder(w, h)
+    full = [(-1, -1), (w + 1, -1), (w + 1, h + 1), (-1, h + 1)]
+
+    def rgb():
+        return tuple(int(v) for v in rng.integers(0, 256, 3))
+
+    def layer(lo, hi):
+        b.path(0, rgb() + (int(rng.integers(lo, hi)),)).polygon(full)
+
+    def shape():
+        x, y, r = float(rng.uniform(0, w)), float(rng.uniform(0, h)), float(rng.uniform(3, 300))
+        b.path(int(rng.integers(2)), rgb() + (int(rng.integers(60, 256)),)).polygon(
+            [(x - r, y - 0.3 * r), (x + 0.7 * r, y - 0.4 * r), (x + 0.1 * r, y + 0.9 * r)])
+
+    for _ in range(3):
+        layer(102, 255)
+    shape()
+    for _ in range(40):
+        layer(102, 255)
+    shape()
+    for _ in range(40):
+        layer(1, 4)
+    shape()
+    shape()
+    for _ in range(5):
+        layer(1, 4)
+    shape()
+    for _ in range(6):
+        for _ in range(int(rng.integers(1, 8))):
+            layer(102, 255)
+        shape()
+    b.path(0, (10, 20, 30, 200)).polygon([(256, -1), (w + 1, -1), (w + 1, h + 1), (256, h + 1)])
+    b.path(0, (200, 20, 30, 230)).polygon([(1280, -1), (w + 1, -1), (w + 1, h + 1), (1280, h + 1)])
+    for _ in range(3):
+        layer(1, 3)
+    return b.arrays()
+
+
 ALL = {
     "square": square,
     "star_nonzero": lambda: star(rule=0),
@@ -184,4 +230,5 @@ ALL = {
     "opaque_layers": opaque_layers,
     "long_line": long_line,
     "very_long_piece": very_long_piece,
+    "translucent_layers": translucent_layers,
 }

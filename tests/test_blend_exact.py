@@ -68,3 +68,35 @@ def test_oracle_blend_matches_formula_and_keeps_alpha():
             sc, dc = (s >> (8 * ch)) & 255, (d >> (8 * ch)) & 255
             assert (got >> (8 * ch)) & 255 == (sc * a + dc * (255 - a) + 127) // 255
         assert got >> 24 == 255
+
+
+def _blend(c, s, a):
+    return (s * a + c * (255 - a) + 127) // 255
+
+
+def test_blend_is_monotone_in_the_old_value():
+    # every (s, a): c -> blend(c) never decreases, so a composition of blends
+    # sends every colour between what it sends 0 and 255 to
+    c = np.arange(256, dtype=np.int64)
+    s = np.arange(256, dtype=np.int64)[:, None, None]
+    a = np.arange(256, dtype=np.int64)[None, :, None]
+    v = _blend(c[None, None, :], s, a)
+    assert np.all(np.diff(v, axis=2) >= 0)
+
+
+def test_collapsed_runs_send_every_colour_to_one():
+    # the resolve starts a segment at a run of whole-segment layers whose
+    # composition sends 0 and 255 to one value: check it sends all 256 there
+    rng = np.random.default_rng(5)
+    hits = 0
+    for _ in range(4000):
+        n = int(rng.integers(1, 12))
+        s = rng.integers(0, 256, n)
+        a = rng.integers(1, 256, n)
+        c = np.arange(256, dtype=np.int64)
+        for k in range(n):
+            c = _blend(c, int(s[k]), int(a[k]))
+        if c[0] == c[255]:
+            hits += 1
+            assert np.all(c == c[0])
+    assert hits > 500

@@ -227,7 +227,7 @@ struct Pipeline {
     DevBuf tpos, path_visible, cut, count, offs, ctl, scan_status, pieces, chain_lists, chain_sort_scratch, long_list;
     DevBuf curve_wide, wide_curves;
     DevBuf cbuf, rec, keys, keys_alt, wnp, skeys, svals, vals_alt, sort_scratch, wind_status, draw, draw_row, totals;
-    DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, seg_cut, row_count, row_scan, image;
+    DevBuf rkeys, rvals, rkeys_alt, rvals_alt, row_sort_scratch, row_start, seg_cut, row_count, row_px, row_scan, image;
     DevBuf d_fkey, d_fwn, d_fleft, d_wscan, d_fflag, d_sflag, d_skey;
     // learned sizing: per-path curve ranges, draw counters, features,
     // predictions, allotments and their sums
@@ -256,7 +256,7 @@ struct Pipeline {
                          &scenes_d, &cta_base_d, &tpos, &path_visible, &cut, &count, &offs, &ctl, &scan_status,
                          &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf, &rec, &keys, &keys_alt,
                          &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status, &draw, &draw_row, &totals,
-                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &row_count,
+                         &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &row_count, &row_px,
                          &row_scan, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
                          &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide,
                          &wide_curves, &cta_narrow_d};
@@ -486,6 +486,7 @@ struct Pipeline {
         CUDA_TRY(ensure(row_start, sizeof(int32_t) * ((size_t)total_rows + 1)));
         CUDA_TRY(ensure(seg_cut, sizeof(uint32_t) * std::max<size_t>(cut_words(), 1)));
         CUDA_TRY(ensure(row_count, sizeof(uint32_t) * std::max<size_t>(total_rows, 1)));
+        CUDA_TRY(ensure(row_px, sizeof(unsigned long long) * std::max<size_t>(total_rows, 1)));
         CUDA_TRY(ensure(row_scan, sizeof(uint64_t) * sr::scan_status_words(total_rows)));
         if (segmented()) CUDA_TRY(ensure(seg_scratch, sr::segsort_scratch_bytes(std::max<uint32_t>(C, 1))));
         return SR_OK;
@@ -582,7 +583,7 @@ struct Pipeline {
                                &ctl, &scan_status, &pieces, &chain_lists, &chain_sort_scratch, &long_list, &cbuf,
                                &rec, &keys, &keys_alt, &wnp, &skeys, &svals, &vals_alt, &sort_scratch, &wind_status,
                                &draw, &draw_row, &totals, &rkeys, &rvals, &rkeys_alt, &rvals_alt,
-                               &row_sort_scratch, &row_start, &seg_cut, &row_count, &row_scan, &image, &d_fkey,
+                               &row_sort_scratch, &row_start, &seg_cut, &row_count, &row_px, &row_scan, &image, &d_fkey,
                                &d_fwn, &d_fleft,
                                &d_wscan,
                                &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw, &feats, &preds, &allot,
@@ -735,8 +736,10 @@ struct Pipeline {
         wa.cut_rows = total_rows;
         wa.cut_segs = cut_segs();
         wa.row_count = row_count.as<uint32_t>();
+        wa.row_px = row_px.as<unsigned long long>();
         CUDA_TRY(cudaMemsetAsync(seg_cut.p, 0, sizeof(uint32_t) * cut_words(), st));
         CUDA_TRY(cudaMemsetAsync(row_count.p, 0, sizeof(uint32_t) * total_rows, st));
+        CUDA_TRY(cudaMemsetAsync(row_px.p, 0, sizeof(unsigned long long) * total_rows, st));
         CUDA_TRY(cudaMemsetAsync(row_scan.p, 0, sizeof(uint64_t) * sr::scan_status_words(total_rows), st));
         mark(ST_WINDING, false);
         launch_winding_emit(wa, tune.wind_items, wind_status.as<uint64_t>(), ctlp + CTL_WIND_COUNTER, status, st);
@@ -765,6 +768,7 @@ struct Pipeline {
         ra.image = image.as<uint32_t>();
         ra.seg_cut = seg_cut.as<uint32_t>();
         ra.cut_segs = cut_segs();
+        ra.row_px = row_px.as<unsigned long long>();
         ra.cta_narrow = cta_narrow_d.as<uint8_t>();
         ra.any_narrow = any_narrow ? 1 : 0;
         mark(ST_RESOLVE, false);
@@ -1041,6 +1045,7 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     ra.image = p.image.as<uint32_t>();
     ra.seg_cut = nullptr;
     ra.cut_segs = 0;
+    ra.row_px = nullptr;
     ra.cta_narrow = p.cta_narrow_d.as<uint8_t>();
     ra.any_narrow = p.any_narrow ? 1 : 0;
     sr::launch_resolve(ra, p.res_ctas, st);

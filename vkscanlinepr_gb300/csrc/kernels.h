@@ -202,6 +202,7 @@ struct WindArgs {
     uint32_t* seg_cut;
     uint32_t cut_rows, cut_segs;
     uint32_t* row_count;            // [cut_rows] draw records per global cell row (zeroed before), or NULL
+    unsigned long long* row_px;     // [cut_rows] pixels of a row's records (widths summed; zeroed before), or NULL
     // parity dumps (NULL in production)
     int32_t* dbg_wscan;             // [N+1]
     int32_t* dbg_fflag;             // [N]
@@ -228,6 +229,7 @@ struct ResolveArgs {
     int32_t warps;                    // warps per CTA: 8 or 16
     uint32_t* image;                  // all scenes' RGBA8 framebuffers
     const uint32_t* seg_cut;          // [rows][cut_segs] from the emit, or NULL
+    const unsigned long long* row_px; // [rows] summed record widths from the emit, or NULL (every row searched)
     uint32_t cut_segs;
     const uint8_t* cta_narrow;        // [CTAs] 1 for a CTA of several rows
     int any_narrow;                   // some CTA is (then pixel mode runs a second kernel for them)

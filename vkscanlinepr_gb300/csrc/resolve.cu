@@ -7,9 +7,11 @@
 // records land in draw order.  Reference mode overwrites (blending is off in
 // the reference pipeline); pixel mode composites source-over with integer
 // arithmetic.  Draw records are first sorted stably by cell row (onesweep),
-// so each CTA owns one cell row, keeps it in shared memory, and applies the
-// row's records in path order; a thread owns a fixed set of pixels, so no
-// barrier is needed between records.
+// so a CTA owns one cell row (or several short ones), stages its records in
+// shared memory, and applies them in path order; a thread owns a fixed set
+// of pixels, so no barrier is needed between records.  In pixel mode a warp
+// first finds where its 256-pixel segment's painting may start (the
+// collapse cut below) and skips the records before it.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -55,7 +57,8 @@ struct PixRec {
     uint32_t idx1;      // 1 + draw index
 };
 
-SR_DEV void blend3(uint32_t& rb, float& g, const PixRec& q) {
+// q: a record's iau, sab, ia and sg (a PixRec or a RunRec).
+template <class Rec> SR_DEV void blend3(uint32_t& rb, float& g, const Rec& q) {
     const uint32_t u = rb * q.iau + q.sab;
     rb = __byte_perm(u + __byte_perm(u, 0u, 0x4341u), 0u, 0x4341u);
     const float ug = __fmaf_rn(g, q.ia, q.sg);
@@ -166,43 +169,134 @@ SR_DEV void apply_pix(const PixRec& pr, int32_t seg, int lane, uint32_t (&rb)[kK
     }
 }
 
-// A CTA of several short rows (a canvas narrower than WARPS segments): each
-// warp streams its own row's records 32 at a time through its own
-// shared-memory slots, without waiting for the other warps.
-template <int WARPS>
-SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, PixRec* sq) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int32_t seg = resolve_seg<WARPS>(w, 0) * kResolveSeg;
-    if (!w.active || seg >= w.W) return;
-    const uint32_t cut = resolve_cut(a, w, seg, true);
-    uint32_t rb[kK];
-    float g[kK];
+// Where a segment's painting may start.  Every pixel-blend is monotone in
+// the pixel's old value (c' = floor((s*a + c*(255-a) + 127) / 255)), and so
+// is any composition of them.  If a run of records that each cover the whole
+// segment maps 0 and 255 to the same value in R, G and B, it maps every
+// value there: the segment holds one colour after the run whatever it held
+// before, so painting from white at the run's first record gives the same
+// pixels as painting from the row's first record.  With alpha >= 0.4 a run
+// of a handful of layers usually does this; an opaque span is a run of one.
+// A warp walks the last kChunk records of its row from the end back,
+// collects each run of whole-segment records between records that cover
+// only part of the segment (the latest 32 of a longer run), and lane t
+// tests the run's suffix from its record t: the latest start that collapses
+// is the cut.  Without one the segment is painted from the row's start.
+// The walk costs about a pass over the records it reads, so it is skipped
+// for rows of fewer than kSearchLayers layers a pixel (record widths summed
+// by the emit, over the row's width): a cut needs a run of several whole-
+// segment layers and saves little there.
+constexpr unsigned kSearchLayers = 32;
+
+SR_DEV bool row_searched(const ResolveArgs& a, uint32_t r, int32_t W) {
+    return !a.row_px || a.row_px[r] >= (unsigned long long)kSearchLayers * (unsigned long long)W;
+}
+
+struct RunRec {
+    uint32_t iau, sab;
+    float ia, sg;
+};
+
+SR_DEV RunRec run_rec(const PixRec& p) {
+    RunRec r;
+    r.iau = p.iau;
+    r.sab = p.sab;
+    r.ia = p.ia;
+    r.sg = p.sg;
+    return r;
+}
+
+// A warp's run of whole-segment records, in draw order with the latest at
+// [31], and their positions.
+struct RunBuf {
+    RunRec rec[32];
+    int32_t pos[32];
+};
+
+// The latest position among the n held records from which the run to [31]
+// sends 0 and 255 to one colour, or -1.
+SR_DEV int32_t run_collapse(const RunBuf& buf, int n, int lane) {
+    uint32_t lo_rb = 0u, hi_rb = 0x00FF00FFu;
+    float lo_g = 0.0f, hi_g = 255.0f;
+    for (int k = 32 - n; k < 32; ++k) {
+        const RunRec r = buf.rec[k];
+        if (k >= lane) {
+            blend3(lo_rb, lo_g, r);
+            blend3(hi_rb, hi_g, r);
+        }
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, lane >= 32 - n && lo_rb == hi_rb && lo_g == hi_g);
+    return m ? buf.pos[31 - __clz(m)] : -1;
+}
+
+// The run bookkeeping of a backward walk: feed() takes 32 records at a time
+// (latest lane first), each overlapping the segment or not and covering all
+// of it or not.
+struct RunWalk {
+    int n = 0;          // records of the current run held
+    bool full = false;  // the held run filled the buffer and did not collapse
+    int32_t cut = -1;
+
+    // Returns true once a cut is found.  Covers above the highest record
+    // over part of the segment extend the current run; that record ends it;
+    // the covers below it start the next run, and so on.  A run's records
+    // enter the buffer together, each lane at its rank from the top.
+    SR_DEV bool feed(uint32_t mo, uint32_t mc, const PixRec& mine, int32_t pos, int lane, RunBuf& buf) {
+        uint32_t mp = mo & ~mc;
+        for (;;) {
+            const uint32_t above = mp ? ~((2u << (31 - __clz(mp))) - 1u) : 0xFFFFFFFFu;
+            const uint32_t run = mc & above;
+            if (run && !full) {
+                const int rank = n + __popc(run & ~((2u << lane) - 1u));
+                if (((run >> lane) & 1u) && rank < 32) {
+                    buf.rec[31 - rank] = run_rec(mine);
+                    buf.pos[31 - rank] = pos;
+                }
+                __syncwarp();
+                n += __popc(run);
+                if (n >= 32) {
+                    n = 32;
+                    cut = run_collapse(buf, n, lane);
+                    if (cut >= 0) return true;
+                    full = true;
+                }
+            }
+            if (!mp) return false;
+            if (close(lane, buf)) return true;
+            mc &= ~above;
+            mp &= ~above & ((1u << (31 - __clz(mp))) - 1u);
+            if (!mc) return false;
+        }
+    }
+
+    SR_DEV bool close(int lane, RunBuf& buf) {
+        if (n && !full) {
+            cut = run_collapse(buf, n, lane);
+            if (cut >= 0) return true;
+        }
+        n = 0;
+        full = false;
+        return false;
+    }
+};
+
+SR_DEV void stage_pix(const ResolveArgs& a, PixRec* sq, int32_t c0, int32_t cnt) {
+    for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+        const uint32_t di = a.row_sorted_idx[c0 + q];
+        sq[q] = pix_rec(a.draw[di], di);
+    }
+}
+
+SR_DEV void init_pix(uint32_t (&rb)[kK], float (&g)[kK]) {
 #pragma unroll
     for (int j = 0; j < kK; ++j) {
         rb[j] = 0x00FF00FFu;
         g[j] = 255.0f;
     }
-    PixRec* my = sq + warp * 32;
-    const uint32_t r = w.si->row_base + (uint32_t)(w.r0 + w.my_row);
-    const int32_t beg = a.row_start[r], end = a.row_start[r + 1];
-    for (int32_t c0 = beg; c0 < end; c0 += 32) {
-        const int32_t q = c0 + lane;
-        bool ov = false;
-        if (q < end) {
-            const uint32_t di = a.row_sorted_idx[q];
-            const PixRec pr = pix_rec(a.draw[di], di);
-            ov = pr.x0 < seg + kResolveSeg && pr.x1 > seg && pr.idx1 >= cut;
-            if (ov) my[lane] = pr;
-        }
-        uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
-        __syncwarp();
-        while (m) {
-            const PixRec pr = my[__ffs(m) - 1];
-            m &= m - 1;
-            apply_pix(pr, seg, lane, rb, g);
-        }
-        __syncwarp();
-    }
+}
+
+SR_DEV void store_pix(const ResolveArgs& a, const ResolveWork& w, int32_t seg, int lane, const uint32_t (&rb)[kK],
+                      const float (&g)[kK]) {
     uint32_t* out = a.image + w.si->image_off + (size_t)(w.r0 + w.my_row) * w.W;
 #pragma unroll
     for (int j = 0; j < kK; ++j) {
@@ -211,108 +305,152 @@ SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, PixRe
     }
 }
 
-// The CTAs of several rows (canvases narrower than WARPS segments); the
-// row-per-CTA kernel below skips them.  The two kernels run one after the
-// other over the same grid.
+// A CTA of several short rows (a canvas narrower than WARPS segments): each
+// warp finds its cut and streams its own row's records 32 at a time through
+// its own shared-memory slots, without waiting for the other warps.
+SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, int32_t seg, PixRec* slot, RunBuf& buf) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t r = w.si->row_base + (uint32_t)(w.r0 + w.my_row);
+    const int32_t beg = a.row_start[r], end = a.row_start[r + 1];
+    const int32_t segend = imin(seg + kResolveSeg, w.W);
+    const uint32_t cut = resolve_cut(a, w, seg, true);
+    int32_t start = beg;
+    if (row_searched(a, r, w.W)) {
+        RunWalk rw;
+        const int32_t lim = imax(beg, end - kChunk);
+        bool found = false;
+        for (int32_t c1 = end; c1 > lim && !found; c1 -= 32) {
+            const int32_t q = c1 - 32 + lane;
+            bool ov = false, cover = false;
+            PixRec pr;
+            if (q >= lim) {
+                const uint32_t di = a.row_sorted_idx[q];
+                pr = pix_rec(a.draw[di], di);
+                ov = pr.x0 < seg + kResolveSeg && pr.x1 > seg;
+                cover = pr.x0 <= seg && pr.x1 >= segend;
+            }
+            found = rw.feed(__ballot_sync(0xFFFFFFFFu, ov), __ballot_sync(0xFFFFFFFFu, cover), pr, q, lane, buf);
+        }
+        if (found || rw.close(lane, buf)) start = rw.cut;
+    }
+    uint32_t rb[kK];
+    float g[kK];
+    init_pix(rb, g);
+    for (int32_t c0 = start; c0 < end; c0 += 32) {
+        const int32_t q = c0 + lane;
+        bool ov = false;
+        if (q < end) {
+            const uint32_t di = a.row_sorted_idx[q];
+            const PixRec pr = pix_rec(a.draw[di], di);
+            ov = pr.x0 < seg + kResolveSeg && pr.x1 > seg && pr.idx1 >= cut;
+            if (ov) slot[lane] = pr;
+        }
+        uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
+        __syncwarp();
+        while (m) {
+            const PixRec p = slot[__ffs(m) - 1];
+            m &= m - 1;
+            apply_pix(p, seg, lane, rb, g);
+        }
+        __syncwarp();
+    }
+    store_pix(a, w, seg, lane, rb, g);
+}
+
+// CTAs of several rows (canvases narrower than WARPS segments) run the path
+// above in their own kernel, with little shared memory; the kernel below
+// skips them.  The two run one after the other over the same grid.
+//
+// A CTA per cell row (a canvas of at least half as many segments as the CTA
+// has warps; warps beyond the row's segments idle): the row's last kChunk
+// records are staged once, every warp finds its segment's cut in them, and the CTA
+// stages from the earliest cut on (chunks end-aligned, so the last one is
+// the chunk already staged); a warp skips the records before its own cut.
 template <int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel_rows(const ResolveArgs a) {
-    __shared__ PixRec sq[WARPS * 32];
+    __shared__ PixRec slots[WARPS * 32];
+    __shared__ RunBuf bufs[WARPS];
     if (!a.cta_narrow[blockIdx.x]) return;
-    resolve_pixel_rows<WARPS>(a, resolve_work<WARPS>(a), sq);
+    const ResolveWork w = resolve_work<WARPS>(a);
+    const int warp = threadIdx.x >> 5;
+    if (w.active) resolve_pixel_rows(a, w, resolve_seg<WARPS>(w, 0) * kResolveSeg, slots + warp * 32, bufs[warp]);
 }
 
 template <int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs a) {
     if (a.any_narrow && a.cta_narrow[blockIdx.x]) return;   // k_resolve_pixel_rows
     __shared__ PixRec sq[kChunk];
+    __shared__ RunBuf bufs[WARPS];
+    __shared__ int32_t cta_start[2];   // by group parity: a warp may still read the last group's
     const ResolveWork w = resolve_work<WARPS>(a);
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t W = w.W;
-    const uint32_t gr0 = w.si->row_base + (uint32_t)w.r0;
-    const int32_t beg = a.row_start[gr0], end = a.row_start[gr0 + (uint32_t)w.nr];
+    const uint32_t r = w.si->row_base + (uint32_t)w.r0;
+    const int32_t beg = a.row_start[r], end = a.row_start[r + 1];
+    const int32_t tail0 = imax(beg, end - kChunk);
+    const bool search = row_searched(a, r, W);
+    bool tail_staged = false;   // sq holds [tail0, end)
+    if (search) {
+        stage_pix(a, sq, tail0, end - tail0);
+        tail_staged = true;
+    }
     for (int group = 0; group < w.groups; ++group) {
         const int32_t seg = resolve_seg<WARPS>(w, group) * kResolveSeg;
-        const bool live = w.active && seg < W;
+        const bool live = w.active && seg < W;   // a row of fewer segments than warps leaves some idle
+        int32_t start = beg, s0 = beg;
+        if (search) {
+            if (threadIdx.x == 0) cta_start[group & 1] = end;
+            __syncthreads();
+            if (live) {
+                const int32_t segend = imin(seg + kResolveSeg, W);
+                RunWalk rw;
+                bool found = false;
+                for (int32_t c1 = end - tail0; c1 > 0 && !found; c1 -= 32) {
+                    const int32_t i = c1 - 32 + lane;
+                    bool ov = false, cover = false;
+                    if (i >= 0) {
+                        const int32_t x0 = sq[i].x0, x1 = sq[i].x1;
+                        ov = x0 < seg + kResolveSeg && x1 > seg;
+                        cover = x0 <= seg && x1 >= segend;
+                    }
+                    found = rw.feed(__ballot_sync(0xFFFFFFFFu, ov), __ballot_sync(0xFFFFFFFFu, cover),
+                                    sq[i < 0 ? 0 : i], tail0 + i, lane, bufs[warp]);
+                }
+                if (found || rw.close(lane, bufs[warp])) start = rw.cut;
+                if (lane == 0) atomicMin(&cta_start[group & 1], start);
+            }
+            __syncthreads();
+            s0 = cta_start[group & 1];
+        }
         const uint32_t cut = resolve_cut(a, w, seg, live);
         uint32_t rb[kK];
         float g[kK];
-#pragma unroll
-        for (int j = 0; j < kK; ++j) {
-            rb[j] = 0x00FF00FFu;
-            g[j] = 255.0f;
-        }
-        for (int32_t c0 = beg; c0 < end; c0 += kChunk) {
-            const int32_t cnt = imin(kChunk, end - c0);
-            __syncthreads();
-            for (int q = tid; q < cnt; q += blockDim.x) {
-                const uint32_t di = a.row_sorted_idx[c0 + q];
-                int4 d = a.draw[di];
-                PixRec pr;
-                pr.idx1 = di + 1u;
-                int32_t x = d.x & 0xFFFF;
-                pr.x0 = x;
-                pr.x1 = wadd(x, d.y);
-                uint32_t col = (uint32_t)d.z, al = col >> 24;
-                pr.ia = (float)(255u - al);
-                pr.sg = (float)(((col >> 8) & 0xFFu) * al);
-                pr.iau = 255u - al;
-                pr.sab = ((col & 0xFFu) * al + 128u) | ((((col >> 16) & 0xFFu) * al + 128u) << 16);
-                pr.row = (d.x >> 16) / a.F - w.r0;
-                sq[q] = pr;
+        init_pix(rb, g);
+        const int32_t nchunks = (end - s0 + kChunk - 1) / kChunk;
+        for (int k = nchunks - 1; k >= 0; --k) {
+            const int32_t c0 = imax(s0, end - (k + 1) * kChunk), c1 = end - k * kChunk;
+            const int32_t base = k ? c0 : tail0;
+            if (k || !tail_staged) {
+                __syncthreads();
+                stage_pix(a, sq, base, c1 - base);
+                __syncthreads();
+                tail_staged = k == 0;
             }
-            __syncthreads();
             if (!live) continue;
-            for (int32_t g0 = 0; g0 < cnt; g0 += 32) {
+            const int32_t hi = c1 - base;
+            for (int32_t g0 = imax(c0, start) - base; g0 < hi; g0 += 32) {
                 const int32_t qi = g0 + lane;
                 bool ov = false;
-                if (qi < cnt)
-                    ov = sq[qi].row == w.my_row && sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg &&
-                         sq[qi].idx1 >= cut;
+                if (qi < hi) ov = sq[qi].x0 < seg + kResolveSeg && sq[qi].x1 > seg && sq[qi].idx1 >= cut;
                 uint32_t m = __ballot_sync(0xFFFFFFFFu, ov);
                 while (m) {
-                    const int q = g0 + __ffs(m) - 1;
+                    const PixRec pr = sq[g0 + __ffs(m) - 1];
                     m &= m - 1;
-                    const PixRec pr = sq[q];
-                    if (pr.x1 - pr.x0 == 1) {
-                        // one pixel: a uniform branch on its register slot
-                        const int32_t off = pr.x0 - seg;
-                        const int j = off >> 5;
-                        if (lane == (off & 31)) {
-                            switch (j) {
-                                case 0: blend3(rb[0], g[0], pr); break;
-                                case 1: blend3(rb[1], g[1], pr); break;
-                                case 2: blend3(rb[2], g[2], pr); break;
-                                case 3: blend3(rb[3], g[3], pr); break;
-                                case 4: blend3(rb[4], g[4], pr); break;
-                                case 5: blend3(rb[5], g[5], pr); break;
-                                case 6: blend3(rb[6], g[6], pr); break;
-                                default: blend3(rb[7], g[7], pr); break;
-                            }
-                        }
-                    } else if (pr.x0 <= seg && pr.x1 >= seg + kResolveSeg) {
-#pragma unroll
-                        for (int j = 0; j < kK; ++j) blend3(rb[j], g[j], pr);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < kK; ++j) {
-                            int32_t p = seg + lane + 32 * j;
-                            if (p >= pr.x0 && p < pr.x1) blend3(rb[j], g[j], pr);
-                        }
-                    }
+                    apply_pix(pr, seg, lane, rb, g);
                 }
             }
         }
-        if (live) {
-            uint32_t* out = a.image + w.si->image_off + (size_t)(w.r0 + w.my_row) * W;
-#pragma unroll
-            for (int j = 0; j < kK; ++j) {
-                int32_t p = seg + lane + 32 * j;
-                if (p < W) {
-                    uint32_t v = rb[j] | ((uint32_t)__float2int_rn(g[j]) << 8) | 0xFF000000u;
-                    out[p] = v;
-                }
-            }
-        }
+        if (live) store_pix(a, w, seg, lane, rb, g);
     }
 }
 

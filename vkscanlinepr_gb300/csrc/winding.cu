@@ -353,15 +353,16 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
     // ---- emit draw records (gen_merged_fragment_and_span.comp:155-196)
     // An emitted record's cell is on the canvas: y = yy F with yy its row
     // (rank Hy is row 0, rank r < Hy - 1 is row r + 1), x = (xo - 1) F.
-    // The records written per cell row are counted for the row sort; a
-    // thread's records are consecutive, so it adds a run of one row at once.
-    uint32_t run_row = 0, run_cnt = 0;
+    // The records written per cell row are counted for the row sort, and
+    // their pixels summed for the resolve; a thread's records are
+    // consecutive, so it adds a run of one row at once.
+    uint32_t run_row = 0, run_cnt = 0, run_px = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         int64_t i = ibase + k;
         uint64_t fb = brun >> kFragShift, sb = brun & kSpanMask;
         brun += ((uint64_t)ff[k] << kFragShift) | (uint64_t)sf[k];
-        uint32_t row = 0, written = 0;
+        uint32_t row = 0, written = 0, px = 0;
         if (i < n && (ff[k] | sf[k])) {
             int jl = (int)(i - tbase);
             const uint64_t k1 = S.keys[jl + 1];
@@ -378,6 +379,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
                     a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x1, F, info, (int32_t)(fb + 1));
                     a.draw_row[o] = row;
                     ++written;
+                    px += (uint32_t)F;
                 } else {
                     set_error(status, ERR_CAPACITY);
                 }
@@ -390,6 +392,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
                     a.draw[o] = make_int4((int32_t)((uint32_t)y << 16) | x0, x1 - x0, info, 0);
                     a.draw_row[o] = row;
                     ++written;
+                    px += (uint32_t)imax(x1 - x0, 0);
                     // a span that hides everything under it ends the resolve's
                     // work before it in each segment it covers whole
                     if (a.seg_cut && (!a.pixel_mode || ((uint32_t)info >> 24) == 255u) && row < a.cut_rows) {
@@ -405,13 +408,19 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         if (a.row_count && written != 0 && row < a.cut_rows) {
             if (run_cnt != 0 && row != run_row) {
                 atomicAdd(&a.row_count[run_row], run_cnt);
+                if (a.row_px) atomicAdd(&a.row_px[run_row], (unsigned long long)run_px);
                 run_cnt = 0;
+                run_px = 0;
             }
             run_row = row;
             run_cnt += written;
+            run_px += px;
         }
     }
-    if (run_cnt != 0) atomicAdd(&a.row_count[run_row], run_cnt);
+    if (run_cnt != 0) {
+        atomicAdd(&a.row_count[run_row], run_cnt);
+        if (a.row_px) atomicAdd(&a.row_px[run_row], (unsigned long long)run_px);
+    }
 }
 
 size_t winding_status_words(int64_t n, int items) {
