@@ -191,7 +191,10 @@ def stage_bytes(st, n_curves, n_points, W, H):
         # sorted keys in; draw records (16 B) and their cell rows (4 B) out
         "winding_emit": N * 8 + O * (16 + 4),
         "row_sort": O * 4 + row_passes * O * 2 * (4 + 4),
-        "resolve": O * (4 + 16) + W * H * 4,
+        # the image written and the row starts; a segment also reads the draw
+        # records after its collapse cut (about 6% of them in the 4096^2
+        # frame), which depend on the scene and are left out
+        "resolve": W * H * 4 + (H + 1) * 4,
         # the wide chains and their curves' merge and fragments, on a second
         # stream beside chains, merge and fragment (their bytes are counted there)
         "wide": 0,
