@@ -218,6 +218,29 @@ def translucent_layers(w=1300, h=48):
     return b.arrays()
 
 
+def deep_tail(w=2304, h=8):
+    """Rows of about 1,300 records over nine resolve segments: 40 translucent
+    full-canvas layers, 1,200 thin shapes in the first segment, then 10 layers
+    over the other segments.  Those segments find their cut among the last
+    records; the first finds none in the last 1,024, so the row is painted
+    from its start in several staged chunks, and the CTA's two groups of
+    segments share them."""
+    rng = np.random.default_rng(23)
+    b = Builder(w, h)
+
+    def rgba(lo):
+        return tuple(int(v) for v in rng.integers(0, 256, 3)) + (int(rng.integers(lo, 255)),)
+
+    for _ in range(40):
+        b.path(0, rgba(102)).polygon([(-1, -1), (w + 1, -1), (w + 1, h + 1), (-1, h + 1)])
+    for k in range(1200):
+        x = 0.2 * (k % 1200) + 0.25
+        b.path(int(rng.integers(2)), rgba(60)).polygon([(x, -1), (x + 1.5, -1), (x + 1.5, h + 1), (x, h + 1)])
+    for _ in range(10):
+        b.path(0, rgba(200)).polygon([(256, -1), (w + 1, -1), (w + 1, h + 1), (256, h + 1)])
+    return b.arrays()
+
+
 ALL = {
     "square": square,
     "star_nonzero": lambda: star(rule=0),
@@ -231,4 +254,5 @@ ALL = {
     "long_line": long_line,
     "very_long_piece": very_long_piece,
     "translucent_layers": translucent_layers,
+    "deep_tail": deep_tail,
 }

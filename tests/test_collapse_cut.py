@@ -204,3 +204,9 @@ def test_mask_walk_finds_the_record_walk_cut():
             a = rng.randint(1, 4) if low_alpha and rng.random() < 0.7 else rng.randint(1, 255)
             recs.append((ov, cv, rng.randint(0, 0xFFFFFF) | (a << 24)))
         assert mask_walk(recs) == record_walk(recs)
+
+
+def test_painting_from_the_cut_equals_the_oracle_deep_tail(oracle_lib):
+    # segments without a cut in the row's last 1,024 records beside ones with
+    cuts = _check_scene(oracle_lib, scenes.to_oracle(scenes.deep_tail()))
+    assert 0 < cuts < 8 * 9
