@@ -172,7 +172,7 @@ class ClockSampler:
 
 
 def stage_bytes(st, n_curves, n_points, W, H):
-    """Algorithmic bytes per stage for one frame (see DESIGN.md)."""
+    """Algorithmic bytes per stage for one frame."""
     N = st["n_intersections"]
     O = st["n_draw_records"]
     passes = st["sort_passes"]

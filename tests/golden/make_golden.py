@@ -10,9 +10,11 @@
                            SHA-256 of every stage the oracle produces for the
                            seeded synthetic scenes and the hand-made scenes
 
-Run from the repository root in a checkout that has the reference at
-/root/reference (only this script reads it; the fixtures it writes travel
-with the repository):  python tests/golden/make_golden.py
+Run from the repository root; the mock draw lists are read from the
+reference's workdir given as the argument (only this script reads it; the
+fixtures it writes travel with the repository):
+
+  python tests/golden/make_golden.py [<reference>/workdir]
 """
 import hashlib
 import json
@@ -29,7 +31,6 @@ sys.path.insert(0, os.path.dirname(HERE))
 import oracle  # noqa: E402
 import scenes  # noqa: E402
 
-REF = "/root/reference/workdir"
 STAGES = ["curve_count", "curve_offset", "intersection", "frag_key", "frag_winding", "sorted_key",
           "sorted_index", "winding_scan", "frag_flag", "span_flag", "draw_list", "image"]
 
@@ -46,7 +47,7 @@ def frame_record(scene, mode, **kw):
     return rec
 
 
-def main():
+def main(ref=None):
     out = {"synthetic": {}, "handmade": {}}
     for name, (preset, seed, w, h, p) in {"star1024_seed0": (0, 0, 0, 0, 0),
                                            "mixed1000x750_seed7": (1, 7, 1000, 750, 1500)}.items():
@@ -63,10 +64,10 @@ def main():
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 
-    if os.path.isdir(REF):
+    if ref and os.path.isdir(ref):
         arrays = {}
         for nm in ("test_data", "test_data3"):
-            a = np.loadtxt(os.path.join(REF, nm + ".csv"), delimiter=",", dtype=np.int64).astype(np.int32)
+            a = np.loadtxt(os.path.join(ref, nm + ".csv"), delimiter=",", dtype=np.int64).astype(np.int32)
             arrays[nm] = a
             arrays[nm + "_image"] = oracle.resolve(a, 1200, 1024, oracle.MODE_REFERENCE, threads=4)
         np.savez_compressed(os.path.join(HERE, "ref_mock_drawlists.npz"), **arrays)
@@ -74,4 +75,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)
