@@ -192,7 +192,9 @@ void sr_destroy(sr_ctx* ctx);
  * kernel workdir/shaders/common/naive_scan.comp:27-73 (one workgroup,
  * 1023-element batches) with a single-pass decoupled look-back scan.
  * Asynchronous on `stream`; its look-back scratch comes from
- * cudaMallocAsync/cudaFreeAsync on the same stream.  0 <= n < 2^31. */
+ * cudaMallocAsync/cudaFreeAsync on the same stream.  0 <= n < 2^31.
+ * A look-back wait that gives up (SR_ERR_TIMEOUT) leaves a wrong prefix in
+ * d_out; it is reported by sr_scan_status, not by this call. */
 sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
 
 /* The same scan for callers that cannot allocate device memory: a host that
@@ -207,14 +209,41 @@ sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, 
  * the process exits.  n is limited to SR_NOALLOC_SCAN_MAX_N; larger n is
  * rejected with SR_ERR_INVALID_ARG.  The first call on a device looks up the
  * array's device address (with that device current); make that first call
- * before any stream capture.  Every call uses the same array and clears the
- * part it needs, so calls that overlap on the GPU (on different streams, or
- * from different threads) race: serialise them on one stream.  Inputs,
- * outputs and results are as for sr_exclusive_scan_i32; asynchronous on
- * `stream`. */
+ * before any stream capture; the address does not survive a cudaDeviceReset.
+ * Every call uses the same array and clears the part it needs, so calls that
+ * overlap on the GPU (on different streams, or from different threads) race:
+ * serialise them on one stream.  Inputs, outputs and results are as for
+ * sr_exclusive_scan_i32 (timeouts included, reported by sr_scan_status);
+ * asynchronous on `stream`. */
 #define SR_NOALLOC_SCAN_MAX_N (1ll << 24)
 #define SR_NOALLOC_SCAN_SCRATCH_BYTES (4104u * 8u)
 sr_status sr_exclusive_scan_i32_noalloc(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
+
+/* Waits for `stream`, then reports whether a look-back wait of a standalone
+ * scan (sr_exclusive_scan_i32 or sr_exclusive_scan_i32_noalloc) on the
+ * current device gave up since the last call: SR_ERR_TIMEOUT if one did
+ * (that scan's output is wrong), else SR_OK.  It clears the report.  Scans
+ * still running on other streams are reported by a later call.  The
+ * reference's scan has no wait to give up (naive_scan.comp runs in one
+ * workgroup), so this has no counterpart there.  Allocates nothing. */
+sr_status sr_scan_status(void* stream);
+
+/* Sets how many polls every bounded device-side wait (the look-backs of the
+ * scans, of the radix sort and of the winding pass) makes before it gives up
+ * and the call reports SR_ERR_TIMEOUT; 0 restores the default of 2^22 polls
+ * with back-off (a second or more).  Kernels launched after the call use the
+ * new limit, in every context of the process; a captured batch graph keeps
+ * the limit it was captured with.  No reference counterpart (its waits are
+ * host-side queue idles). */
+void sr_set_spin_limit(uint32_t polls);
+
+/* Test hook for the bounded waits: the allocating standalone scan with its
+ * tile counter started at 1, so that tile 0 never runs and never publishes
+ * its sum.  Tile 1's look-back (and any that reach tile 0) waits until the
+ * spin limit and gives up; sr_scan_status then reports SR_ERR_TIMEOUT.
+ * d_out[0..4095] is left unwritten and the rest is wrong.  n > 0.  No
+ * reference counterpart. */
+sr_status sr_debug_scan_without_first_tile(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* sr_last_error(void);

@@ -41,3 +41,39 @@ def test_exclusive_scan_rejects_bad_sizes(gpu):
         gpu.exclusive_scan_i32(d.data_ptr(), d.data_ptr(), -1)
     with pytest.raises(gpu.SRError):
         gpu.exclusive_scan_i32(d.data_ptr(), None, 3)
+
+
+def test_scan_status_is_ok_after_good_scans(gpu):
+    import torch
+    a = np.arange(50000, dtype=np.int32)
+    d_in = torch.from_numpy(a).cuda()
+    d_out = torch.zeros(a.size + 1, dtype=torch.int32, device="cuda")
+    gpu.exclusive_scan_i32(d_in.data_ptr(), d_out.data_ptr(), a.size)
+    gpu.exclusive_scan_i32_noalloc(d_in.data_ptr(), d_out.data_ptr(), a.size)
+    gpu.scan_status()
+    assert np.array_equal(d_out.cpu().numpy(), _excl_scan_ref(a))
+
+
+def test_bounded_wait_gives_up_and_the_context_stays_usable(gpu):
+    """A look-back whose predecessor never publishes (tile 0 is skipped)
+    gives up after the spin limit; the scan reports SR_ERR_TIMEOUT through
+    sr_scan_status, and the next scan on the same device is correct."""
+    import torch
+    n = 64 * 4096 + 5
+    a = np.ones(n, np.int32)
+    d_in = torch.from_numpy(a).cuda()
+    d_out = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+    L = gpu.lib()
+    gpu.set_spin_limit(2000)
+    try:
+        assert L.sr_debug_scan_without_first_tile(d_in.data_ptr(), d_out.data_ptr(), n, None) == 0, \
+            L.sr_last_error()
+        with pytest.raises(gpu.SRError) as e:
+            gpu.scan_status()
+        assert e.value.code == 4 and "timed out" in str(e.value)
+        gpu.scan_status()   # the report was cleared
+    finally:
+        gpu.set_spin_limit(0)
+    gpu.exclusive_scan_i32(d_in.data_ptr(), d_out.data_ptr(), n)
+    gpu.scan_status()
+    assert np.array_equal(d_out.cpu().numpy(), _excl_scan_ref(a))

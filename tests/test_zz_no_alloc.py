@@ -28,6 +28,7 @@ def _scan_both(sr, a):
         L.sr_last_error()
     assert L.sr_exclusive_scan_i32(d_in.data_ptr(), out_ref.data_ptr(), n, stream) == 0, L.sr_last_error()
     torch.cuda.synchronize()
+    sr.scan_status(stream)
     return out_free.cpu().numpy(), out_ref.cpu().numpy()
 
 
@@ -40,6 +41,32 @@ def test_two_calls_in_a_row_match_the_allocating_scan(gpu):
         got, want = _scan_both(gpu, a)
         assert np.array_equal(got, want)
         assert got[0] == 0 and got[-1] == np.int32(a.astype(np.int64).sum())
+
+
+def test_calls_leave_free_device_memory_unchanged_and_scan_in_place(gpu):
+    """Once the library's device code is loaded (the first call on a device
+    may load it), further calls take no device memory: the free bytes the
+    driver reports are the same before and after.  In place (d_in == d_out)
+    at a size that is not a whole number of 4,096-element tiles."""
+    import torch
+    n = 1_000_003
+    rng = np.random.default_rng(7)
+    a = rng.integers(-50, 50, size=n, dtype=np.int32)
+    buf = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+    L = gpu.lib()
+    assert L.sr_exclusive_scan_i32_noalloc(buf.data_ptr(), buf.data_ptr(), n, None) == 0, L.sr_last_error()
+    torch.cuda.synchronize()
+    buf[:n] = torch.from_numpy(a).cuda()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert L.sr_exclusive_scan_i32_noalloc(buf.data_ptr(), buf.data_ptr(), n, None) == 0, L.sr_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    gpu.scan_status()
+    assert free1 == free0
+    want = np.zeros(n + 1, np.int64)
+    np.cumsum(a.astype(np.int64), out=want[1:])
+    assert np.array_equal(buf.cpu().numpy(), want.astype(np.int32))
 
 
 def test_sizes_beyond_the_fixed_scratch_are_rejected(gpu):

@@ -160,7 +160,8 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_batch_query", "sr_batch_finish", "sr_batch_release", "sr_batch_held_bytes", "sr_batch_path_ranges",
            "sr_server_create", "sr_server_submit", "sr_server_wait", "sr_server_get_stats", "sr_server_destroy",
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
-           "sr_batch_tuning_class", "sr_batch_autotune"]
+           "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
+           "sr_debug_scan_without_first_tile"]
 
 _lib = None
 
@@ -193,6 +194,10 @@ def lib():
     L.sr_rvg_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
     L.sr_scene_buf_view.argtypes = [vp, ctypes.POINTER(SceneView)]
     L.sr_scene_buf_free.argtypes = [vp]
+    L.sr_scan_status.argtypes = [vp]
+    L.sr_set_spin_limit.argtypes = [ctypes.c_uint32]
+    L.sr_set_spin_limit.restype = None
+    L.sr_debug_scan_without_first_tile.argtypes = [vp, vp, ctypes.c_int64, vp]
     L.sr_scene_buf_free.restype = None
     L.sr_scene_buf_size.argtypes = [vp, vp]
     L.sr_host_alloc.argtypes = [ctypes.c_size_t]
@@ -402,6 +407,17 @@ def load_rvg(path):
 def exclusive_scan_i32(d_in, d_out, n, stream=None):
     """Exclusive scan of n int32 at device address d_in into d_out[0..n]."""
     _check(lib().sr_exclusive_scan_i32(d_in, d_out, int(n), stream))
+
+
+def scan_status(stream=None):
+    """Waits for `stream`; raises SrError(SR_ERR_TIMEOUT) if a look-back of a
+    standalone scan gave up since the last call (its output is wrong)."""
+    _check(lib().sr_scan_status(stream))
+
+
+def set_spin_limit(polls):
+    """Polls every bounded device wait makes before giving up (0: default)."""
+    lib().sr_set_spin_limit(int(polls))
 
 
 NOALLOC_SCAN_MAX_N = 1 << 24

@@ -119,6 +119,8 @@ std::atomic<uint64_t> g_launches{0};
 namespace sr {
 sr_status report_error(sr_status s, const char* msg) { return fail(s, "%s", msg); }
 void count_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+static std::atomic<uint32_t> g_spin_limit{kSpinLimitDefault};
+uint32_t spin_limit() { return g_spin_limit.load(std::memory_order_relaxed); }
 uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace sr
 
@@ -1108,29 +1110,60 @@ sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
     return SR_OK;
 }
 
-sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream) {
+// The allocating standalone scan; first_tile > 0 starts the tile counter
+// there (tiles before it never run), which only sr_debug_scan_without_first_tile
+// asks for.
+static sr_status standalone_scan(const int32_t* d_in, int32_t* d_out, int64_t n, uint32_t first_tile,
+                                 cudaStream_t st) {
     if (n < 0 || n >= (1ll << 31)) return fail(SR_ERR_INVALID_ARG, "scan length %lld out of range", (long long)n);
     if (!d_out || (n > 0 && !d_in)) return fail(SR_ERR_INVALID_ARG, "NULL device pointer");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (n == 0) {
         CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(int32_t), st));
         return SR_OK;
     }
-    // tile words, then the tile counter and the status word
-    const size_t words = sr::scan_status_words(n) + 2;
+    uint32_t* status = nullptr;
+    CUDA_TRY(sr::standalone_scan_status(&status));
+    // tile words, then the tile counter
+    const size_t words = sr::scan_status_words(n) + 1;
     void* scratch = nullptr;
     CUDA_TRY(cudaMallocAsync(&scratch, words * sizeof(uint64_t), st));
     uint64_t* tiles = static_cast<uint64_t*>(scratch);
-    uint32_t* tail = reinterpret_cast<uint32_t*>(tiles + words - 2);
+    uint32_t* counter = reinterpret_cast<uint32_t*>(tiles + words - 1);
     cudaError_t e = cudaMemsetAsync(scratch, 0, words * sizeof(uint64_t), st);
+    if (e == cudaSuccess && first_tile) e = cudaMemcpyAsync(counter, &first_tile, sizeof first_tile,
+                                                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && first_tile) e = cudaStreamSynchronize(st);   // first_tile is on this stack
     if (e == cudaSuccess) {
-        sr::launch_exclusive_scan_i32(d_in, d_out, n, tiles, tail, tail + 1, st);
+        sr::launch_exclusive_scan_i32(d_in, d_out, n, tiles, counter, status, st);
         e = cudaGetLastError();
     }
     cudaError_t f = cudaFreeAsync(scratch, st);
     CUDA_TRY(e);
     CUDA_TRY(f);
     return SR_OK;
+}
+
+sr_status sr_exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream) {
+    return standalone_scan(d_in, d_out, n, 0, static_cast<cudaStream_t>(stream));
+}
+
+sr_status sr_debug_scan_without_first_tile(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream) {
+    if (n <= 0) return fail(SR_ERR_INVALID_ARG, "the stalled scan needs n > 0");
+    return standalone_scan(d_in, d_out, n, 1, static_cast<cudaStream_t>(stream));
+}
+
+sr_status sr_scan_status(void* stream) {
+    CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    uint32_t* word = nullptr;
+    CUDA_TRY(sr::standalone_scan_status(&word));
+    uint32_t h = 0;
+    CUDA_TRY(cudaMemcpy(&h, word, sizeof h, cudaMemcpyDeviceToHost));
+    if (h) CUDA_TRY(cudaMemset(word, 0, sizeof h));
+    return check_status_word(h);
+}
+
+void sr_set_spin_limit(uint32_t polls) {
+    sr::g_spin_limit.store(polls ? polls : sr::kSpinLimitDefault, std::memory_order_relaxed);
 }
 
 void sr_destroy(sr_ctx* c) {

@@ -22,8 +22,10 @@ enum : uint32_t {
     ERR_BAD_INDEX = 1u << 3,         // an index read from memory was out of range
 };
 
-// Polls allowed before a bounded spin gives up (with backoff, ~seconds).
-constexpr uint32_t kSpinLimit = 1u << 22;
+// Polls a bounded spin makes before it gives up (with backoff, ~seconds),
+// unless sr_set_spin_limit chose another limit.  Launchers pass the limit to
+// each kernel that spins (see spin_limit() in kernels.h).
+constexpr uint32_t kSpinLimitDefault = 1u << 22;
 
 SR_DEV float lerp_rn(float a, float b, float t) {
     // LERP(a,b,t) = a + t*(b-a)   (make_intersection_0.comp:10)

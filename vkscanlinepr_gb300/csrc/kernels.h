@@ -25,6 +25,13 @@ template <typename Fn> void once_per_device(std::atomic<uint32_t>& flags, Fn&& f
     flags.fetch_or(bit, std::memory_order_release);
 }
 uint64_t launches_so_far();
+// Polls a bounded device spin makes before it gives up: kSpinLimitDefault
+// unless sr_set_spin_limit chose another.  Read at each launch.
+uint32_t spin_limit();
+// Device address, on the current device, of the sticky error word of the
+// standalone scans (sr_exclusive_scan_i32 and its allocation-free variant),
+// which sr_scan_status reads and clears.
+cudaError_t standalone_scan_status(uint32_t** out);
 
 struct Mvp {
     float m[16];   // rows m0..m3

@@ -3,8 +3,8 @@
 // Replaces naive_scan.comp:27-73, which runs in ONE workgroup and walks the
 // input in dependent batches of 1023.  Here every CTA scans a 4096-element
 // tile, publishes its aggregate, and a single warp looks back over the
-// predecessors' published values.  Every spin is bounded: after kSpinLimit
-// polls the tile records ERR_LOOKBACK_TIMEOUT and carries on, so a stalled
+// predecessors' published values.  Every spin is bounded: after the spin
+// limit's polls the tile records ERR_LOOKBACK_TIMEOUT and carries on, so a stalled
 // predecessor can never hang the GPU.  Output: out[0..n], out[n] = total
 // (exactly n+1 writes).
 #include "common.cuh"
@@ -38,7 +38,7 @@ SR_DEV int32_t warp_sum(int32_t v) {
 
 // Warp-cooperative look-back over 64-bit tile words (flag in bits 62-63,
 // value in bits 0-31).  Returns the sum of all predecessors of `tile`.
-__device__ int32_t lookback_i32(uint64_t* tstat, uint32_t tile, uint32_t* status) {
+__device__ int32_t lookback_i32(uint64_t* tstat, uint32_t tile, uint32_t* status, uint32_t spin_limit) {
     uint32_t lane = lane_id();
     int32_t excl = 0;
     int64_t look = (int64_t)tile - 1;
@@ -52,7 +52,7 @@ __device__ int32_t lookback_i32(uint64_t* tstat, uint32_t tile, uint32_t* status
         int firstp = pm ? (__ffs(pm) - 1) : 31;
         uint32_t need = firstp == 31 ? 0xFFFFFFFFu : ((2u << firstp) - 1u);
         if ((ready & need) != need) {
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 if (lane == 0) set_error(status, ERR_LOOKBACK_TIMEOUT);
                 break;
             }
@@ -68,7 +68,8 @@ __device__ int32_t lookback_i32(uint64_t* tstat, uint32_t tile, uint32_t* status
 }
 
 __global__ void __launch_bounds__(kThreads) k_scan_i32(const int32_t* in, int32_t* out, int64_t n,
-                                                       uint64_t* tstat, uint32_t* counter, uint32_t* status) {
+                                                       uint64_t* tstat, uint32_t* counter, uint32_t* status,
+                                                       uint32_t spin_limit) {
     __shared__ uint32_t s_tile;
     __shared__ int32_t s_warp[kThreads / 32];
     __shared__ int32_t s_prefix;
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_i32(const int32_t* in, int32_
         if (lane == 0) st_release_u64(&tstat[tile], (tile == 0 ? kFlagP : kFlagA) | (uint32_t)agg);
         int32_t excl = 0;
         if (tile > 0) {
-            excl = lookback_i32(tstat, tile, status);
+            excl = lookback_i32(tstat, tile, status, spin_limit);
             if (lane == 0) st_release_u64(&tstat[tile], kFlagP | (uint32_t)wadd(excl, agg));
         }
         if (lane == 0) {
@@ -134,6 +135,17 @@ __global__ void __launch_bounds__(kThreads) k_scan_i32(const int32_t* in, int32_
     }
 }
 
+// Sticky error bits of the standalone scans on each device that loads the
+// library (4 bytes, held until exit).
+static __device__ uint32_t g_standalone_scan_status;
+
+cudaError_t standalone_scan_status(uint32_t** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_standalone_scan_status);
+    *out = static_cast<uint32_t*>(p);
+    return e;
+}
+
 size_t scan_status_words(int64_t n) { return (size_t)((n + kTile - 1) / kTile + 1); }
 
 void launch_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, uint64_t* tile_status,
@@ -144,7 +156,7 @@ void launch_exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, uint6
     }
     int64_t tiles = (n + kTile - 1) / kTile;
     count_launches(1);
-    k_scan_i32<<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, tile_status, tile_counter, status);
+    k_scan_i32<<<(unsigned)tiles, kThreads, 0, st>>>(in, out, n, tile_status, tile_counter, status, spin_limit());
 }
 
 }  // namespace sr

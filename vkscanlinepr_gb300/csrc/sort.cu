@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, onesweep_min_blocks(kVals, ITEMS)) k
                                                        uint32_t shift, uint32_t dmask,
                                                        const uint32_t* __restrict__ global_off,
                                                        uint32_t* __restrict__ lookback, uint32_t* counter,
-                                                       uint32_t* status) {
+                                                       uint32_t* status, uint32_t spin_limit) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int kItems = ITEMS, kTile = kThreads * ITEMS;
     OnesweepSmem<K, kVals, ITEMS>& S = *reinterpret_cast<OnesweepSmem<K, kVals, ITEMS>*>(smem_raw);
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, onesweep_min_blocks(kVals, ITEMS)) k
             if (done) break;
             look -= used;
             if (used == 0) {
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     set_error(status, ERR_LOOKBACK_TIMEOUT);
                     break;
                 }
@@ -379,7 +379,7 @@ static void sort_impl(const SortPlan& p, const K* keys_in, const uint32_t* vals_
                                                              digit_mask(p.key_bits, pass * kRadixBits),
                                                              s.hist + pass * kRadix,
                                                              s.lookback + (size_t)pass * (p.tiles + 1) * kRadix,
-                                                             s.counters + pass, status);
+                                                             s.counters + pass, status, spin_limit());
         ksrc = kdst;
         vsrc = vdst;
     }

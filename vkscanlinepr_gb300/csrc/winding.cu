@@ -52,7 +52,7 @@ template <typename T> SR_DEV T warp_incl(T v) {
 
 // Look-back over 64-bit tile words; `add` combines values (wrapping).
 template <bool kSigned32>
-SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
+SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status, uint32_t spin_limit) {
     uint32_t lane = lane_id();
     uint64_t excl = 0;
     int64_t look = (int64_t)tile - 1;
@@ -68,7 +68,7 @@ SR_DEV uint64_t lookback(uint64_t* tstat, uint32_t tile, uint32_t* status) {
         int firstp = pm ? (__ffs(pm) - 1) : 31;
         uint32_t need = firstp == 31 ? 0xFFFFFFFFu : ((2u << firstp) - 1u);
         if ((ready & need) != need) {
-            if (++spins > kSpinLimit) {
+            if (++spins > spin_limit) {
                 if (lane == 0) set_error(status, ERR_LOOKBACK_TIMEOUT);
                 break;
             }
@@ -108,7 +108,7 @@ template <int ITEMS> struct Smem {
 template <int ITEMS>
 __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uint64_t* __restrict__ tstatA,
                                                            uint64_t* __restrict__ tstatB, uint32_t* counter,
-                                                           uint32_t* status) {
+                                                           uint32_t* status, uint32_t spin_limit) {
     constexpr int kItems = ITEMS, kTile = kThreads * ITEMS;
     __shared__ Smem<ITEMS> S;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
             st_release_u64(&tstatA[tile], (tile == 0 ? kFlagP : kFlagA) | (aggf ? kHeadBit : 0ull) | (uint32_t)agg);
         int32_t excl = 0;
         if (tile > 0) {
-            excl = (int32_t)(uint32_t)lookback<true>(tstatA, tile, status);
+            excl = (int32_t)(uint32_t)lookback<true>(tstatA, tile, status, spin_limit);
             if (lane == 0) st_release_u64(&tstatA[tile], kFlagP | (uint32_t)(aggf ? agg : wadd(excl, agg)));
         }
         // carry into each warp: the tile prefix combined with the warp's exclusive pair
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kThreads) k_winding_emit(const WindArgs a, uin
         if (lane == 0) st_release_u64(&tstatB[tile], (tile == 0 ? kFlagP : kFlagA) | agg);
         uint64_t excl = 0;
         if (tile > 0) {
-            excl = lookback<false>(tstatB, tile, status);
+            excl = lookback<false>(tstatB, tile, status, spin_limit);
             if (lane == 0) st_release_u64(&tstatB[tile], kFlagP | (excl + agg));
         }
         if (lane == 0) {
@@ -437,8 +437,9 @@ void launch_winding_emit(const WindArgs& a, int items, uint64_t* tile_status, ui
     uint64_t* sA = tile_status;
     uint64_t* sB = tile_status + (tiles + 1);
     count_launches(1);
-    if (items == 4) k_winding_emit<4><<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
-    else k_winding_emit<8><<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status);
+    const uint32_t lim = spin_limit();
+    if (items == 4) k_winding_emit<4><<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status, lim);
+    else k_winding_emit<8><<<(unsigned)tiles, kThreads, 0, st>>>(a, sA, sB, tile_counter, status, lim);
 }
 
 }  // namespace sr
