@@ -44,6 +44,11 @@ WORKLOADS = {
     "mixed2048": (1, 1, 2048, 2048, 5000),
 }
 L2_FLUSH_BYTES = 256 << 20
+# GPU images kept (as SHA-256) for the oracle check in the CPU-baseline leg:
+# "batch" holds (scene index, hash) of a seeded sample of the batch workload,
+# "served" (scene index, hash) of served requests
+CHECKS = {"batch": [], "served": []}
+ORACLE_SAMPLE = 64
 # What bounds each stage's main kernel (profiles/ncu_top_kernels_frame4096.md):
 # the HBM fraction is the roofline only for the stages that move bytes.
 LIMITS = {
@@ -274,6 +279,9 @@ def run_batched(sr, args, sptr, steps):
         times.append(time.perf_counter() - t1)
     overflows = sum(b.stats()["overflows"] for b in batches)
     batched_sps = total / (sum(times) / len(times))
+    # a seeded sample of the timed frames' images, checked against the oracle later
+    sample = sorted(np.random.default_rng(11).choice(total, min(ORACLE_SAMPLE, total), replace=False).tolist())
+    CHECKS["batch"] = [(i, image_hash(batches[i // per].image(i % per))) for i in sample]
     # plain per-scene renderer on the first scenes of the same set
     nplain = min(args.plain_scenes, total)
     ctx = None
@@ -518,7 +526,8 @@ def run_serving(sr, args, sz, margins):
         srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=args.serve_batch, memory_budget=120e9,
                               margins=margins)
         _serve(sr, srv, pool[:64], [None] * 64)                      # warm the slots' buffers
-        t, imgs = _serve(sr, srv, pool, arrivals, check_every=64 if name == "learned" else 0)
+        t, imgs = _serve(sr, srv, pool, arrivals,
+                         check_every=max(1, n // ORACLE_SAMPLE) if name == "learned" else 0)
         res = _lat_summary(t[:, 0], t[:, 1])
         res["mean_batch"] = round(float(t[:, 2].mean()), 1)
         ts, _ = _serve(sr, srv, pool, [None] * n)                     # saturation: all at once
@@ -559,12 +568,40 @@ def run_serving(sr, args, sz, margins):
             exact += int(np.array_equal(ctx.render(), checked[i]))
     if ctx is not None:
         ctx.close()
+    CHECKS["served"] = [(i % len(pool), image_hash(img)) for i, img in sorted(checked.items())]
     out["plain"] = _lat_summary(np.array(arrivals), np.array(done))
     out["bit_exact_vs_plain"] = "%d/%d" % (exact, len(checked))
     out["speedup_vs_plain"] = round(out["learned"]["scenes_per_s"] / out["plain"]["scenes_per_s"], 2)
     out["saturated_speedup_vs_plain"] = round(out["learned"]["saturated_scenes_per_s"] /
                                               out["plain"]["scenes_per_s"], 2)
     return out
+
+
+def image_hash(img):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(img).tobytes()).hexdigest()
+
+
+def check_against_oracle(threads):
+    """The kept batch and served images against the oracle's frames of the
+    same scenes (pixel mode), and their samples that flip against the FP64
+    oracle.  Returns ({"batch": "k/n", "served": "k/n"}, flips summary)."""
+    import oracle
+    exact, flips = {}, []
+    for key, items in CHECKS.items():
+        ok = 0
+        for idx, h in items:
+            sc = oracle.synth(2, 2, scene_index=idx)
+            img = oracle.Frame(sc, mode=oracle.MODE_PIXEL, threads=threads).get("image")
+            ok += int(image_hash(img) == h)
+            if key == "batch":
+                flips.append(oracle.fp64_flips(sc, oracle.MODE_PIXEL, threads=threads, image=img))
+        exact[key] = "%d/%d" % (ok, len(items))
+    fl = None
+    if flips:
+        fl = {"scenes": len(flips), "total": int(sum(flips)), "max": int(max(flips)),
+              "scenes_with_flips": int(sum(1 for f in flips if f))}
+    return exact, fl
 
 
 def oracle_scene(preset, seed, W, H, P):
@@ -752,6 +789,19 @@ def main():
         cpu, ref_img = run_cpu_baseline(so, W, H)
         line["cpu_baseline"] = cpu
         line["bit_exact"] = bool(np.array_equal(ref_img, gpu_img))
+        import oracle
+        th = oracle.hw_threads()
+        flips = {"frame": oracle.fp64_flips(so, oracle.MODE_PIXEL, threads=th, image=gpu_img),
+                 "what": "pixels whose colour differs from the FP64 oracle (double arithmetic, 52 bisection "
+                         "steps); the GPU image is bit-exact to the FP32 oracle"}
+        exact, batch_flips = check_against_oracle(th)
+        if batch_flips is not None:
+            flips["batch_sample"] = batch_flips
+        line["fp64_flips"] = flips
+        if batched is not None:
+            line["batched"]["bit_exact_vs_oracle"] = exact["batch"]
+        if serving is not None:
+            line["serving"]["bit_exact_vs_oracle"] = exact["served"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -224,6 +224,17 @@ class Frame:
             pass
 
 
+def fp64_flips(scene, mode, mvp=None, threads=0, image=None):
+    """Samples (pixels, at 1 sample per pixel) whose colour differs between
+    the FP32 frame -- `image` when given (e.g. the GPU's, which is bit-exact
+    to the oracle's FP32 frame), else the oracle's own -- and the oracle's
+    FP64 instance of the same scene (double arithmetic, 52 bisection steps)."""
+    if image is None:
+        image = Frame(scene, mvp=mvp, mode=mode, threads=threads).get("image")
+    ref = Frame(scene, mvp=mvp, mode=mode, threads=threads, fp64=True).get("image")
+    return int(np.any(np.asarray(image) != ref, axis=2).sum())
+
+
 def resolve(draw, width, height, mode, threads=1):
     """Paint an int32x4 draw list with the oracle's resolve step."""
     d = np.ascontiguousarray(draw, np.int32).reshape(-1, 4)

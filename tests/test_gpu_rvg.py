@@ -1,0 +1,22 @@
+"""The reference's eight shipped RVG scenes (tests/golden/rvg), rendered by
+the CUDA renderer through the C ABI and compared stage by stage with the
+oracle, in reference mode (the reference's own semantics: 2x2 cells, whole
+boundary cells, the last path wins) and in pixel mode.  The scenes are read
+by the library's RVG reader, which follows the reference's RVG::load; the arc
+scenes (chord, chord-black) stop at their first arc as the reference's reader
+does, and render as empty canvases."""
+import pytest
+
+import rvg_scenes
+from parity_util import STAGES_COMMON, compare_all, render_both
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("name", rvg_scenes.NAMES)
+def test_reference_scene_stages(gpu, oracle_lib, tmp_path, name, mode):
+    d, _ = rvg_scenes.load(gpu, name, tmp_path)
+    of, r, img = render_both(gpu, oracle_lib, d, mode)
+    compare_all(of, r, img, mode, stages=STAGES_COMMON)
+    r.close()
