@@ -147,7 +147,9 @@ typedef struct sr_stats {
     uint32_t key_bits;         /* bits of the sort key                   */
     uint32_t sort_passes;      /* radix passes run                       */
     uint32_t kernel_launches;  /* kernels this library launched for the frame */
-    uint32_t reserved;
+    uint32_t reruns;           /* sr_render: pre-sized frames of this context
+                                * that overflowed and were rerun with exact
+                                * sizing (cumulative; 0 for batches)        */
     /* with SR_FLAG_PROFILE: device time of each stage (CUDA events on the
      * render stream): transform, count, offset scan, crossing chains,
      * record merge, fragments, sort, winding+emit, row sort, resolve; then

@@ -65,7 +65,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("n_intersections", ctypes.c_uint64), ("n_draw_records", ctypes.c_uint64),
                 ("n_merged_fragments", ctypes.c_uint64), ("n_spans", ctypes.c_uint64),
                 ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32),
-                ("kernel_launches", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("kernel_launches", ctypes.c_uint32), ("reruns", ctypes.c_uint32),
                 ("stage_ms", ctypes.c_float * 12)]
 
 STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
@@ -509,7 +509,7 @@ class ScanlineVGRasterizer:
     def stats(self):
         s = Stats()
         _check(lib().sr_get_stats(self._ctx, ctypes.byref(s)))
-        d = {k: getattr(s, k) for k, _ in Stats._fields_ if k not in ("stage_ms", "reserved")}
+        d = {k: getattr(s, k) for k, _ in Stats._fields_ if k != "stage_ms"}
         d["stage_ms"] = dict(zip(STAGE_NAMES, [float(x) for x in s.stage_ms]))
         return d
 
@@ -699,7 +699,7 @@ class SceneBatch:
         _check(lib().sr_batch_get_stats(self._h, ctypes.byref(s)))
         f = s.frame
         d = {k: getattr(s, k) for k, _ in BatchStats._fields_ if k != "frame"}
-        d.update({k: getattr(f, k) for k, _ in Stats._fields_ if k not in ("stage_ms", "reserved")})
+        d.update({k: getattr(f, k) for k, _ in Stats._fields_ if k not in ("stage_ms", "reruns")})
         d["stage_ms"] = dict(zip(STAGE_NAMES, [float(x) for x in f.stage_ms]))
         return d
 

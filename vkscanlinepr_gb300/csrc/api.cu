@@ -243,6 +243,7 @@ struct Pipeline {
     // results
     sr_stats stats{};
     int64_t last_N = 0, last_O = 0, last_cap = 0, last_dcap = 0;
+    uint32_t last_largest = 0;   // records of the frame's largest sort segment
     bool stages_valid = false;
     // profiling
     cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
@@ -790,22 +791,28 @@ struct Pipeline {
                                      cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         SR_TRY(check_status_word(h_u32[1]));
-        // merge rounds for the largest segment; past the limit the radix sort
-        seg_levels = 0;
-        const uint32_t T = (uint32_t)sr::segsort_tile();
-        uint32_t chunks = (h_u32[2] + T - 1) / T;
-        while (chunks > (1u << seg_levels)) ++seg_levels;
-        if (seg_levels > kSegLevelsMax) seg_levels = -1;
+        seg_levels = levels_for(h_u32[2]);
         *N = (int64_t)(int32_t)h_u32[0];
         if (*N < 0 || *N >= (1ll << 30))
             return fail(SR_ERR_OVERFLOW_REFIT, "record count %lld out of range", (long long)*N);
         return SR_OK;
     }
 
+    // Merge rounds of the segmented sort for a largest segment of `largest`
+    // records; -1 past the limit (the radix sort then).
+    static int levels_for(uint32_t largest) {
+        int lv = 0;
+        const uint32_t T = (uint32_t)sr::segsort_tile();
+        const uint32_t chunks = (largest + T - 1) / T;
+        while (chunks > (1u << lv)) ++lv;
+        return lv > kSegLevelsMax ? -1 : lv;
+    }
+
     // One frame.  cap < 0: size the record buffers exactly (one host wait
-    // for N); cap >= 0: use that capacity without waiting.  dcap <= 0 sizes
-    // the draw records at 2 x cap.
-    sr_status frame(cudaStream_t st, int64_t cap, int64_t dcap = -1) {
+    // for N); cap >= 0: use that capacity without waiting, with `levels`
+    // merge rounds of the segmented sort (a larger segment flags an
+    // overflow).  dcap <= 0 sizes the draw records at 2 x cap.
+    sr_status frame(cudaStream_t st, int64_t cap, int64_t dcap = -1, int levels = kSegLevelsMax) {
         CUDA_TRY(cudaSetDevice(device));
         if (!loaded) return fail(SR_ERR_NO_SCENE, "render before a scene was loaded");
         cur = st;
@@ -814,8 +821,9 @@ struct Pipeline {
         SR_TRY(prepare_front());
         // exact sizing reads the largest segment back; a pre-sized frame
         // runs the most merge rounds and flags larger segments as overflow
-        seg_check = cap < 0 ? 0u : (uint32_t)sr::segsort_tile() << kSegLevelsMax;
-        seg_levels = kSegLevelsMax;
+        if (levels < 0 || levels > kSegLevelsMax) levels = kSegLevelsMax;
+        seg_check = cap < 0 ? 0u : (uint32_t)sr::segsort_tile() << levels;
+        seg_levels = levels;
         SR_TRY(enqueue_front(st));
         if (cap < 0) {
             int64_t N = 0;
@@ -838,6 +846,10 @@ struct Pipeline {
         CUDA_TRY(cudaMemcpyAsync(&h_u32[0], offs.as<int32_t>() + C, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(&h_u32[1], ctl.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(h_u64, totals.p, sizeof(uint64_t) * 2, cudaMemcpyDeviceToHost, st));
+        h_u32[2] = 0;
+        if (segmented())
+            CUDA_TRY(cudaMemcpyAsync(&h_u32[2], sr::segsort_largest(seg_scratch.p, C), sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, st));
         return SR_OK;
     }
 
@@ -851,6 +863,7 @@ struct Pipeline {
     sr_status collect() {
         last_N = (int64_t)(int32_t)h_u32[0];
         last_O = (int64_t)(h_u64[0] + h_u64[1]);
+        last_largest = h_u32[2];
         stats.n_intersections = (uint64_t)last_N;
         stats.n_draw_records = (uint64_t)last_O;
         stats.n_merged_fragments = h_u64[0];
@@ -886,6 +899,14 @@ struct sr_ctx {
     Pipeline p;
     int32_t W = 0, H = 0;
     float mvp[16];
+    // Counts of the last frame that completed without overflow, and the
+    // curve and path counts of its scene: the next frame of a scene with the
+    // same counts is pre-sized from them instead of waiting for its count.
+    bool hint_valid = false;
+    uint32_t hint_C = 0, hint_P = 0;
+    int64_t hint_N = 0, hint_O = 0;
+    uint32_t hint_largest = 0;
+    uint32_t refits = 0;
 };
 
 // Batch of scenes (several uneven scenes per frame).
@@ -985,16 +1006,52 @@ sr_status sr_set_mvp(sr_ctx* c, const float m[16]) {
     return SR_OK;
 }
 
+// ScanlineVGRasterizer::render (scanline_rasterizer.cpp:282-696) waits on
+// the host twice inside a frame, for the record count (:355-356) and the
+// fragment and span counts (:578-580).  A frame here is pre-sized from the
+// previous frame of a scene with the same curve and path counts (1/16 more,
+// and the merge rounds its largest sort segment needed) and enqueued whole;
+// the only host wait is at its end, where the counters are read.  If the
+// frame overflowed (a new matrix or scene that needs more), it is rerun with
+// exact sizing, which waits for the count as the reference does; so does the
+// first frame of a scene.
 sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) {
     if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    SR_TRY(c->p.frame(st, -1));
-    if (rgba_out) {
-        size_t bytes = (size_t)c->W * c->H * 4;
-        CUDA_TRY(cudaMemcpyAsync(rgba_out, c->p.image.p, bytes,
-                                 out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    Pipeline& p = c->p;
+    const size_t bytes = (size_t)c->W * c->H * 4;
+    const bool presized = c->hint_valid && p.loaded && c->hint_C == p.C && c->hint_P == p.P;
+    const uint64_t launches0 = sr::launches_so_far();
+    sr_status s = SR_ERR_OVERFLOW_REFIT;
+    if (presized) {
+        const int64_t cap = c->hint_N + c->hint_N / 16 + 256;
+        const int64_t dcap = c->hint_O + c->hint_O / 16 + 256;
+        int levels = Pipeline::levels_for(c->hint_largest + c->hint_largest / 16);
+        SR_TRY(p.frame(st, cap, dcap, levels < 0 ? Pipeline::kSegLevelsMax : levels));
+        if (rgba_out)
+            CUDA_TRY(cudaMemcpyAsync(rgba_out, p.image.p, bytes,
+                                     out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        s = p.finish(st);
+        if (s == SR_ERR_OVERFLOW_REFIT) ++c->refits;
     }
-    return c->p.finish(st);
+    if (s == SR_ERR_OVERFLOW_REFIT) {
+        SR_TRY(p.frame(st, -1));
+        if (rgba_out)
+            CUDA_TRY(cudaMemcpyAsync(rgba_out, p.image.p, bytes,
+                                     out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        s = p.finish(st);
+    }
+    p.stats.kernel_launches = (uint32_t)(sr::launches_so_far() - launches0);
+    p.stats.reruns = c->refits;
+    c->hint_valid = s == SR_OK;
+    if (s == SR_OK) {
+        c->hint_C = p.C;
+        c->hint_P = p.P;
+        c->hint_N = p.last_N;
+        c->hint_O = p.last_O;
+        c->hint_largest = p.last_largest;
+    }
+    return s;
 }
 
 sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void* rgba_out, int out_is_device,
