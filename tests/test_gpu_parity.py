@@ -133,26 +133,30 @@ def test_segmented_sort_equals_radix_sort_at_full_size(gpu, oracle_lib):
 
 def test_presized_frames_and_the_overflow_rerun(gpu, oracle_lib):
     """sr_render pre-sizes a frame from the previous frame of a scene with the
-    same curve and path counts and waits only at its end.  A zoomed matrix
-    needs more records than that: the frame overflows and is rerun with exact
-    sizing.  Every image equals the oracle's."""
+    same curve and path counts and waits only at its end.  Going from a
+    half-scale matrix (200k records) to the identity (367k) needs more than
+    that: the frame overflows and is rerun with exact sizing.  Every image
+    equals the oracle's."""
     import oracle
     s = oracle.synth(0, 0)
     d = dict(width=s.width, height=s.height, **{f: getattr(s, f) for f in oracle.Scene.FIELDS})
+    half = np.array([0.5, 0, 0, 256, 0, 0.5, 0, 256, 0, 0, 1, 0, 0, 0, 0, 1], np.float32)
+    ident = np.eye(4, dtype=np.float32).reshape(16)
+    want_half = oracle_lib.Frame(s, mode=1, mvp=half).get("image")
     want_id = oracle_lib.Frame(s, mode=1).get("image")
-    want_zoom = oracle_lib.Frame(s, mode=1, mvp=MVP_ZOOM).get("image")
     r = gpu.ScanlineVGRasterizer(mode=1)
     r.initialize(None, d["width"], d["height"])
     r.loadVG(scenes.to_container(d))
-    assert np.array_equal(r.render(), want_id)      # exact: first frame of the scene
-    assert np.array_equal(r.render(), want_id)      # pre-sized from the first
+    r.setMVP(half)
+    assert np.array_equal(r.render(), want_half)    # exact: first frame of the scene
+    assert np.array_equal(r.render(), want_half)    # pre-sized from the first
     assert r.stats()["reruns"] == 0
-    r.setMVP(MVP_ZOOM)
-    assert np.array_equal(r.render(), want_zoom)    # overflows, rerun exact
+    r.setMVP(ident)
+    assert np.array_equal(r.render(), want_id)      # overflows, rerun exact
     assert r.stats()["reruns"] == 1
-    assert np.array_equal(r.render(), want_zoom)    # pre-sized from the zoomed frame
+    assert np.array_equal(r.render(), want_id)      # pre-sized from the rerun
     r.loadVG(scenes.to_container(d))                # same scene again: still pre-sized
-    r.setMVP(np.eye(4, dtype=np.float32).reshape(16))
-    assert np.array_equal(r.render(), want_id)
+    r.setMVP(half)
+    assert np.array_equal(r.render(), want_half)
     assert r.stats()["reruns"] == 1
     r.close()
