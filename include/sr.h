@@ -563,6 +563,22 @@ sr_status sr_scene_buf_view(const sr_scene_buf* buf, sr_scene_view* view);
 sr_status sr_scene_buf_size(const sr_scene_buf* buf, uint32_t wh[2]);
 void sr_scene_buf_free(sr_scene_buf* buf);
 
+/* ------------------------------------------------------------------ */
+/* Image output (host only).  The reference presents its frame through */
+/* a swapchain (core/scanline/scanline_rasterizer.cpp:610-695); headless */
+/* the frame is an RGBA8 host buffer (sr_render to host memory), which  */
+/* this writes to a file.                                               */
+/* ------------------------------------------------------------------ */
+typedef enum sr_image_format {
+    SR_IMAGE_PNG = 0,   /* truecolour + alpha, stored (uncompressed) deflate */
+    SR_IMAGE_PPM = 1,   /* binary P6, RGB (alpha dropped)                    */
+    SR_IMAGE_PAM = 2    /* P7 RGB_ALPHA                                       */
+} sr_image_format;
+
+/* Writes width x height RGBA8 pixels (row 0 first, 4 x width bytes a row)
+ * to `path`.  Framebuffer row y is scene row y (no vertical flip). */
+sr_status sr_write_image(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height, int format);
+
 /* Page-locked host memory (cudaMallocHost) for full-bandwidth copies of
  * scenes and frames; NULL on failure. */
 void* sr_host_alloc(size_t bytes);

@@ -20,3 +20,15 @@ def test_reference_scene_stages(gpu, oracle_lib, tmp_path, name, mode):
     of, r, img = render_both(gpu, oracle_lib, d, mode)
     compare_all(of, r, img, mode, stages=STAGES_COMMON)
     r.close()
+
+
+def test_rendered_scene_written_as_png(gpu, oracle_lib, tmp_path):
+    """The headless stand-in for the reference's swapchain: the frame read
+    back to host memory and written as a PNG file holds the same pixels."""
+    from test_image_writer import _read_png
+    d, _ = rvg_scenes.load(gpu, "tiger", tmp_path)
+    of, r, img = render_both(gpu, oracle_lib, d, 0)
+    r.close()
+    gpu.write_image(tmp_path / "tiger.png", img)
+    assert img.shape == (d["height"], d["width"], 4)
+    assert (_read_png(tmp_path / "tiger.png") == of.get("image")).all()

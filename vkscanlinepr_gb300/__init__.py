@@ -161,7 +161,7 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_server_create", "sr_server_submit", "sr_server_wait", "sr_server_get_stats", "sr_server_destroy",
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
            "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
-           "sr_debug_scan_without_first_tile"]
+           "sr_debug_scan_without_first_tile", "sr_write_image"]
 
 _lib = None
 
@@ -198,6 +198,7 @@ def lib():
     L.sr_set_spin_limit.argtypes = [ctypes.c_uint32]
     L.sr_set_spin_limit.restype = None
     L.sr_debug_scan_without_first_tile.argtypes = [vp, vp, ctypes.c_int64, vp]
+    L.sr_write_image.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
     L.sr_scene_buf_free.restype = None
     L.sr_scene_buf_size.argtypes = [vp, vp]
     L.sr_host_alloc.argtypes = [ctypes.c_size_t]
@@ -407,6 +408,21 @@ def load_rvg(path):
 def exclusive_scan_i32(d_in, d_out, n, stream=None):
     """Exclusive scan of n int32 at device address d_in into d_out[0..n]."""
     _check(lib().sr_exclusive_scan_i32(d_in, d_out, int(n), stream))
+
+
+IMAGE_FORMATS = {"png": 0, "ppm": 1, "pam": 2}
+
+
+def write_image(path, rgba, fmt=None):
+    """Writes an (H, W, 4) uint8 frame to `path` as PNG, PPM or PAM (from the
+    file's extension unless `fmt` is given)."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    if img.ndim != 3 or img.shape[2] != 4:
+        raise ValueError("expected an (H, W, 4) uint8 array")
+    if fmt is None:
+        fmt = os.path.splitext(str(path))[1].lstrip(".").lower() or "png"
+    _check(lib().sr_write_image(str(path).encode(), img.ctypes.data, img.shape[1], img.shape[0],
+                                IMAGE_FORMATS[fmt]))
 
 
 def scan_status(stream=None):

@@ -16,7 +16,7 @@ LIB = os.path.join(HERE, "libsr.so")
 REPO = os.path.dirname(HERE)
 
 CU_SOURCES = ["geom.cu", "scan.cu", "sort.cu", "winding.cu", "resolve.cu", "mlp.cu", "segsort.cu", "api.cu", "noalloc.cu"]
-CPP_SOURCES = ["host.cpp", "server.cpp"]
+CPP_SOURCES = ["host.cpp", "server.cpp", "image.cpp"]
 HEADERS = ["common.cuh", "kernels.h", "synth.h"]
 
 NVCC = os.environ.get("NVCC", "nvcc")
