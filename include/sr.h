@@ -48,8 +48,17 @@ typedef enum sr_status {
 /* Curve types, same values as Galaxysailing::CurveType
  * (core/vg/vg_container.h:9-15).  QUADRIC is listed as TODO in every
  * reference shader; this library defines it natively (3 control points,
- * monotonised at the derivative root, evaluated by a 2-level lerp). */
-enum { SR_CURVE_LINE = 0x02, SR_CURVE_QUADRIC = 0x03, SR_CURVE_CUBIC = 0x04 };
+ * monotonised at the derivative root, evaluated by a 2-level lerp).
+ * ARC (a TODO in the reference too) is a rational quadratic, the RVG
+ * format's 'A' segment.  It owns 4 point slots: P0, the control point in
+ * homogeneous coordinates (w*x, w*y), P2, and (w, w), with w finite and
+ * w > -1 (w = 0 is a half ellipse).  It is evaluated by a 2-level lerp of
+ * the homogeneous points (x*w, w), then one division, and monotonised at
+ * the roots of its derivative's numerator, a quadratic.  Under the matrix,
+ * P0 and P2 transform as points; the control point transforms linearly as
+ * (w*x, w*y, 0, w), its w becoming the fourth row's result (for an affine
+ * matrix, w itself). */
+enum { SR_CURVE_LINE = 0x02, SR_CURVE_QUADRIC = 0x03, SR_CURVE_CUBIC = 0x04, SR_CURVE_ARC = 0x13 };
 
 /* Fill rules, same values as Galaxysailing::FillRule (vg_container.h:16-19). */
 enum { SR_FILL_NONZERO = 0, SR_FILL_EVENODD = 1 };
@@ -556,6 +565,11 @@ sr_status sr_synth_scene(const sr_synth_params* p, sr_scene_buf** out);
  * M/L/C/Z/fL commands, nzfill/ofill, solid rgb/rgba paint, the last open
  * contour closed by a line; other elements are skipped. */
 sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]);
+
+/* The same reader completed where RVG::load stops (rvg.cpp:160-169,
+ * :234-251): 'A' segments become SR_CURVE_ARC curves and 'Q' segments
+ * quadrics; linear and radial gradient paints are read (see sr_paint). */
+sr_status sr_rvg_load_full(const char* path, sr_scene_buf** out, float viewport[4]);
 
 /* Points `view` at the arrays of `buf` (valid until sr_scene_buf_free). */
 sr_status sr_scene_buf_view(const sr_scene_buf* buf, sr_scene_view* view);

@@ -101,9 +101,16 @@ static inline bool path_visible_mask(int32_t m) {
 }
 
 // Curve evaluation of one coordinate: LINE lerp, QUADRIC 2-level, CUBIC
-// 3-level de Casteljau (make_intersection_1.comp:117-148).
+// 3-level de Casteljau (make_intersection_1.comp:117-148).  ARC (an
+// extension; p = x0, w*x1, x2, w): a 2-level lerp of the homogeneous points
+// (x0, 1), (w*x1, w), (x2, 1), then one division.
 template <class R> static inline R interp(uint32_t type, R t, const R* p) {
     switch (type) {
+        case SR_CURVE_ARC: {
+            R q0 = lerp(p[0], p[1], t), q1 = lerp(p[1], p[2], t);
+            R r0 = lerp((R)1, p[3], t), r1 = lerp(p[3], (R)1, t);
+            return lerp(q0, q1, t) / lerp(r0, r1, t);
+        }
         case SR_CURVE_LINE: return lerp(p[0], p[1], t);
         case SR_CURVE_QUADRIC: {
             R q0 = lerp(p[0], p[1], t), q1 = lerp(p[1], p[2], t);
@@ -231,7 +238,7 @@ template <class R> struct Frame {
 
     const R* pts(uint32_t c, int axis, R* buf) const {
         uint32_t pi = s->curve_pos_map[c];
-        uint32_t np = s->curve_type[c] & 7u;
+        uint32_t np = s->curve_type[c] == SR_CURVE_ARC ? 4u : (s->curve_type[c] & 7u);
         for (uint32_t i = 0; i < 4; ++i) buf[i] = (R)0;
         for (uint32_t i = 0; i < np && i < 4; ++i) buf[i] = tpos[2 * (size_t)(pi + i) + axis];
         return buf;
@@ -281,6 +288,28 @@ template <class R> struct Frame {
                 default: break;
             }
             path_visible[s->pos_path_idx[p]] |= v;
+        }
+        // arcs (an extension): the control slot transforms linearly as
+        // (w*x, w*y, 0, w) with no division, the weight slot becomes the
+        // fourth row's result, and the path is marked visible outright
+        for (uint32_t c = 0; c < s->n_curves; ++c) {
+            if (s->curve_type[c] != SR_CURVE_ARC) continue;
+            const uint32_t f = s->curve_pos_map[c];
+            R hx = (R)s->position[2 * (size_t)(f + 1)], hy = (R)s->position[2 * (size_t)(f + 1) + 1];
+            R w = (R)s->position[2 * (size_t)(f + 3)];
+            R o[4];
+            for (int r = 0; r < 4; ++r) {
+                R acc = hx * mm[4 * r + 0];
+                acc = acc + hy * mm[4 * r + 1];
+                acc = acc + (R)0 * mm[4 * r + 2];
+                acc = acc + w * mm[4 * r + 3];
+                o[r] = acc;
+            }
+            tpos[2 * (size_t)(f + 1)] = o[0];
+            tpos[2 * (size_t)(f + 1) + 1] = o[1];
+            tpos[2 * (size_t)(f + 3)] = o[3];
+            tpos[2 * (size_t)(f + 3) + 1] = o[3];
+            path_visible[s->curve_path_idx[c]] |= 0x11111111;
         }
     }
 
@@ -365,6 +394,15 @@ template <class R> struct Frame {
                         R r0 = (p[0] - p[1]) / den;
                         if (r0 > (R)0 && r0 < (R)1) q[n++] = r0;
                     }
+                } else if (type == SR_CURVE_ARC) {
+                    // extension: roots of the arc's derivative numerator
+                    // N'D - ND' (its cubic terms cancel), halved
+                    R wm1 = p[3] - (R)1;
+                    R r0 = (R)0, r1 = (R)0;
+                    solve_quad<R>(wm1 * (p[2] - p[0]), ((p[0] - p[1]) + (p[2] - p[1])) + ((R)2 * p[0]) * wm1,
+                                  p[1] - p[3] * p[0], r0, r1);
+                    if (r0 > (R)0 && r0 < (R)1) q[n++] = r0;
+                    if (r1 > (R)0 && r1 < (R)1 && r1 != r0) q[n++] = r1;
                 }
             }
             // insertion network, including the reference's `t2 = q3`

@@ -22,10 +22,11 @@ def rvg_file(name, tmpdir):
     return p
 
 
-def load(sr, name, tmpdir):
+def load(sr, name, tmpdir, full=False):
     """(scene dict for scenes.to_oracle/to_container, viewport) of a shipped
-    scene, parsed by the library's RVG reader."""
-    sc, vp = sr.load_rvg(rvg_file(name, tmpdir))
+    scene, parsed by the library's RVG reader (full: with arcs, quadratics
+    and gradients)."""
+    sc, vp = sr.load_rvg(rvg_file(name, tmpdir), full=full)
     a = sc.arrays()
     d = dict(width=int(vp[2]), height=int(vp[3]), **a)
     return d, vp

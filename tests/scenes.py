@@ -8,7 +8,7 @@ import math
 
 import numpy as np
 
-LINE, QUADRIC, CUBIC = 2, 3, 4
+LINE, QUADRIC, CUBIC, ARC = 2, 3, 4, 0x13
 
 
 class Builder:
@@ -241,7 +241,34 @@ def deep_tail(w=2304, h=8):
     return b.arrays()
 
 
+def arcs(w=96, h=80):
+    """A circle of four quarter arcs (w = sqrt(1/2)), a half ellipse closed by
+    its chord (w = 0: the control point at infinity, given in homogeneous
+    form), and an even-odd ring of arcs with w = 2 (hyperbolic) and w = 0.3
+    (elliptic)."""
+    import math
+    b = Builder(w, h)
+    wq = math.sqrt(0.5)
+    cx, cy, r = 28.0, 30.0, 20.0
+    b.path(0, (200, 30, 30, 255))
+    for k in range(4):
+        a0 = k * math.pi / 2
+        a1 = a0 + math.pi / 2
+        p0 = (cx + r * math.cos(a0), cy + r * math.sin(a0))
+        p2 = (cx + r * math.cos(a1), cy + r * math.sin(a1))
+        ctl = (cx + r * (math.cos(a0) + math.cos(a1)), cy + r * (math.sin(a0) + math.sin(a1)))
+        b.curve(ARC, [p0, (ctl[0] * wq, ctl[1] * wq), p2, (wq, wq)])
+    b.path(0, (30, 60, 200, 180))
+    b.curve(ARC, [(60.0, 40.0), (0.0, -25.0), (90.0, 40.0), (0.0, 0.0)])
+    b.curve(LINE, [(90.0, 40.0), (60.0, 40.0)])
+    b.path(1, (20, 160, 40, 200))
+    b.curve(ARC, [(50.0, 70.0), (2 * 70.0, 2 * 52.0), (90.0, 70.0), (2.0, 2.0)])
+    b.curve(ARC, [(90.0, 70.0), (0.3 * 70.0, 0.3 * 78.0), (50.0, 70.0), (0.3, 0.3)])
+    return b.arrays()
+
+
 ALL = {
+    "arcs": arcs,
     "square": square,
     "star_nonzero": lambda: star(rule=0),
     "star_evenodd": lambda: star(rule=1),

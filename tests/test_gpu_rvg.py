@@ -22,6 +22,18 @@ def test_reference_scene_stages(gpu, oracle_lib, tmp_path, name, mode):
     r.close()
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("name", ["car", "chord", "chord-black", "embrace"])
+def test_full_reader_scene_stages(gpu, oracle_lib, tmp_path, name, mode):
+    """The same scenes read in full (arcs as rational quadratics): every stage
+    bit-exact against the oracle, including the arcs' transformed slots,
+    monotonic cuts and bisected crossings."""
+    d, _ = rvg_scenes.load(gpu, name, tmp_path, full=True)
+    of, r, img = render_both(gpu, oracle_lib, d, mode)
+    compare_all(of, r, img, mode, stages=STAGES_COMMON)
+    r.close()
+
+
 def test_rendered_scene_written_as_png(gpu, oracle_lib, tmp_path):
     """The headless stand-in for the reference's swapchain: the frame read
     back to host memory and written as a PNG file holds the same pixels."""

@@ -106,3 +106,18 @@ def test_fp64_restatement_agrees_on_clean_geometry():
         a = render(scenes.mixed_curves(), mode).get("image")
         b = render(scenes.mixed_curves(), mode, fp64=True).get("image")
         assert np.any(a != b, axis=2).sum() <= 2
+
+
+def test_arcs_known_answers(oracle_lib):
+    """Rational quadratic arcs: a circle of four quarter arcs (w = sqrt(1/2))
+    covers pi r^2 pixels up to its boundary; the half ellipse of weight 0
+    reaches 25 px above its chord at its apex; both modes render."""
+    import numpy as np
+    d = scenes.arcs()
+    img = oracle_lib.Frame(scenes.to_oracle(d), mode=oracle_lib.MODE_PIXEL).get("image")
+    circle = np.all(img[:, :, :3] == [200, 30, 30], axis=2)
+    assert abs(int(circle.sum()) - np.pi * 20 ** 2) < 2 * np.pi * 20 * 0.5
+    assert circle[30, 28] and not circle[30, 49] and circle[30, 47]
+    assert not np.all(img[16, 75] == 255) and np.all(img[14, 75] == 255)
+    f0 = oracle_lib.Frame(scenes.to_oracle(d), mode=oracle_lib.MODE_REFERENCE)
+    assert f0.n_intersections > 0 and f0.n_draw > 0

@@ -55,3 +55,30 @@ def test_reference_scenes_render_on_the_oracle(srlib, tmp_path, name):
         f = oracle.Frame(scenes.to_oracle(d), mode=mode)
         assert f.n_intersections > 0 and f.n_draw > 0
         assert f.get("image").shape == (d["height"], d["width"], 4)
+
+
+def test_full_reader_reads_arcs_and_quadratics(srlib, tmp_path):
+    """The full reader keeps what RVG::load drops: 'A' segments as arcs
+    (4 slots: P0, homogeneous control point, P2, (w, w)) and 'Q' segments."""
+    p = tmp_path / "arc.rvg"
+    p.write_text("""viewport 0,0 40,30
+window 0,0 40,30
+scene dyn_identity
+  1 element nzfill dyn_concrete 0,0 0,0 0,0: M 2,20 A 0,-10,0 30,20 Q 16,28 2,20 Z dyn_identity dyn_paint 1 solid rgba(1,0,0,1)
+""")
+    ref, _ = srlib.load_rvg(str(p))
+    assert ref.arrays()["curve_type"].size == 0          # the reference reader stops at the 'A'
+    sc, vp = srlib.load_rvg(str(p), full=True)
+    a = sc.arrays()
+    assert a["curve_type"].tolist() == [0x13, 3]
+    pos = a["position"].reshape(-1, 2)
+    assert pos[:4].tolist() == [[2, 20], [0, -10], [30, 20], [0, 0]]
+    assert pos[4:7].tolist() == [[30, 20], [16, 28], [2, 20]]
+
+
+@pytest.mark.parametrize("name,arcs", [("car", 124), ("chord", 9312), ("chord-black", 9312), ("drops", 0)])
+def test_full_reader_on_reference_scenes(srlib, tmp_path, name, arcs):
+    d, _ = rvg_scenes.load(srlib, name, tmp_path, full=True)
+    assert int((d["curve_type"] == 0x13).sum()) == arcs
+    w = d["position"].reshape(-1, 2)[d["curve_pos_map"][d["curve_type"] == 0x13] + 3]
+    assert np.all(w[:, 0] == w[:, 1]) and np.all(w[:, 0] > -1)

@@ -161,7 +161,7 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_server_create", "sr_server_submit", "sr_server_wait", "sr_server_get_stats", "sr_server_destroy",
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
            "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
-           "sr_debug_scan_without_first_tile", "sr_write_image"]
+           "sr_debug_scan_without_first_tile", "sr_write_image", "sr_rvg_load_full"]
 
 _lib = None
 
@@ -192,6 +192,7 @@ def lib():
     L.sr_last_error.restype = ctypes.c_char_p
     L.sr_synth_scene.argtypes = [ctypes.POINTER(SynthParams), ctypes.POINTER(vp)]
     L.sr_rvg_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
+    L.sr_rvg_load_full.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
     L.sr_scene_buf_view.argtypes = [vp, ctypes.POINTER(SceneView)]
     L.sr_scene_buf_free.argtypes = [vp]
     L.sr_scan_status.argtypes = [vp]
@@ -392,13 +393,15 @@ def synth_scene(preset, seed, scene_index=0, width=0, height=0, n_paths=0):
         L.sr_scene_buf_free(h)
 
 
-def load_rvg(path):
-    """Read an .rvg file the way the reference's RVG::load does; returns
+def load_rvg(path, full=False):
+    """Read an .rvg file the way the reference's RVG::load does, or with
+    full=True also its arcs, quadratics and gradient paints; returns
     (container, viewport[4])."""
     L = lib()
     h = ctypes.c_void_p()
     vp = np.zeros(4, np.float32)
-    _check(L.sr_rvg_load(path.encode(), ctypes.byref(h), vp.ctypes.data))
+    fn = L.sr_rvg_load_full if full else L.sr_rvg_load
+    _check(fn(path.encode(), ctypes.byref(h), vp.ctypes.data))
     try:
         return _from_buf(h), vp
     finally:

@@ -159,10 +159,16 @@ static sr_status validate_scene(const sr_scene_view* s) {
     if (C > (1u << 27) || V > (1u << 29) || P > (1u << 26)) return fail(SR_ERR_INVALID_ARG, "scene too large");
     for (uint32_t i = 0; i < C; ++i) {
         uint32_t t = s->curve_type[i];
-        if (t != SR_CURVE_LINE && t != SR_CURVE_QUADRIC && t != SR_CURVE_CUBIC)
+        if (t != SR_CURVE_LINE && t != SR_CURVE_QUADRIC && t != SR_CURVE_CUBIC && t != SR_CURVE_ARC)
             return fail(SR_ERR_INVALID_ARG, "curve %u: unsupported type 0x%x", i, t);
-        if ((uint64_t)s->curve_pos_map[i] + (t & 7u) > V)
+        const uint32_t slots = t == SR_CURVE_ARC ? 4u : (t & 7u);
+        if ((uint64_t)s->curve_pos_map[i] + slots > V)
             return fail(SR_ERR_INVALID_ARG, "curve %u: control points out of range", i);
+        if (t == SR_CURVE_ARC) {
+            const float* w = s->position + 2 * ((size_t)s->curve_pos_map[i] + 3);
+            if (!(w[0] > -1.0f) || w[0] != w[1])
+                return fail(SR_ERR_INVALID_ARG, "curve %u: arc weight must be (w, w) with w > -1", i);
+        }
         if (s->curve_path_idx[i] >= P) return fail(SR_ERR_INVALID_ARG, "curve %u: path index out of range", i);
         if (i > 0 && s->curve_path_idx[i] < s->curve_path_idx[i - 1])
             return fail(SR_ERR_INVALID_ARG, "curves must be grouped by path in path order");
@@ -209,6 +215,7 @@ struct Pipeline {
     int32_t mode = SR_MODE_PIXEL, F = 1;
     uint32_t flags = 0;
     bool loaded = false;
+    bool arcs = false;   // the scene set has SR_CURVE_ARC curves
     sr_tuning tune{sizeof(sr_tuning), 12, 8, 8, 0};
     // segmented sort of this frame: merge rounds (-1: radix sort instead) and
     // the largest segment the tables accept without flagging an overflow
@@ -376,6 +383,7 @@ struct Pipeline {
         CUDA_TRY(up(fill_rule, h.fill_rule.data(), sizeof(uint32_t) * P));
         CUDA_TRY(up(fill_info, h.fill_info.data(), sizeof(uint32_t) * P));
         CUDA_TRY(up(path_scene, h.path_scene.data(), sizeof(uint32_t) * P));
+        arcs = std::find(h.curve_type.begin(), h.curve_type.end(), (uint32_t)SR_CURVE_ARC) != h.curve_type.end();
         SR_TRY(upload_table());
         loaded = true;
         stages_valid = false;
@@ -418,6 +426,8 @@ struct Pipeline {
         CUDA_TRY(up(fill_rule, s->fill_rule, sizeof(uint32_t) * P));
         CUDA_TRY(up(fill_info, s->fill_info, sizeof(uint32_t) * P));
         CUDA_TRY(cudaMemset(path_scene.p, 0, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
+        arcs = s->n_curves && std::find(s->curve_type, s->curve_type + s->n_curves, (uint32_t)SR_CURVE_ARC) !=
+                                  s->curve_type + s->n_curves;
         SR_TRY(upload_table());
         loaded = true;
         stages_valid = false;
@@ -631,6 +641,9 @@ struct Pipeline {
         mark(ST_TRANSFORM, false);
         launch_transform(pos.as<float2>(), pos_path.as<uint32_t>(), V, table(), tpos.as<float2>(),
                          path_visible.as<int32_t>(), st);
+        if (arcs)
+            launch_arc_fixup(curve_type.as<uint32_t>(), curve_pos.as<uint32_t>(), curve_path.as<uint32_t>(), C,
+                             pos.as<float2>(), table(), tpos.as<float2>(), path_visible.as<int32_t>(), st);
         mark(ST_TRANSFORM, true);
         const GeomArgs g = geom(0);
         const ChainWork cw = chain_work();
@@ -1737,6 +1750,9 @@ sr_status sr_batch_path_features(sr_batch* b, float* d_feats, void* stream) {
     CUDA_TRY(cudaMemsetAsync(p.path_visible.p, 0, sizeof(int32_t) * std::max<uint32_t>(p.P, 1), st));
     sr::launch_transform(p.pos.as<float2>(), p.pos_path.as<uint32_t>(), p.V, p.table(), p.tpos.as<float2>(),
                          p.path_visible.as<int32_t>(), st);
+    if (p.arcs)
+        sr::launch_arc_fixup(p.curve_type.as<uint32_t>(), p.curve_pos.as<uint32_t>(), p.curve_path.as<uint32_t>(), p.C,
+                             p.pos.as<float2>(), p.table(), p.tpos.as<float2>(), p.path_visible.as<int32_t>(), st);
     sr::launch_path_features(p.geom(0), p.path_first.as<uint32_t>(), p.P, d_feats, st);
     CUDA_TRY(cudaGetLastError());
     return SR_OK;

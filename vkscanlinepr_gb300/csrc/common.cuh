@@ -51,8 +51,20 @@ SR_DEV bool path_visible_mask(int32_t m) {
     return !inv;
 }
 
-// Coordinate of a curve at t: line lerp, quadric 2-level, cubic 3-level.
+// Curve type of a rational quadratic (SR_CURVE_ARC): 4 point slots, the
+// last holding its weight.
+constexpr uint32_t kArc = 0x13u;
+SR_DEV uint32_t curve_slots(uint32_t type) { return type == kArc ? 4u : (type & 7u); }
+
+// Coordinate of a curve at t: line lerp, quadric 2-level, cubic 3-level; an
+// arc (p = x0, w*x1, x2, w) a 2-level lerp of the homogeneous points
+// (x0, 1), (w*x1, w), (x2, 1), then one division.
 SR_DEV float interp(uint32_t type, float t, const float* p) {
+    if (type == kArc) {
+        const float q0 = lerp_rn(p[0], p[1], t), q1 = lerp_rn(p[1], p[2], t);
+        const float r0 = lerp_rn(1.0f, p[3], t), r1 = lerp_rn(p[3], 1.0f, t);
+        return __fdiv_rn(lerp_rn(q0, q1, t), lerp_rn(r0, r1, t));
+    }
     if (type == 2u) return lerp_rn(p[0], p[1], t);
     if (type == 3u) {
         float q0 = lerp_rn(p[0], p[1], t), q1 = lerp_rn(p[1], p[2], t);

@@ -68,13 +68,43 @@ __global__ void __launch_bounds__(256) k_transform(const float2* __restrict__ po
     if (i < n_points && run_end && v != 0) atomicOr(&path_visible[pidx], v);
 }
 
+// Arcs, after k_transform (which took every slot for a point): the control
+// slot (w*x, w*y) transforms linearly as (w*x, w*y, 0, w), the same dot
+// products in the same order, with no division; the weight slot becomes the
+// fourth row's result.  An arc with w <= 0 can leave the hull of its slots,
+// so the region codes cannot cull it: its path is marked visible outright.
+__global__ void __launch_bounds__(256) k_arc_fixup(const uint32_t* __restrict__ curve_type,
+                                                   const uint32_t* __restrict__ curve_pos,
+                                                   const uint32_t* __restrict__ curve_path, uint32_t n_curves,
+                                                   const float2* __restrict__ pos, const SceneTable t,
+                                                   float2* __restrict__ tpos, int32_t* __restrict__ path_visible) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_curves || curve_type[c] != kArc) return;
+    const uint32_t first = curve_pos[c], path = curve_path[c];
+    const SceneInfo& si = scene_of_path(t, path);
+    const float2 h = pos[first + 1];
+    const float w = pos[first + 3].x;
+    float o[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float acc = __fmul_rn(h.x, si.mvp[4 * r + 0]);
+        acc = __fadd_rn(acc, __fmul_rn(h.y, si.mvp[4 * r + 1]));
+        acc = __fadd_rn(acc, __fmul_rn(0.0f, si.mvp[4 * r + 2]));
+        acc = __fadd_rn(acc, __fmul_rn(w, si.mvp[4 * r + 3]));
+        o[r] = acc;
+    }
+    tpos[first + 1] = make_float2(o[0], o[1]);
+    tpos[first + 3] = make_float2(o[3], o[3]);
+    atomicOr(&path_visible[path], 0x11111111);
+}
+
 // ------------------------------------------------- shared curve helpers --
 struct CurvePts {
     float x[4], y[4];
 };
 
 SR_DEV void load_curve(const float2* __restrict__ tpos, uint32_t first, uint32_t type, CurvePts& c) {
-    uint32_t np = type & 7u;
+    uint32_t np = curve_slots(type);
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
         float2 p = make_float2(0.0f, 0.0f);
@@ -144,11 +174,11 @@ SR_DEV int32_t piece_ny(uint32_t n) { return (int32_t)((n >> 16) & 0x7FFFu); }
 SR_DEV uint32_t chain_key(int32_t len, uint32_t type) {
     uint32_t lg = 31u - (uint32_t)__clz(len);
     if (lg > 14u) lg = 14u;
-    if (type != 3u && type != 4u) lg = lg > 7u ? lg - 7u : 0u;
-    uint32_t cls = type == 4u ? 0u : (type == 3u ? 1u : 2u);
+    if (type == 2u) lg = lg > 7u ? lg - 7u : 0u;
+    uint32_t cls = type == 4u ? 0u : (type == 3u ? 1u : (type == kArc ? 3u : 2u));
     return ((14u - lg) << 2) | cls;
 }
-// Cubic and quadric chains of >= 512 bisected roots (class >= 9) are solved
+// Cubic, quadric and arc chains of >= 512 bisected roots (class >= 9) are solved
 // by a whole warp each (run_chain_warp); they sort before every other chain.
 SR_DEV bool chain_key_wide(uint32_t key) { return (key >> 2) <= 14u - 9u && (key & 3u) != 2u; }
 constexpr uint32_t kChainKeyBits = 6;
@@ -221,6 +251,18 @@ __global__ void __launch_bounds__(256) k_count(const GeomArgs g, float* __restri
                         float r0 = __fdiv_rn(__fsub_rn(p[0], p[1]), den);
                         if (r0 > 0.0f && r0 < 1.0f) q[n++] = r0;
                     }
+                } else if (type == kArc) {
+                    // roots of the derivative's numerator N'D - ND' (a
+                    // quadratic; its cubic terms cancel), halved:
+                    // (w-1)(x2-x0) t^2 + ((x0-x1) + (x2-x1) + 2 x0 (w-1)) t + (x1 - w x0)
+                    const float wm1 = __fsub_rn(p[3], 1.0f);
+                    float r0 = 0.0f, r1 = 0.0f;
+                    solve_quad(__fmul_rn(wm1, __fsub_rn(p[2], p[0])),
+                               __fadd_rn(__fadd_rn(__fsub_rn(p[0], p[1]), __fsub_rn(p[2], p[1])),
+                                         __fmul_rn(__fmul_rn(2.0f, p[0]), wm1)),
+                               __fsub_rn(p[1], __fmul_rn(p[3], p[0])), r0, r1);
+                    if (r0 > 0.0f && r0 < 1.0f) q[n++] = r0;
+                    if (r1 > 0.0f && r1 < 1.0f && r1 != r0) q[n++] = r1;
                 }
             }
             // insertion network of make_intersection_0.comp:315-359, including
@@ -370,6 +412,15 @@ struct AxisPoly {
 
 template <int kType> SR_DEV float eval_axis(const AxisPoly& a, float t) {
     if (kType == 2) return __fadd_rn(a.p0, __fmul_rn(t, a.d01));
+    if (kType == (int)kArc) {
+        // as interp(): the homogeneous lerps, then the division (p3 = w)
+        float q0 = __fadd_rn(a.p0, __fmul_rn(t, a.d01));
+        float q1 = __fadd_rn(a.p1, __fmul_rn(t, a.d12));
+        float r0 = __fadd_rn(1.0f, __fmul_rn(t, __fsub_rn(a.p3, 1.0f)));
+        float r1 = __fadd_rn(a.p3, __fmul_rn(t, __fsub_rn(1.0f, a.p3)));
+        return __fdiv_rn(__fadd_rn(q0, __fmul_rn(t, __fsub_rn(q1, q0))),
+                         __fadd_rn(r0, __fmul_rn(t, __fsub_rn(r1, r0))));
+    }
     float q0 = __fadd_rn(a.p0, __fmul_rn(t, a.d01));
     float q1 = __fadd_rn(a.p1, __fmul_rn(t, a.d12));
     if (kType == 3) return __fadd_rn(q0, __fmul_rn(t, __fsub_rn(q1, q0)));
@@ -583,7 +634,7 @@ SR_DEV ChainSetup chain_setup(const GeomArgs& g, const int32_t* __restrict__ off
     s.t_lo = piece == 0 ? 0.0f : __uint_as_float(pt[piece - 1].y);
     s.t_hi = __uint_as_float(me.y);
     const float2* cp = g.tpos + g.curve_pos[c];
-    const uint32_t np = s.type & 7u;
+    const uint32_t np = curve_slots(s.type);
     float p[4];
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) {
@@ -622,6 +673,8 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
             int32_t* out = cbuf + s.base;
             if (s.type == 4u) run_chain_warp<4>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
             else if (s.type == 3u) run_chain_warp<3>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
+            else if (s.type == kArc)
+                run_chain_warp<(int)kArc>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out, tl);
         }
         return;
     }
@@ -638,6 +691,7 @@ __global__ void __launch_bounds__(128) k_chains(const GeomArgs g, const int32_t*
         int32_t* out = cbuf + s.base;
         if (s.type == 2u) run_chain<2>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
         else if (s.type == 3u) run_chain<3>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
+        else if (s.type == kArc) run_chain<(int)kArc>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
         else run_chain<4>(s.a, s.len, s.x, s.dx, s.t_lo, s.t_hi, s.side, out);
     }
 }
@@ -1017,6 +1071,15 @@ __global__ void __launch_bounds__(256) k_fragment(const GeomArgs g, const int2* 
 }
 
 // -------------------------------------------------------------- launches --
+void launch_arc_fixup(const uint32_t* curve_type, const uint32_t* curve_pos, const uint32_t* curve_path,
+                      uint32_t n_curves, const float2* pos, const SceneTable& t, float2* tpos, int32_t* path_visible,
+                      cudaStream_t st) {
+    if (n_curves == 0) return;
+    count_launches(1);
+    k_arc_fixup<<<(n_curves + 255) / 256, 256, 0, st>>>(curve_type, curve_pos, curve_path, n_curves, pos, t, tpos,
+                                                        path_visible);
+}
+
 void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const SceneTable& t,
                       float2* tpos, int32_t* path_visible, cudaStream_t st) {
     if (n_points == 0) return;

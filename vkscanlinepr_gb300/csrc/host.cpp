@@ -95,11 +95,17 @@ struct PathRec {
     uint32_t rule = 0;
     float color[4] = {0.f, 0.f, 0.f, 1.f};
     float opacity = 0.f;
+    bool gradient = false;   // a gradient paint (full reader)
 };
 
 }  // namespace
 
-extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]) {
+// full = false: exactly the reference reader's behaviour.  full = true adds
+// what RVG::load leaves out (rvg.cpp:160-169, :234-251): 'A' (a rational
+// quadratic, "A x,y,w x2,y2": the control point in homogeneous coordinates,
+// then the end point) as SR_CURVE_ARC, 'Q' as SR_CURVE_QUADRIC, and linear
+// and radial gradient paints, which are consumed whole.
+static sr_status rvg_parse(const char* path, bool full, sr_scene_buf** out, float viewport[4]) {
     if (!path || !out) return SR_ERR_INVALID_ARG;
     std::ifstream fin(path);
     if (!fin.is_open()) {
@@ -136,7 +142,8 @@ extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float vie
     auto add_curve = [&](uint32_t type, const Pt* p) {
         curve_first.push_back((uint32_t)pts.size());
         curve_type.push_back(type);
-        for (uint32_t k = 0; k < (type & 7u); ++k) pts.push_back(p[k]);
+        const uint32_t np = type == SR_CURVE_ARC ? 4u : (type & 7u);
+        for (uint32_t k = 0; k < np; ++k) pts.push_back(p[k]);
     };
 
     while (tk.next(t)) {
@@ -170,8 +177,30 @@ extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float vie
         while (tk.next(t)) {
             if (t != "fL" && t.size() != 1) break;
             char cmd = t[0];
-            if (std::string("MmZzLlCcAa").find(cmd) == std::string::npos && t != "fL") break;
+            if (std::string(full ? "MmZzLlCcAaQq" : "MmZzLlCcAa").find(cmd) == std::string::npos && t != "fL") break;
             std::string a, b, c;
+            if (full && cmd == 'A') {
+                // control point (x, y, w) in homogeneous coordinates, then the end point
+                tk.next(a);
+                tk.next(b);
+                for (char& ch : a)
+                    if (ch == ',') ch = ' ';
+                float hx = 0.f, hy = 0.f, hw = 1.f;
+                std::sscanf(a.c_str(), "%f %f %f", &hx, &hy, &hw);
+                Pt q[4] = {p[0], Pt{hx, hy}, parse_point(b), Pt{hw, hw}};
+                add_curve(SR_CURVE_ARC, q);
+                p[0] = q[2];
+                continue;
+            }
+            if (full && cmd == 'Q') {
+                tk.next(a);
+                tk.next(b);
+                p[1] = parse_point(a);
+                p[2] = parse_point(b);
+                add_curve(SR_CURVE_QUADRIC, p);
+                p[0] = p[2];
+                continue;
+            }
             switch (cmd) {
                 case 'M':
                     tk.next(a);
@@ -208,7 +237,9 @@ extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float vie
         }
         // the last contour, if open, is closed by a straight line (rvg.cpp:211-223)
         if (!closed && pts.size() > contour_begin) {
-            Pt first = pts[contour_begin], last = pts.back();
+            // an arc's last slot is its weight: its end point is the slot before
+            const bool arc_last = curve_type.back() == SR_CURVE_ARC && full;
+            Pt first = pts[contour_begin], last = arc_last ? pts[pts.size() - 2] : pts.back();
             if (first.x != last.x || first.y != last.y) {
                 Pt q[2] = {last, first};
                 add_curve(SR_CURVE_LINE, q);
@@ -222,7 +253,13 @@ extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float vie
             pr.opacity = (float)std::strtod(o.c_str(), nullptr);
         }
         tk.next(t);
-        if (t == "solid") {
+        if (full && (t == "linear" || t == "radial")) {
+            // "gradient", the geometry, "dyn_ramp", the stops, the spread,
+            // then "dyn_affine(...)", which ends the paint
+            pr.gradient = true;
+            while (tk.next(t) && t.compare(0, 10, "dyn_affine") != 0) {
+            }
+        } else if (t == "solid") {
             tk.next(t);
             std::string inner;
             bool rgba = t.compare(0, 4, "rgba") == 0;
@@ -263,6 +300,7 @@ extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float vie
         }
         uint32_t c = (uint32_t)b8[0] | ((uint32_t)b8[1] << 8) | ((uint32_t)b8[2] << 16) | ((uint32_t)b8[3] << 24);
         if (!(c & 0xFF000000u)) c = 0;
+        if (pr.gradient) c = 0;
         s.fill_rule.push_back(pr.rule);
         s.fill_info.push_back(c);
         for (uint32_t ci = cb; ci < ce; ++ci) {
@@ -292,4 +330,12 @@ extern "C" void* sr_host_alloc(size_t bytes) {
 }
 extern "C" void sr_host_free(void* p) {
     if (p) cudaFreeHost(p);
+}
+
+extern "C" sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]) {
+    return rvg_parse(path, false, out, viewport);
+}
+
+extern "C" sr_status sr_rvg_load_full(const char* path, sr_scene_buf** out, float viewport[4]) {
+    return rvg_parse(path, true, out, viewport);
 }

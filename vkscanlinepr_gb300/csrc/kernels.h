@@ -103,6 +103,10 @@ size_t piece_table_bytes(uint32_t n_curves);
 uint32_t chain_key_bits();
 uint32_t chain_list_capacity(uint32_t n_curves);
 
+// Arcs' control and weight slots after launch_transform (SR_CURVE_ARC).
+void launch_arc_fixup(const uint32_t* curve_type, const uint32_t* curve_pos, const uint32_t* curve_path,
+                      uint32_t n_curves, const float2* pos, const SceneTable& t, float2* tpos, int32_t* path_visible,
+                      cudaStream_t st);
 void launch_transform(const float2* pos, const uint32_t* pos_path, uint32_t n_points, const SceneTable& t,
                       float2* tpos, int32_t* path_visible, cudaStream_t st);
 void launch_count(const GeomArgs& g, float* cut_cache, int32_t* count, const ChainWork& w, uint32_t* status,
