@@ -63,6 +63,42 @@ enum { SR_CURVE_LINE = 0x02, SR_CURVE_QUADRIC = 0x03, SR_CURVE_CUBIC = 0x04, SR_
 /* Fill rules, same values as Galaxysailing::FillRule (vg_container.h:16-19). */
 enum { SR_FILL_NONZERO = 0, SR_FILL_EVENODD = 1 };
 
+/* Gradient paints (the RVG format's linear and radial "dyn_paint", which
+ * RVG::load skips, rvg.cpp:234-251).  A path painted by paint i of the
+ * context's table (sr_set_paints) has fill_info SR_FILL_PAINT(i): alpha byte
+ * 0 and i + 1 in the colour bytes (a solid colour with alpha 0 is stored as
+ * 0, so the two never meet).
+ *
+ * Evaluation, identical in the renderer and the oracle: a pixel's centre
+ * (x + 0.5, y + 0.5) -- in reference mode (x + 0.5, cell_y + 1), the centre
+ * row of the 2-pixel cell -- is mapped to gradient space by the inverse of
+ * (the matrix's affine part) * xf, computed in double and rounded to float
+ * once per paint; then in float: linear t = the projection on p0 -> p1
+ * (folded into one affine form of the pixel); radial t solves
+ * |g - f - t (c - f)| = t r (focus f = p1, centre c = p0; the root the
+ * focus-inside case takes; t = 0 where none exists); the spread (pad clamps
+ * to [0, 1], repeat takes t - floor t, reflect folds it); the colour is the
+ * linear interpolation between the two stops around t (the first or last
+ * stop outside them); alpha is multiplied by opacity; each channel is packed
+ * as u8(v * 255) truncated, and alpha 0 leaves the pixel alone (pixel mode)
+ * or writes 0 (reference mode, whose overwrite writes alpha raw). */
+#define SR_PAINT_MAX_STOPS 16
+enum { SR_PAINT_LINEAR = 1, SR_PAINT_RADIAL = 2 };
+enum { SR_SPREAD_PAD = 0, SR_SPREAD_REPEAT = 1, SR_SPREAD_REFLECT = 2 };
+typedef struct sr_paint {
+    int32_t  kind;          /* SR_PAINT_LINEAR or SR_PAINT_RADIAL              */
+    int32_t  spread;        /* SR_SPREAD_*                                      */
+    float    p0[2];         /* linear: start point; radial: centre              */
+    float    p1[2];         /* linear: end point; radial: focus                 */
+    float    radius;        /* radial                                           */
+    float    xf[6];         /* gradient -> scene: (xf0 x + xf1 y + xf2, xf3 x + xf4 y + xf5) */
+    float    opacity;       /* multiplies every stop's alpha                     */
+    uint32_t n_stops;       /* 1..SR_PAINT_MAX_STOPS, offsets non-decreasing     */
+    float    offset[SR_PAINT_MAX_STOPS];
+    float    rgba[SR_PAINT_MAX_STOPS][4];   /* each channel in [0, 1]          */
+} sr_paint;
+#define SR_FILL_PAINT(i) ((uint32_t)(i) + 1u)
+
 /* Render modes.
  * SR_MODE_REFERENCE: the reference's own semantics — 2-px fragment grid
  *   (FRAG_SIZE 2), winding sampled on the line y = cell_y + 1, every boundary
@@ -127,6 +163,11 @@ sr_status sr_load_scene(sr_ctx* ctx, const sr_scene_view* scene);
  * given transpose(camera.mv()) as the application passes it
  * (app/vg_app.cpp:159-160). */
 sr_status sr_set_mvp(sr_ctx* ctx, const float m[16]);
+
+/* Sets the gradient paints the loaded scene's SR_FILL_PAINT(i) fills refer
+ * to (copied; they follow later sr_set_mvp calls).  n = 0 clears the table;
+ * a fill that names no paint of the table paints nothing. */
+sr_status sr_set_paints(sr_ctx* ctx, const sr_paint* paints, uint32_t n);
 
 /* Replaces VGRasterizer::render (rasterizer.h:13).  Renders one frame on
  * `stream` (a cudaStream_t, NULL for the legacy default stream) into
@@ -570,6 +611,10 @@ sr_status sr_rvg_load(const char* path, sr_scene_buf** out, float viewport[4]);
  * :234-251): 'A' segments become SR_CURVE_ARC curves and 'Q' segments
  * quadrics; linear and radial gradient paints are read (see sr_paint). */
 sr_status sr_rvg_load_full(const char* path, sr_scene_buf** out, float viewport[4]);
+
+/* The gradient paints a scene read by sr_rvg_load_full refers to (*n = 0
+ * for other scenes); valid until sr_scene_buf_free. */
+sr_status sr_scene_buf_paints(const sr_scene_buf* buf, const sr_paint** paints, uint32_t* n);
 
 /* Points `view` at the arrays of `buf` (valid until sr_scene_buf_free). */
 sr_status sr_scene_buf_view(const sr_scene_buf* buf, sr_scene_view* view);

@@ -60,6 +60,14 @@ class SceneView(ctypes.Structure):
     ]
 
 
+class Paint(ctypes.Structure):
+    """sr_paint (include/sr.h): a linear or radial gradient."""
+    _fields_ = [("kind", ctypes.c_int32), ("spread", ctypes.c_int32), ("p0", ctypes.c_float * 2),
+                ("p1", ctypes.c_float * 2), ("radius", ctypes.c_float), ("xf", ctypes.c_float * 6),
+                ("opacity", ctypes.c_float), ("n_stops", ctypes.c_uint32), ("offset", ctypes.c_float * 16),
+                ("rgba", (ctypes.c_float * 4) * 16)]
+
+
 class SynthParams(ctypes.Structure):
     _fields_ = [
         ("struct_size", ctypes.c_uint32), ("preset", ctypes.c_int32),
@@ -80,6 +88,9 @@ def lib():
         L.or_render.argtypes = [ctypes.POINTER(SceneView), ctypes.c_uint32, ctypes.c_uint32,
                                 ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.POINTER(ctypes.c_void_p)]
+        L.or_render_paints.argtypes = [ctypes.POINTER(SceneView), ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
         L.or_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
                              ctypes.POINTER(ctypes.c_size_t)]
         L.or_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -103,7 +114,8 @@ class Scene:
               "curve_path_idx", "fill_rule", "fill_info")
 
     def __init__(self, width, height, position, pos_path_idx, curve_pos_map, curve_type,
-                 curve_path_idx, fill_rule, fill_info):
+                 curve_path_idx, fill_rule, fill_info, paints=None):
+        self.paints = paints   # gradient paints: a ctypes array of sr_paint-layout structs, or None
         self.width = int(width)
         self.height = int(height)
         self.position = np.ascontiguousarray(position, dtype=np.float32).reshape(-1)
@@ -181,8 +193,10 @@ class Frame:
         self.width, self.height, self.mode, self.fp64 = w, h, mode, fp64
         v = scene.view()
         hd = ctypes.c_void_p()
-        rc = L.or_render(ctypes.byref(v), w, h, m.ctypes.data, mode, threads, 1 if fp64 else 0,
-                         ctypes.byref(hd))
+        paints = getattr(scene, "paints", None)
+        rc = L.or_render_paints(ctypes.byref(v), w, h, m.ctypes.data, mode, threads, 1 if fp64 else 0,
+                                ctypes.cast(paints, ctypes.c_void_p) if paints else None,
+                                len(paints) if paints else 0, ctypes.byref(hd))
         self._h = hd
         if rc != 0:
             raise RuntimeError("oracle render failed (%d)" % rc)

@@ -209,6 +209,119 @@ struct Rec {
     int64_t tb;   // t bits | flags (float: low 32 bits used)
 };
 
+// ---- gradient paints (an extension; sr.h gives the definition) --------
+// A paint for the resolve: the pixel -> gradient map in double, rounded to
+// float once, then float arithmetic per pixel.
+struct OPaint {
+    int kind = 1, spread = 0, n = 0;
+    float lin[3] = {0, 0, 0}, m[6] = {0, 0, 0, 0, 0, 0};
+    float fx = 0, fy = 0, dx = 0, dy = 0, A = 0, opacity = 0;
+    float off[SR_PAINT_MAX_STOPS] = {};
+    float rgba[SR_PAINT_MAX_STOPS][4] = {};
+};
+
+static OPaint make_paint(const sr_paint& p, const float* m) {
+    OPaint d;
+    d.kind = p.kind == SR_PAINT_RADIAL ? 2 : 1;
+    d.spread = p.spread == SR_SPREAD_REPEAT ? 1 : p.spread == SR_SPREAD_REFLECT ? 2 : 0;
+    const double A0 = m[0], A1 = m[1], A2 = m[3], A3 = m[4], A4 = m[5], A5 = m[7];
+    const double X0 = p.xf[0], X1 = p.xf[1], X2 = p.xf[2], X3 = p.xf[3], X4 = p.xf[4], X5 = p.xf[5];
+    const double F0 = A0 * X0 + A1 * X3, F1 = A0 * X1 + A1 * X4, F2 = (A0 * X2 + A1 * X5) + A2;
+    const double F3 = A3 * X0 + A4 * X3, F4 = A3 * X1 + A4 * X4, F5 = (A3 * X2 + A4 * X5) + A5;
+    const double det = F0 * F4 - F1 * F3;
+    const uint32_t ns = p.n_stops > SR_PAINT_MAX_STOPS ? SR_PAINT_MAX_STOPS : p.n_stops;
+    if (det == 0.0 || !std::isfinite(det)) return d;
+    const double G0 = F4 / det, G1 = -F1 / det, G3 = -F3 / det, G4 = F0 / det;
+    const double G2 = -(G0 * F2 + G1 * F5), G5 = -(G3 * F2 + G4 * F5);
+    if (d.kind == 1) {
+        const double dx = (double)p.p1[0] - p.p0[0], dy = (double)p.p1[1] - p.p0[1];
+        const double l2 = dx * dx + dy * dy;
+        if (l2 > 0.0) {
+            d.lin[0] = (float)((G0 * dx + G3 * dy) / l2);
+            d.lin[1] = (float)((G1 * dx + G4 * dy) / l2);
+            d.lin[2] = (float)(((G2 - p.p0[0]) * dx + (G5 - p.p0[1]) * dy) / l2);
+        }
+    } else {
+        const double G[6] = {G0, G1, G2, G3, G4, G5};
+        for (int k = 0; k < 6; ++k) d.m[k] = (float)G[k];
+        const double dx = (double)p.p0[0] - p.p1[0], dy = (double)p.p0[1] - p.p1[1];
+        d.fx = p.p1[0];
+        d.fy = p.p1[1];
+        d.dx = (float)dx;
+        d.dy = (float)dy;
+        d.A = (float)(dx * dx + dy * dy - (double)p.radius * p.radius);
+    }
+    d.opacity = p.opacity;
+    d.n = (int)ns;
+    for (uint32_t k = 0; k < ns; ++k) {
+        d.off[k] = p.offset[k];
+        for (int q = 0; q < 4; ++q) d.rgba[k][q] = p.rgba[k][q];
+    }
+    return d;
+}
+
+// Colour of paint P at the pixel-space point (x, y), packed RGBA8, 0 when
+// transparent; every float operation one IEEE operation in this order.
+static uint32_t paint_color(const OPaint& P, float x, float y) {
+    float t;
+    if (P.kind == 1) {
+        t = (P.lin[0] * x + P.lin[1] * y) + P.lin[2];
+    } else {
+        const float gx = (P.m[0] * x + P.m[1] * y) + P.m[2];
+        const float gy = (P.m[3] * x + P.m[4] * y) + P.m[5];
+        const float ex = gx - P.fx, ey = gy - P.fy;
+        const float b = ex * P.dx + ey * P.dy;
+        const float c = ex * ex + ey * ey;
+        if (P.A == 0.0f) {
+            t = b != 0.0f ? c / (2.0f * b) : 0.0f;
+        } else {
+            const float disc = b * b - P.A * c;
+            if (disc < 0.0f) {
+                t = 0.0f;
+            } else {
+                const float sq = std::sqrt(disc);
+                t = (P.A < 0.0f ? b - sq : b + sq) / P.A;
+            }
+        }
+    }
+    if (!(t == t)) t = 0.0f;
+    if (P.spread == 1) {
+        t = t - std::floor(t);
+    } else if (P.spread == 2) {
+        const float u = t - 2.0f * std::floor(t * 0.5f);
+        t = u > 1.0f ? 2.0f - u : u;
+    } else {
+        t = gmin<float>(gmax<float>(t, 0.0f), 1.0f);
+    }
+    const int n = P.n;
+    if (n <= 0) return 0u;
+    float ch[4];
+    if (!(t > P.off[0])) {
+        for (int q = 0; q < 4; ++q) ch[q] = P.rgba[0][q];
+    } else if (!(t < P.off[n - 1])) {
+        for (int q = 0; q < 4; ++q) ch[q] = P.rgba[n - 1][q];
+    } else {
+        int k = 0;
+        while (k + 2 < n && !(t < P.off[k + 1])) ++k;
+        const float f = (t - P.off[k]) / (P.off[k + 1] - P.off[k]);
+        for (int q = 0; q < 4; ++q) ch[q] = lerp(P.rgba[k][q], P.rgba[k + 1][q], f);
+    }
+    ch[3] = ch[3] * P.opacity;
+    uint32_t col = 0;
+    for (int q = 0; q < 4; ++q) {
+        float v = ch[q] * 255.0f;
+        if (!(v > 0.0f)) v = 0.0f;
+        if (v > 255.0f) v = 255.0f;
+        col |= (uint32_t)v << (8 * q);
+    }
+    return (col >> 24) ? col : 0u;
+}
+
+// The paint a fill names: alpha byte 0 and index + 1 in the colour bytes.
+static inline int32_t fill_paint(uint32_t info) {
+    return (info >> 24) == 0u && (info & 0x00FFFFFFu) != 0u ? (int32_t)(info & 0x00FFFFFFu) - 1 : -1;
+}
+
 template <class R> struct Frame {
     using I = typename FT<R>::I;
     // inputs
@@ -757,7 +870,8 @@ template <class R> struct Frame {
         });
     }
 
-    void resolve_pass() { resolve(draw.data(), O, W, H, F, mode, threads, image); }
+    std::vector<OPaint> paints;
+    void resolve_pass() { resolve(draw.data(), O, W, H, F, mode, threads, image, &paints); }
 
     // ---- K10 surface draw (scanlinepr.vert:18-51, scanlinepr.frag:7-14)
     static uint32_t blend(uint32_t dst, uint32_t src) {
@@ -773,7 +887,7 @@ template <class R> struct Frame {
     }
 
     static void resolve(const int32_t* d, int64_t O, int32_t W, int32_t H, int32_t F, int mode, int threads,
-                        std::vector<uint32_t>& img) {
+                        std::vector<uint32_t>& img, const std::vector<OPaint>* paints = nullptr) {
         img.assign((size_t)W * H, 0xFFFFFFFFu);  // clear to white (scanline_rasterizer.cpp:622)
         // bin record indices by row, keeping draw order
         std::vector<int64_t> cnt((size_t)H + 1, 0);
@@ -804,6 +918,21 @@ template <class R> struct Frame {
                     int32_t w = d[4 * k + 1];
                     uint32_t c = (uint32_t)d[4 * k + 2];
                     int32_t xa = imax(x, 0), xb = imin(wadd(x, w), W);
+                    const int32_t pi = fill_paint(c);
+                    if (pi >= 0) {
+                        // a gradient at each pixel's centre (reference mode:
+                        // the centre row of the 2-pixel cell); a paint the
+                        // table lacks paints nothing
+                        if (!paints || pi >= (int32_t)paints->size()) continue;
+                        const OPaint& P = (*paints)[(size_t)pi];
+                        const float yc = mode == SR_MODE_PIXEL ? (float)y + 0.5f : (float)(d[4 * k] >> 16) + 1.0f;
+                        for (int32_t xx = xa; xx < xb; ++xx) {
+                            const uint32_t gc = paint_color(P, (float)xx + 0.5f, yc);
+                            if (mode == SR_MODE_PIXEL) row[xx] = blend(row[xx], gc);
+                            else row[xx] = gc;
+                        }
+                        continue;
+                    }
                     if (mode == SR_MODE_PIXEL) {
                         for (int32_t xx = xa; xx < xb; ++xx) row[xx] = blend(row[xx], c);
                     } else {
@@ -856,12 +985,13 @@ struct or_scene {
 extern "C" {
 
 // mode: SR_MODE_*; fp64: run the double-precision restatement instead.
-int or_render(const sr_scene_view* scene, uint32_t w, uint32_t h, const float* mvp, int mode, int threads,
-              int fp64, or_frame** out) {
+int or_render_paints(const sr_scene_view* scene, uint32_t w, uint32_t h, const float* mvp, int mode, int threads,
+                     int fp64, const sr_paint* paints, uint32_t n_paints, or_frame** out) {
     if (!scene || !mvp || !out || w == 0 || h == 0 || w > 32000 || h > 32000) return 1;
     or_frame* fr = new or_frame();
     fr->is_double = fp64 != 0;
     auto setup = [&](auto& F) {
+        for (uint32_t i = 0; i < n_paints; ++i) F.paints.push_back(orc::make_paint(paints[i], mvp));
         F.s = scene;
         F.W = (int32_t)w;
         F.H = (int32_t)h;
@@ -875,6 +1005,11 @@ int or_render(const sr_scene_view* scene, uint32_t w, uint32_t h, const float* m
     int err = fr->is_double ? setup(fr->d) : setup(fr->f);
     *out = fr;
     return err ? 2 : 0;
+}
+
+int or_render(const sr_scene_view* scene, uint32_t w, uint32_t h, const float* mvp, int mode, int threads,
+              int fp64, or_frame** out) {
+    return or_render_paints(scene, w, h, mvp, mode, threads, fp64, nullptr, 0, out);
 }
 
 int or_get(const or_frame* fr, int stage, const void** ptr, size_t* bytes) {

@@ -29,4 +29,6 @@ def load(sr, name, tmpdir, full=False):
     sc, vp = sr.load_rvg(rvg_file(name, tmpdir), full=full)
     a = sc.arrays()
     d = dict(width=int(vp[2]), height=int(vp[3]), **a)
+    if sc.paints:
+        d["paints"] = sc.paints
     return d, vp

@@ -4,6 +4,7 @@ Each builder returns a flattened scene (numpy SoA, the reference's loadVG
 layout) as a dict accepted by both oracle.Scene and
 vkscanlinepr_gb300.VGContainer.from_arrays.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -54,14 +55,19 @@ class Builder:
 def to_oracle(d):
     import oracle
     return oracle.Scene(d["width"], d["height"], d["position"], d["pos_path_idx"], d["curve_pos_map"],
-                        d["curve_type"], d["curve_path_idx"], d["fill_rule"], d["fill_info"])
+                        d["curve_type"], d["curve_path_idx"], d["fill_rule"], d["fill_info"], paints=d.get("paints"))
 
 
 def to_container(d):
     import vkscanlinepr_gb300 as sr
-    return sr.VGContainer.from_arrays(d["width"], d["height"], d["position"], d["pos_path_idx"],
-                                      d["curve_pos_map"], d["curve_type"], d["curve_path_idx"],
-                                      d["fill_rule"], d["fill_info"])
+    c = sr.VGContainer.from_arrays(d["width"], d["height"], d["position"], d["pos_path_idx"],
+                                   d["curve_pos_map"], d["curve_type"], d["curve_path_idx"],
+                                   d["fill_rule"], d["fill_info"])
+    p = d.get("paints")
+    if p:
+        c.paints = (sr.Paint * len(p))()
+        ctypes.memmove(c.paints, p, ctypes.sizeof(sr.Paint) * len(p))
+    return c
 
 
 RED = (255, 0, 0, 255)
@@ -267,8 +273,52 @@ def arcs(w=96, h=80):
     return b.arrays()
 
 
+def gradients(w=120, h=60):
+    """A full-canvas linear gradient, opaque black to opaque white from
+    x = 0 to x = w (pad), under a radial gradient disc (centre (80, 30),
+    radius 20, focus at the centre, red to transparent, reflect spread) and a
+    linear gradient square rotated by its transform (repeat spread)."""
+    import oracle
+    b = Builder(w, h)
+    paints = (oracle.Paint * 3)()
+    lin = paints[0]
+    lin.kind, lin.spread, lin.opacity, lin.n_stops = 1, 0, 1.0, 2
+    lin.p0[:] = [0.0, 0.0]
+    lin.p1[:] = [float(w), 0.0]
+    lin.xf[:] = [1, 0, 0, 0, 1, 0]
+    lin.offset[0], lin.offset[1] = 0.0, 1.0
+    lin.rgba[0][:] = [0, 0, 0, 1]
+    lin.rgba[1][:] = [1, 1, 1, 1]
+    rad = paints[1]
+    rad.kind, rad.spread, rad.opacity, rad.n_stops = 2, 2, 0.9, 3
+    rad.p0[:] = [80.0, 30.0]
+    rad.p1[:] = [80.0, 30.0]
+    rad.radius = 20.0
+    rad.xf[:] = [1, 0, 0, 0, 1, 0]
+    rad.offset[0], rad.offset[1], rad.offset[2] = 0.0, 0.5, 1.0
+    rad.rgba[0][:] = [1, 0, 0, 1]
+    rad.rgba[1][:] = [1, 0.5, 0, 0.6]
+    rad.rgba[2][:] = [1, 1, 0, 0]
+    rot = paints[2]
+    rot.kind, rot.spread, rot.opacity, rot.n_stops = 1, 1, 1.0, 2
+    rot.p0[:] = [0.0, 0.0]
+    rot.p1[:] = [8.0, 0.0]
+    rot.xf[:] = [0.6, -0.8, 20.0, 0.8, 0.6, 10.0]
+    rot.offset[0], rot.offset[1] = 0.0, 1.0
+    rot.rgba[0][:] = [0, 0, 1, 1]
+    rot.rgba[1][:] = [0, 1, 0, 1]
+    b.path(0, (0, 0, 0, 255)).polygon([(0, 0), (w, 0), (w, h), (0, h)])
+    b.path(0, (0, 0, 0, 255)).polygon([(60, 10), (100, 10), (100, 50), (60, 50)])
+    b.path(1, (0, 0, 0, 255)).polygon([(10, 10), (40, 10), (40, 40), (10, 40)])
+    d = b.arrays()
+    d["fill_info"][:] = [1, 2, 3]   # SR_FILL_PAINT(0), (1), (2)
+    d["paints"] = paints
+    return d
+
+
 ALL = {
     "arcs": arcs,
+    "gradients": gradients,
     "square": square,
     "star_nonzero": lambda: star(rule=0),
     "star_evenodd": lambda: star(rule=1),

@@ -1,5 +1,6 @@
 """Golden fixtures (tests/golden/): the oracle must reproduce them on the CPU,
 and the CUDA renderer must reproduce them on the GPU."""
+import ctypes
 import hashlib
 import json
 import os
@@ -60,8 +61,12 @@ def test_gpu_matches_golden(gpu, grp, name, mode):
     sc = _scene(name)
     r = gpu.ScanlineVGRasterizer(mode=mode, keep_stages=True)
     r.initialize(None, sc.width, sc.height)
-    r.loadVG(gpu.VGContainer.from_arrays(sc.width, sc.height, sc.position, sc.pos_path_idx, sc.curve_pos_map,
-                                         sc.curve_type, sc.curve_path_idx, sc.fill_rule, sc.fill_info))
+    c = gpu.VGContainer.from_arrays(sc.width, sc.height, sc.position, sc.pos_path_idx, sc.curve_pos_map,
+                                    sc.curve_type, sc.curve_path_idx, sc.fill_rule, sc.fill_info)
+    if sc.paints:
+        c.paints = (gpu.Paint * len(sc.paints))()
+        ctypes.memmove(c.paints, sc.paints, ctypes.sizeof(gpu.Paint) * len(sc.paints))
+    r.loadVG(c)
     img = r.render()
     for s in STAGES:
         got = img if s == "image" else r.dump(s)

@@ -23,11 +23,12 @@ def test_reference_scene_stages(gpu, oracle_lib, tmp_path, name, mode):
 
 
 @pytest.mark.parametrize("mode", [0, 1])
-@pytest.mark.parametrize("name", ["car", "chord", "chord-black", "embrace"])
+@pytest.mark.parametrize("name", ["car", "chord", "chord-black", "drops", "embrace"])
 def test_full_reader_scene_stages(gpu, oracle_lib, tmp_path, name, mode):
-    """The same scenes read in full (arcs as rational quadratics): every stage
-    bit-exact against the oracle, including the arcs' transformed slots,
-    monotonic cuts and bisected crossings."""
+    """The same scenes read in full (arcs as rational quadratics, linear and
+    radial gradient paints): every stage bit-exact against the oracle,
+    including the arcs' transformed slots, monotonic cuts and bisected
+    crossings, and every gradient pixel of the image."""
     d, _ = rvg_scenes.load(gpu, name, tmp_path, full=True)
     of, r, img = render_both(gpu, oracle_lib, d, mode)
     compare_all(of, r, img, mode, stages=STAGES_COMMON)

@@ -121,3 +121,26 @@ def test_arcs_known_answers(oracle_lib):
     assert not np.all(img[16, 75] == 255) and np.all(img[14, 75] == 255)
     f0 = oracle_lib.Frame(scenes.to_oracle(d), mode=oracle_lib.MODE_REFERENCE)
     assert f0.n_intersections > 0 and f0.n_draw > 0
+
+
+def test_gradient_known_answers(oracle_lib):
+    """A linear gradient over the canvas: pixel x has t = (x + 0.5) / W and
+    each channel trunc(t * 255); the radial disc is red at its centre; paths
+    past the paint table paint nothing."""
+    d = scenes.gradients()
+    img = oracle_lib.Frame(scenes.to_oracle(d), mode=oracle_lib.MODE_PIXEL).get("image")
+    W = d["width"]
+    for x in (0, 7, 55, 119):
+        v = int(np.float32(np.float32(x + 0.5) * np.float32(1.0 / W)) * np.float32(255.0))
+        assert abs(int(img[2, x, 0]) - v) <= 1 and img[2, x, 1] == img[2, x, 0]
+    # the radial disc's centre: red at alpha 0.9 over the linear gray
+    cx = img[30, 80]
+    assert cx[0] > 200 and cx[1] < 60
+    # reference mode samples the cell's centre row and overwrites
+    f0 = oracle_lib.Frame(scenes.to_oracle(d), mode=oracle_lib.MODE_REFERENCE)
+    assert f0.n_draw > 0
+    # without the paint table every gradient fill paints nothing: white
+    bare = dict(d)
+    bare.pop("paints")
+    img2 = oracle_lib.Frame(scenes.to_oracle(bare), mode=oracle_lib.MODE_PIXEL).get("image")
+    assert np.all(img2 == 255)

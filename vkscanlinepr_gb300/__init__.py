@@ -45,6 +45,25 @@ class SRError(RuntimeError):
         self.code = code
 
 
+PAINT_MAX_STOPS = 16
+PAINT_LINEAR, PAINT_RADIAL = 1, 2
+SPREAD_PAD, SPREAD_REPEAT, SPREAD_REFLECT = 0, 1, 2
+
+
+class Paint(ctypes.Structure):
+    """sr_paint: a linear or radial gradient (see include/sr.h)."""
+    _fields_ = [("kind", ctypes.c_int32), ("spread", ctypes.c_int32), ("p0", ctypes.c_float * 2),
+                ("p1", ctypes.c_float * 2), ("radius", ctypes.c_float), ("xf", ctypes.c_float * 6),
+                ("opacity", ctypes.c_float), ("n_stops", ctypes.c_uint32),
+                ("offset", ctypes.c_float * PAINT_MAX_STOPS),
+                ("rgba", (ctypes.c_float * 4) * PAINT_MAX_STOPS)]
+
+
+def fill_paint(i):
+    """fill_info of a path painted by gradient paint i."""
+    return int(i) + 1
+
+
 class SceneView(ctypes.Structure):
     _fields_ = [
         ("n_points", ctypes.c_uint32), ("n_curves", ctypes.c_uint32),
@@ -161,7 +180,8 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_server_create", "sr_server_submit", "sr_server_wait", "sr_server_get_stats", "sr_server_destroy",
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
            "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
-           "sr_debug_scan_without_first_tile", "sr_write_image", "sr_rvg_load_full"]
+           "sr_debug_scan_without_first_tile", "sr_write_image", "sr_rvg_load_full", "sr_set_paints",
+           "sr_scene_buf_paints"]
 
 _lib = None
 
@@ -193,6 +213,8 @@ def lib():
     L.sr_synth_scene.argtypes = [ctypes.POINTER(SynthParams), ctypes.POINTER(vp)]
     L.sr_rvg_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
     L.sr_rvg_load_full.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
+    L.sr_set_paints.argtypes = [vp, vp, ctypes.c_uint32]
+    L.sr_scene_buf_paints.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint32)]
     L.sr_scene_buf_view.argtypes = [vp, ctypes.POINTER(SceneView)]
     L.sr_scene_buf_free.argtypes = [vp]
     L.sr_scan_status.argtypes = [vp]
@@ -285,6 +307,7 @@ class VGContainer:
         self._curve_pos, self._curve_type, self._curve_path = [], [], []
         self._fill_rule, self._fill_info = [], []
         self._arrays = None
+        self.paints = None   # gradient paints (ctypes array of Paint), or None
 
     # builder API, after VGContainer::newPath/newCurve/addCurve (vg_container.h:49-86)
     def new_path(self, fill_rule=NON_ZERO, rgba=(0, 0, 0, 255)):
@@ -314,6 +337,7 @@ class VGContainer:
     def from_arrays(cls, width, height, position, pos_path_idx, curve_pos_map, curve_type, curve_path_idx,
                     fill_rule, fill_info):
         c = cls(width, height)
+        c.paints = None
         c._arrays = dict(
             position=np.ascontiguousarray(position, np.float32).reshape(-1),
             pos_path_idx=np.ascontiguousarray(pos_path_idx, np.uint32),
@@ -403,7 +427,13 @@ def load_rvg(path, full=False):
     fn = L.sr_rvg_load_full if full else L.sr_rvg_load
     _check(fn(path.encode(), ctypes.byref(h), vp.ctypes.data))
     try:
-        return _from_buf(h), vp
+        c = _from_buf(h)
+        pp, n = ctypes.c_void_p(), ctypes.c_uint32()
+        _check(L.sr_scene_buf_paints(h, ctypes.byref(pp), ctypes.byref(n)))
+        if n.value:
+            c.paints = (Paint * n.value)()
+            ctypes.memmove(c.paints, pp.value, ctypes.sizeof(Paint) * n.value)
+        return c, vp
     finally:
         L.sr_scene_buf_free(h)
 
@@ -492,6 +522,9 @@ class ScanlineVGRasterizer:
         self._scene = container
         v = container.view()
         _check(lib().sr_load_scene(self._ctx, ctypes.byref(v)))
+        paints = getattr(container, "paints", None)
+        _check(lib().sr_set_paints(self._ctx, ctypes.cast(paints, ctypes.c_void_p) if paints else None,
+                                   len(paints) if paints else 0))
 
     def setMVP(self, m):
         a = np.ascontiguousarray(m, np.float32).reshape(16)

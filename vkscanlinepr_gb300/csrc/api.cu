@@ -183,6 +183,52 @@ static sr_status validate_scene(const sr_scene_view* s) {
     return SR_OK;
 }
 
+// A gradient paint for the resolve: the map from pixel centres to gradient
+// space is the inverse of (the matrix's affine part) * xf, computed in
+// double and rounded to float once (the oracle restates this function).
+// A paint whose map cannot be inverted, or without stops, paints nothing.
+static sr::DevPaint make_dev_paint(const sr_paint& p, const float* m) {
+    sr::DevPaint d{};
+    d.kind = p.kind == SR_PAINT_RADIAL ? 2 : 1;
+    d.spread = p.spread == SR_SPREAD_REPEAT ? 1 : p.spread == SR_SPREAD_REFLECT ? 2 : 0;
+    const double A0 = m[0], A1 = m[1], A2 = m[3], A3 = m[4], A4 = m[5], A5 = m[7];
+    const double X0 = p.xf[0], X1 = p.xf[1], X2 = p.xf[2], X3 = p.xf[3], X4 = p.xf[4], X5 = p.xf[5];
+    // gradient -> pixel
+    const double F0 = A0 * X0 + A1 * X3, F1 = A0 * X1 + A1 * X4, F2 = (A0 * X2 + A1 * X5) + A2;
+    const double F3 = A3 * X0 + A4 * X3, F4 = A3 * X1 + A4 * X4, F5 = (A3 * X2 + A4 * X5) + A5;
+    const double det = F0 * F4 - F1 * F3;
+    const uint32_t ns = p.n_stops > (uint32_t)sr::kMaxStops ? (uint32_t)sr::kMaxStops : p.n_stops;
+    if (det == 0.0 || !std::isfinite(det)) return d;   // n_stops 0: transparent
+    // pixel -> gradient
+    const double G0 = F4 / det, G1 = -F1 / det, G3 = -F3 / det, G4 = F0 / det;
+    const double G2 = -(G0 * F2 + G1 * F5), G5 = -(G3 * F2 + G4 * F5);
+    if (d.kind == 1) {
+        const double dx = (double)p.p1[0] - p.p0[0], dy = (double)p.p1[1] - p.p0[1];
+        const double l2 = dx * dx + dy * dy;
+        if (l2 > 0.0) {
+            d.lin[0] = (float)((G0 * dx + G3 * dy) / l2);
+            d.lin[1] = (float)((G1 * dx + G4 * dy) / l2);
+            d.lin[2] = (float)(((G2 - p.p0[0]) * dx + (G5 - p.p0[1]) * dy) / l2);
+        }
+    } else {
+        const double G[6] = {G0, G1, G2, G3, G4, G5};
+        for (int k = 0; k < 6; ++k) d.m[k] = (float)G[k];
+        const double dx = (double)p.p0[0] - p.p1[0], dy = (double)p.p0[1] - p.p1[1];
+        d.fx = p.p1[0];
+        d.fy = p.p1[1];
+        d.dx = (float)dx;
+        d.dy = (float)dy;
+        d.A = (float)(dx * dx + dy * dy - (double)p.radius * p.radius);
+    }
+    d.opacity = p.opacity;
+    d.n_stops = (int32_t)ns;
+    for (uint32_t k = 0; k < ns; ++k) {
+        d.off[k] = p.offset[k];
+        for (int q = 0; q < 4; ++q) d.rgba[k][q] = p.rgba[k][q];
+    }
+    return d;
+}
+
 // Appends one validated scene to a host set.
 static void append_scene(HostScenes& h, uint32_t w, uint32_t hgt, const sr_scene_view* s, const float* mvp) {
     const uint32_t pb = h.n_paths(), vb = h.n_points();
@@ -216,6 +262,10 @@ struct Pipeline {
     uint32_t flags = 0;
     bool loaded = false;
     bool arcs = false;   // the scene set has SR_CURVE_ARC curves
+    // gradient paints (single-scene contexts): as set, and for the resolve
+    std::vector<sr_paint> paints_h;
+    DevBuf paints_d;
+    uint32_t n_paints = 0;
     sr_tuning tune{sizeof(sr_tuning), 12, 8, 8, 0};
     // segmented sort of this frame: merge rounds (-1: radix sort instead) and
     // the largest segment the tables accept without flagging an overflow
@@ -269,7 +319,7 @@ struct Pipeline {
                          &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &row_count, &row_px,
                          &row_scan, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
                          &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide,
-                         &wide_curves, &cta_narrow_d};
+                         &wide_curves, &cta_narrow_d, &paints_d};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : {ev_fork, ev_merged, ev_join})
             if (e) cudaEventDestroy(e);
@@ -787,6 +837,8 @@ struct Pipeline {
         ra.row_px = row_px.as<unsigned long long>();
         ra.cta_narrow = cta_narrow_d.as<uint8_t>();
         ra.any_narrow = any_narrow ? 1 : 0;
+        ra.paints = n_paints ? paints_d.as<DevPaint>() : nullptr;
+        ra.n_paints = n_paints;
         mark(ST_RESOLVE, false);
         launch_resolve(ra, res_ctas, st);
         mark(ST_RESOLVE, true);
@@ -1008,15 +1060,42 @@ sr_status sr_load_scene(sr_ctx* c, const sr_scene_view* s) {
     return c->p.upload_single(s, c->W, c->H, c->mvp);
 }
 
+// The context's paints for its current matrix, on the device.
+static sr_status upload_paints(sr_ctx* c) {
+    Pipeline& p = c->p;
+    p.n_paints = (uint32_t)p.paints_h.size();
+    if (!p.n_paints) return SR_OK;
+    std::vector<sr::DevPaint> d(p.n_paints);
+    for (uint32_t i = 0; i < p.n_paints; ++i) d[i] = make_dev_paint(p.paints_h[i], c->mvp);
+    CUDA_TRY(cudaSetDevice(p.device));
+    CUDA_TRY(ensure(p.paints_d, sizeof(sr::DevPaint) * d.size()));
+    CUDA_TRY(cudaMemcpy(p.paints_d.p, d.data(), sizeof(sr::DevPaint) * d.size(), cudaMemcpyHostToDevice));
+    return SR_OK;
+}
+
 sr_status sr_set_mvp(sr_ctx* c, const float m[16]) {
     if (!c || !m) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     std::memcpy(c->mvp, m, sizeof(float) * 16);
+    SR_TRY(upload_paints(c));
     if (c->p.loaded) {
         std::memcpy(c->p.info[0].mvp, m, sizeof(float) * 16);
         CUDA_TRY(cudaSetDevice(c->p.device));
         return c->p.upload_table();
     }
     return SR_OK;
+}
+
+sr_status sr_set_paints(sr_ctx* c, const sr_paint* paints, uint32_t n) {
+    if (!c || (n && !paints)) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (n > (1u << 24) - 1u) return fail(SR_ERR_INVALID_ARG, "too many paints");
+    for (uint32_t i = 0; i < n; ++i) {
+        const sr_paint& q = paints[i];
+        if ((q.kind != SR_PAINT_LINEAR && q.kind != SR_PAINT_RADIAL) || q.spread < 0 || q.spread > 2 ||
+            q.n_stops == 0 || q.n_stops > SR_PAINT_MAX_STOPS)
+            return fail(SR_ERR_INVALID_ARG, "paint %u: bad kind, spread or stop count", i);
+    }
+    c->p.paints_h.assign(paints, paints + n);
+    return upload_paints(c);
 }
 
 // ScanlineVGRasterizer::render (scanline_rasterizer.cpp:282-696) waits on
@@ -1120,6 +1199,8 @@ sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void
     ra.row_px = nullptr;
     ra.cta_narrow = p.cta_narrow_d.as<uint8_t>();
     ra.any_narrow = p.any_narrow ? 1 : 0;
+    ra.paints = p.n_paints ? p.paints_d.as<sr::DevPaint>() : nullptr;
+    ra.n_paints = p.n_paints;
     sr::launch_resolve(ra, p.res_ctas, st);
     CUDA_TRY(cudaGetLastError());
     p.last_O = n;

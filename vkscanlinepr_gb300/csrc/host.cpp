@@ -13,6 +13,7 @@
 
 struct sr_scene_buf {
     srsynth::Scene s;
+    std::vector<sr_paint> paints;   // gradient paints (full RVG reader)
 };
 
 namespace {
@@ -56,6 +57,13 @@ extern "C" sr_status sr_scene_buf_view(const sr_scene_buf* b, sr_scene_view* v) 
 
 extern "C" void sr_scene_buf_free(sr_scene_buf* b) { delete b; }
 
+extern "C" sr_status sr_scene_buf_paints(const sr_scene_buf* b, const sr_paint** paints, uint32_t* n) {
+    if (!b || !paints || !n) return SR_ERR_INVALID_ARG;
+    *paints = b->paints.empty() ? nullptr : b->paints.data();
+    *n = (uint32_t)b->paints.size();
+    return SR_OK;
+}
+
 extern "C" sr_status sr_scene_buf_size(const sr_scene_buf* b, uint32_t* wh) {
     if (!b || !wh) return SR_ERR_INVALID_ARG;
     wh[0] = b->s.width;
@@ -96,7 +104,29 @@ struct PathRec {
     float color[4] = {0.f, 0.f, 0.f, 1.f};
     float opacity = 0.f;
     bool gradient = false;   // a gradient paint (full reader)
+    sr_paint paint{};
 };
+
+// The numbers of a token, brackets, parentheses, commas and colons taken as
+// blanks: "(1,2)" -> 1 2, "dyn_affine([1,0,2],[0,1,3])" -> 1 0 2 0 1 3.
+std::vector<float> token_numbers(const std::string& t) {
+    std::string s = t;
+    for (char& ch : s)
+        if (ch == '(' || ch == ')' || ch == '[' || ch == ']' || ch == ',' || ch == ':') ch = ' ';
+    std::vector<float> v;
+    const char* p = s.c_str();
+    while (*p) {
+        char* end = nullptr;
+        const float x = std::strtof(p, &end);
+        if (end == p) {
+            ++p;
+            continue;
+        }
+        v.push_back(x);
+        p = end;
+    }
+    return v;
+}
 
 }  // namespace
 
@@ -254,11 +284,44 @@ static sr_status rvg_parse(const char* path, bool full, sr_scene_buf** out, floa
         }
         tk.next(t);
         if (full && (t == "linear" || t == "radial")) {
-            // "gradient", the geometry, "dyn_ramp", the stops, the spread,
-            // then "dyn_affine(...)", which ends the paint
+            // linear gradient (x0,y0) (x1,y1) | radial gradient (cx,cy) (fx,fy) r,
+            // then dyn_ramp, stops "offset:rgba(r,g,b,a)", the spread (pad,
+            // repeat or reflect) and dyn_affine([a,b,c],[d,e,f]), which ends it
             pr.gradient = true;
-            while (tk.next(t) && t.compare(0, 10, "dyn_affine") != 0) {
+            sr_paint& g = pr.paint;
+            g.kind = t == "radial" ? SR_PAINT_RADIAL : SR_PAINT_LINEAR;
+            g.opacity = pr.opacity;
+            g.xf[0] = 1.f;
+            g.xf[4] = 1.f;
+            tk.next(t);   // gradient
+            std::string a, b;
+            tk.next(a);
+            tk.next(b);
+            std::vector<float> pa = token_numbers(a), pb = token_numbers(b);
+            if (pa.size() >= 2) { g.p0[0] = pa[0]; g.p0[1] = pa[1]; }
+            if (pb.size() >= 2) { g.p1[0] = pb[0]; g.p1[1] = pb[1]; }
+            if (g.kind == SR_PAINT_RADIAL) {
+                tk.next(a);
+                g.radius = std::strtof(a.c_str(), nullptr);
             }
+            while (tk.next(t) && t.compare(0, 10, "dyn_affine") != 0) {
+                if (t == "pad") g.spread = SR_SPREAD_PAD;
+                else if (t == "repeat") g.spread = SR_SPREAD_REPEAT;
+                else if (t == "reflect") g.spread = SR_SPREAD_REFLECT;
+                else if (t.find(':') != std::string::npos && g.n_stops < SR_PAINT_MAX_STOPS) {
+                    std::vector<float> v = token_numbers(t);
+                    const bool rgb = t.find("rgba") == std::string::npos;
+                    if (v.size() >= (rgb ? 4u : 5u)) {
+                        g.offset[g.n_stops] = v[0];
+                        for (int q = 0; q < 3; ++q) g.rgba[g.n_stops][q] = v[1 + q];
+                        g.rgba[g.n_stops][3] = rgb ? 1.f : v[4];
+                        ++g.n_stops;
+                    }
+                }
+            }
+            std::vector<float> xf = token_numbers(t);
+            if (xf.size() >= 6)
+                for (int q = 0; q < 6; ++q) g.xf[q] = xf[q];
         } else if (t == "solid") {
             tk.next(t);
             std::string inner;
@@ -300,7 +363,10 @@ static sr_status rvg_parse(const char* path, bool full, sr_scene_buf** out, floa
         }
         uint32_t c = (uint32_t)b8[0] | ((uint32_t)b8[1] << 8) | ((uint32_t)b8[2] << 16) | ((uint32_t)b8[3] << 24);
         if (!(c & 0xFF000000u)) c = 0;
-        if (pr.gradient) c = 0;
+        if (pr.gradient) {
+            c = pr.paint.n_stops ? SR_FILL_PAINT(bobj->paints.size()) : 0u;
+            if (pr.paint.n_stops) bobj->paints.push_back(pr.paint);
+        }
         s.fill_rule.push_back(pr.rule);
         s.fill_info.push_back(c);
         for (uint32_t ci = cb; ci < ce; ++ci) {

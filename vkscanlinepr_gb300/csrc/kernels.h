@@ -226,6 +226,27 @@ void launch_winding_emit(const WindArgs& a, int items, uint64_t* tile_status, ui
                          uint32_t* status, cudaStream_t st);
 
 // ---- resolve.cu
+// A gradient paint ready for the resolve (built on the host from an
+// sr_paint and the scene's matrix, see sr.h for the definition): linear
+// t = (lin0 X + lin1 Y) + lin2 of the pixel-space point (X, Y); radial
+// g = (m0 X + m1 Y) + m2, (m3 X + m4 Y) + m5 in gradient space, focus
+// (fx, fy), centre - focus (dx, dy), A = dx^2 + dy^2 - r^2.
+constexpr int kMaxStops = 16;
+struct DevPaint {
+    int32_t kind, spread, n_stops, pad;
+    float lin[3];
+    float m[6];
+    float fx, fy, dx, dy, A;
+    float opacity;
+    float off[kMaxStops];
+    float rgba[kMaxStops][4];
+};
+// The paint a fill_info names: alpha byte 0 and index + 1 in the colour
+// bytes; -1 for a solid colour.
+__host__ __device__ __forceinline__ int32_t fill_paint(uint32_t info) {
+    return (info >> 24) == 0u && (info & 0x00FFFFFFu) != 0u ? (int32_t)(info & 0x00FFFFFFu) - 1 : -1;
+}
+
 // Resolve work: each CTA paints rows_per_cta cell rows of one scene;
 // cta_base[s] is the first CTA of scene s (host-built, n_scenes+1 entries).
 struct ResolveArgs {
@@ -244,6 +265,8 @@ struct ResolveArgs {
     uint32_t cut_segs;
     const uint8_t* cta_narrow;        // [CTAs] 1 for a CTA of several rows
     int any_narrow;                   // some CTA is (then pixel mode runs a second kernel for them)
+    const DevPaint* paints;           // gradient paints of the scene (single-scene contexts), or NULL
+    uint32_t n_paints;
 };
 // Pixels per warp of a resolve CTA.
 constexpr int kResolveSeg = 256;

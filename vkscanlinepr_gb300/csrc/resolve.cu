@@ -123,13 +123,99 @@ template <int WARPS> SR_DEV int32_t resolve_seg(const ResolveWork& w, int group)
     return w.segs >= kResolveWarps ? group * kResolveWarps + warp : warp % w.segs;
 }
 
-SR_DEV PixRec pix_rec(const int4 d, uint32_t di) {
+// Colour of gradient paint P at the pixel-space point (x, y), packed RGBA8,
+// 0 when transparent (the definition is in sr.h; the oracle restates it).
+__device__ __noinline__ uint32_t paint_color(const DevPaint& P, float x, float y) {
+    float t;
+    if (P.kind == 1) {
+        t = __fadd_rn(__fadd_rn(__fmul_rn(P.lin[0], x), __fmul_rn(P.lin[1], y)), P.lin[2]);
+    } else {
+        const float gx = __fadd_rn(__fadd_rn(__fmul_rn(P.m[0], x), __fmul_rn(P.m[1], y)), P.m[2]);
+        const float gy = __fadd_rn(__fadd_rn(__fmul_rn(P.m[3], x), __fmul_rn(P.m[4], y)), P.m[5]);
+        const float ex = __fsub_rn(gx, P.fx), ey = __fsub_rn(gy, P.fy);
+        const float b = __fadd_rn(__fmul_rn(ex, P.dx), __fmul_rn(ey, P.dy));
+        const float c = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+        if (P.A == 0.0f) {
+            t = b != 0.0f ? __fdiv_rn(c, __fmul_rn(2.0f, b)) : 0.0f;
+        } else {
+            const float disc = __fsub_rn(__fmul_rn(b, b), __fmul_rn(P.A, c));
+            if (disc < 0.0f) {
+                t = 0.0f;
+            } else {
+                const float sq = __fsqrt_rn(disc);
+                t = __fdiv_rn(P.A < 0.0f ? __fsub_rn(b, sq) : __fadd_rn(b, sq), P.A);
+            }
+        }
+    }
+    if (!(t == t)) t = 0.0f;
+    if (P.spread == 1) {
+        t = __fsub_rn(t, floorf(t));
+    } else if (P.spread == 2) {
+        const float u = __fsub_rn(t, __fmul_rn(2.0f, floorf(__fmul_rn(t, 0.5f))));
+        t = u > 1.0f ? __fsub_rn(2.0f, u) : u;
+    } else {
+        t = gmin(gmax(t, 0.0f), 1.0f);
+    }
+    const int n = P.n_stops;
+    if (n <= 0) return 0u;
+    float ch[4];
+    if (!(t > P.off[0])) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ch[q] = P.rgba[0][q];
+    } else if (!(t < P.off[n - 1])) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ch[q] = P.rgba[n - 1][q];
+    } else {
+        int k = 0;
+        while (k + 2 < n && !(t < P.off[k + 1])) ++k;
+        const float f = __fdiv_rn(__fsub_rn(t, P.off[k]), __fsub_rn(P.off[k + 1], P.off[k]));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ch[q] = lerp_rn(P.rgba[k][q], P.rgba[k + 1][q], f);
+    }
+    ch[3] = __fmul_rn(ch[3], P.opacity);
+    uint32_t col = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        float v = __fmul_rn(ch[q], 255.0f);
+        if (!(v > 0.0f)) v = 0.0f;
+        if (v > 255.0f) v = 255.0f;
+        col |= (uint32_t)v << (8 * q);
+    }
+    return (col >> 24) ? col : 0u;
+}
+
+// A gradient record's PixRec carries iau = kGradient and its paint in sab.
+constexpr uint32_t kGradient = 0xFFFFFFFFu;
+
+SR_DEV PixRec solid_rec(uint32_t col) {
+    PixRec pr;
+    const uint32_t al = col >> 24;
+    pr.ia = (float)(255u - al);
+    pr.sg = (float)(((col >> 8) & 0xFFu) * al);
+    pr.iau = 255u - al;
+    pr.sab = ((col & 0xFFu) * al + 128u) | ((((col >> 16) & 0xFFu) * al + 128u) << 16);
+    return pr;
+}
+
+// GRAD: the kernel paints gradients.  Without it a gradient record is a
+// solid of alpha 0, which leaves every pixel as it was; the kernels without
+// gradients run for scenes without paints and keep their registers.
+template <bool GRAD> SR_DEV PixRec pix_rec(const int4 d, uint32_t di) {
     PixRec pr;
     pr.idx1 = di + 1u;
     const int32_t x = d.x & 0xFFFF;
     pr.x0 = x;
     pr.x1 = wadd(x, d.y);
     const uint32_t col = (uint32_t)d.z, al = col >> 24;
+    const int32_t paint = GRAD ? fill_paint(col) : -1;
+    if (paint >= 0) {
+        pr.iau = kGradient;
+        pr.sab = (uint32_t)paint;
+        pr.ia = 0.0f;
+        pr.sg = 0.0f;
+        pr.row = 0;
+        return pr;
+    }
     pr.ia = (float)(255u - al);
     pr.sg = (float)(((col >> 8) & 0xFFu) * al);
     pr.iau = 255u - al;
@@ -138,11 +224,32 @@ SR_DEV PixRec pix_rec(const int4 d, uint32_t di) {
     return pr;
 }
 
+// A gradient record: each lane blends its covered pixels with the paint's
+// colour at their centres (row centre yc); a paint the table lacks paints
+// nothing.
+SR_DEV void apply_gradient(const ResolveArgs& a, const PixRec& pr, int32_t seg, int lane, float yc,
+                           uint32_t (&rb)[kK], float (&g)[kK]) {
+    if (!a.paints || pr.sab >= a.n_paints) return;
+    const DevPaint& P = a.paints[pr.sab];
+#pragma unroll
+    for (int j = 0; j < kK; ++j) {
+        const int32_t p = seg + lane + 32 * j;
+        if (p >= pr.x0 && p < pr.x1) {
+            const uint32_t col = paint_color(P, __fadd_rn((float)p, 0.5f), yc);
+            if (col) blend3(rb[j], g[j], solid_rec(col));
+        }
+    }
+}
+
 // A record on this warp's segment: a one-pixel record is a uniform branch on
 // its register slot; a record over the whole segment blends every slot;
 // otherwise each lane tests its pixels.
-SR_DEV void apply_pix(const PixRec& pr, int32_t seg, int lane, uint32_t (&rb)[kK], float (&g)[kK]) {
-    if (pr.x1 - pr.x0 == 1) {
+template <bool GRAD>
+SR_DEV void apply_pix(const ResolveArgs& a, const PixRec& pr, int32_t seg, int lane, float yc, uint32_t (&rb)[kK],
+                      float (&g)[kK]) {
+    if (GRAD && pr.iau == kGradient) {
+        apply_gradient(a, pr, seg, lane, yc, rb, g);
+    } else if (pr.x1 - pr.x0 == 1) {
         const int32_t off = pr.x0 - seg;
         const int j = off >> 5;
         if (lane == (off & 31)) {
@@ -280,10 +387,10 @@ struct RunWalk {
     }
 };
 
-SR_DEV void stage_pix(const ResolveArgs& a, PixRec* sq, int32_t c0, int32_t cnt) {
+template <bool GRAD> SR_DEV void stage_pix(const ResolveArgs& a, PixRec* sq, int32_t c0, int32_t cnt) {
     for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
         const uint32_t di = a.row_sorted_idx[c0 + q];
-        sq[q] = pix_rec(a.draw[di], di);
+        sq[q] = pix_rec<GRAD>(a.draw[di], di);
     }
 }
 
@@ -308,6 +415,7 @@ SR_DEV void store_pix(const ResolveArgs& a, const ResolveWork& w, int32_t seg, i
 // A CTA of several short rows (a canvas narrower than WARPS segments): each
 // warp finds its cut and streams its own row's records 32 at a time through
 // its own shared-memory slots, without waiting for the other warps.
+template <bool GRAD>
 SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, int32_t seg, PixRec* slot, RunBuf& buf) {
     const int lane = threadIdx.x & 31;
     const uint32_t r = w.si->row_base + (uint32_t)(w.r0 + w.my_row);
@@ -325,9 +433,10 @@ SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, int32
             PixRec pr;
             if (q >= lim) {
                 const uint32_t di = a.row_sorted_idx[q];
-                pr = pix_rec(a.draw[di], di);
+                pr = pix_rec<GRAD>(a.draw[di], di);
                 ov = pr.x0 < seg + kResolveSeg && pr.x1 > seg;
-                cover = pr.x0 <= seg && pr.x1 >= segend;
+                // a gradient's colour varies over the segment: it ends a run
+                cover = pr.x0 <= seg && pr.x1 >= segend && pr.iau != kGradient;
             }
             found = rw.feed(__ballot_sync(0xFFFFFFFFu, ov), __ballot_sync(0xFFFFFFFFu, cover), pr, q, lane, buf);
         }
@@ -336,12 +445,13 @@ SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, int32
     uint32_t rb[kK];
     float g[kK];
     init_pix(rb, g);
+    const float yc = __fadd_rn((float)(w.r0 + w.my_row), 0.5f);
     for (int32_t c0 = start; c0 < end; c0 += 32) {
         const int32_t q = c0 + lane;
         bool ov = false;
         if (q < end) {
             const uint32_t di = a.row_sorted_idx[q];
-            const PixRec pr = pix_rec(a.draw[di], di);
+            const PixRec pr = pix_rec<GRAD>(a.draw[di], di);
             ov = pr.x0 < seg + kResolveSeg && pr.x1 > seg && pr.idx1 >= cut;
             if (ov) slot[lane] = pr;
         }
@@ -350,7 +460,7 @@ SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, int32
         while (m) {
             const PixRec p = slot[__ffs(m) - 1];
             m &= m - 1;
-            apply_pix(p, seg, lane, rb, g);
+            apply_pix<GRAD>(a, p, seg, lane, yc, rb, g);
         }
         __syncwarp();
     }
@@ -366,17 +476,17 @@ SR_DEV void resolve_pixel_rows(const ResolveArgs& a, const ResolveWork& w, int32
 // records are staged once, every warp finds its segment's cut in them, and the CTA
 // stages from the earliest cut on (chunks end-aligned, so the last one is
 // the chunk already staged); a warp skips the records before its own cut.
-template <int WARPS>
+template <int WARPS, bool GRAD>
 __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel_rows(const ResolveArgs a) {
     __shared__ PixRec slots[WARPS * 32];
     __shared__ RunBuf bufs[WARPS];
     if (!a.cta_narrow[blockIdx.x]) return;
     const ResolveWork w = resolve_work<WARPS>(a);
     const int warp = threadIdx.x >> 5;
-    if (w.active) resolve_pixel_rows(a, w, resolve_seg<WARPS>(w, 0) * kResolveSeg, slots + warp * 32, bufs[warp]);
+    if (w.active) resolve_pixel_rows<GRAD>(a, w, resolve_seg<WARPS>(w, 0) * kResolveSeg, slots + warp * 32, bufs[warp]);
 }
 
-template <int WARPS>
+template <int WARPS, bool GRAD>
 __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs a) {
     if (a.any_narrow && a.cta_narrow[blockIdx.x]) return;   // k_resolve_pixel_rows
     __shared__ PixRec sq[kChunk];
@@ -391,7 +501,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
     const bool search = row_searched(a, r, W);
     bool tail_staged = false;   // sq holds [tail0, end)
     if (search) {
-        stage_pix(a, sq, tail0, end - tail0);
+        stage_pix<GRAD>(a, sq, tail0, end - tail0);
         tail_staged = true;
     }
     for (int group = 0; group < w.groups; ++group) {
@@ -411,7 +521,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
                     if (i >= 0) {
                         const int32_t x0 = sq[i].x0, x1 = sq[i].x1;
                         ov = x0 < seg + kResolveSeg && x1 > seg;
-                        cover = x0 <= seg && x1 >= segend;
+                        cover = x0 <= seg && x1 >= segend && sq[i].iau != kGradient;
                     }
                     found = rw.feed(__ballot_sync(0xFFFFFFFFu, ov), __ballot_sync(0xFFFFFFFFu, cover),
                                     sq[i < 0 ? 0 : i], tail0 + i, lane, bufs[warp]);
@@ -426,13 +536,14 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
         uint32_t rb[kK];
         float g[kK];
         init_pix(rb, g);
+        const float yc = __fadd_rn((float)w.r0, 0.5f);
         const int32_t nchunks = (end - s0 + kChunk - 1) / kChunk;
         for (int k = nchunks - 1; k >= 0; --k) {
             const int32_t c0 = imax(s0, end - (k + 1) * kChunk), c1 = end - k * kChunk;
             const int32_t base = k ? c0 : tail0;
             if (k || !tail_staged) {
                 __syncthreads();
-                stage_pix(a, sq, base, c1 - base);
+                stage_pix<GRAD>(a, sq, base, c1 - base);
                 __syncthreads();
                 tail_staged = k == 0;
             }
@@ -446,7 +557,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_pixel(const ResolveArgs 
                 while (m) {
                     const PixRec pr = sq[g0 + __ffs(m) - 1];
                     m &= m - 1;
-                    apply_pix(pr, seg, lane, rb, g);
+                    apply_pix<GRAD>(a, pr, seg, lane, yc, rb, g);
                 }
             }
         }
@@ -464,7 +575,7 @@ struct RefRec {
     uint32_t idx1;   // 1 + draw index
 };
 
-template <int WARPS>
+template <int WARPS, bool GRAD>
 __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a) {
     __shared__ RefRec sq[kChunk];
     const ResolveWork w = resolve_work<WARPS>(a);
@@ -506,10 +617,25 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
                     const int q = g0 + __ffs(m) - 1;
                     m &= m - 1;
                     const RefRec rr = sq[q];
+                    const int32_t paint = GRAD ? fill_paint(rr.col) : -1;
+                    if (paint >= 0) {
+                        // a gradient, sampled on the cell's centre row; a
+                        // paint the table lacks paints nothing
+                        if (a.paints && (uint32_t)paint < a.n_paints) {
+                            const DevPaint& P = a.paints[paint];
+                            const float yc = __fadd_rn((float)((w.r0 + w.my_row) * a.F), 1.0f);
 #pragma unroll
-                    for (int j = 0; j < kK; ++j) {
-                        int32_t p = seg + lane + 32 * j;
-                        if (p >= rr.x0 && p < rr.x1) px[j] = rr.col;
+                            for (int j = 0; j < kK; ++j) {
+                                int32_t p = seg + lane + 32 * j;
+                                if (p >= rr.x0 && p < rr.x1) px[j] = paint_color(P, __fadd_rn((float)p, 0.5f), yc);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < kK; ++j) {
+                            int32_t p = seg + lane + 32 * j;
+                            if (p >= rr.x0 && p < rr.x1) px[j] = rr.col;
+                        }
                     }
                 }
             }
@@ -529,24 +655,26 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
     }
 }
 
+template <int WARPS, bool GRAD> static void launch_resolve_t(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st) {
+    if (a.pixel_mode) {
+        k_resolve_pixel<WARPS, GRAD><<<n_ctas, 32 * WARPS, 0, st>>>(a);
+        if (a.any_narrow) k_resolve_pixel_rows<WARPS, GRAD><<<n_ctas, 32 * WARPS, 0, st>>>(a);
+    } else {
+        k_resolve_ref<WARPS, GRAD><<<n_ctas, 32 * WARPS, 0, st>>>(a);
+    }
+}
+
 void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st) {
     if (n_ctas == 0) return;
     count_launches(1);
     if (a.pixel_mode && a.any_narrow) count_launches(1);
+    const bool grad = a.paints && a.n_paints;
     if (a.warps == 8) {
-        if (a.pixel_mode) {
-            k_resolve_pixel<8><<<n_ctas, 32 * 8, 0, st>>>(a);
-            if (a.any_narrow) k_resolve_pixel_rows<8><<<n_ctas, 32 * 8, 0, st>>>(a);
-        } else {
-            k_resolve_ref<8><<<n_ctas, 32 * 8, 0, st>>>(a);
-        }
+        if (grad) launch_resolve_t<8, true>(a, n_ctas, st);
+        else launch_resolve_t<8, false>(a, n_ctas, st);
     } else {
-        if (a.pixel_mode) {
-            k_resolve_pixel<16><<<n_ctas, 32 * 16, 0, st>>>(a);
-            if (a.any_narrow) k_resolve_pixel_rows<16><<<n_ctas, 32 * 16, 0, st>>>(a);
-        } else {
-            k_resolve_ref<16><<<n_ctas, 32 * 16, 0, st>>>(a);
-        }
+        if (grad) launch_resolve_t<16, true>(a, n_ctas, st);
+        else launch_resolve_t<16, false>(a, n_ctas, st);
     }
 }
 
