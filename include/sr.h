@@ -164,6 +164,19 @@ sr_status sr_load_scene(sr_ctx* ctx, const sr_scene_view* scene);
  * (app/vg_app.cpp:159-160). */
 sr_status sr_set_mvp(sr_ctx* ctx, const float m[16]);
 
+/* Antialiased frame (SR_MODE_PIXEL contexts): `samples` (1, 2, 4, 8 or 16)
+ * samples a pixel on a comb, every sample on a row and a column of its own:
+ * sample i at (x + ((i * s) mod k + 0.5) / k, y + (i + 0.5) / k), s = 5 for
+ * k = 16, 3 for k = 4 or 8, 1 otherwise.  Each sample is the pixel-mode test
+ * at that point (the pixel-centre sample moved there; composited in path
+ * order over white), and the pixel is the rounded average (sum + k/2) / k
+ * of its samples per channel.  The samples' frames are rendered by moving
+ * the scene by (0.5 - dx, 0.5 - dy) after the matrix (rows 0 and 1 take the
+ * translation times row 3), and summed on the device.  This is the
+ * reference's antialiasing TODO, the "comb-like multisampling" of
+ * README.md:5 and gen_fragment.comp:202.  Waits for the frame. */
+sr_status sr_render_aa(sr_ctx* ctx, uint32_t samples, void* rgba_out, int out_is_device, void* stream);
+
 /* Sets the gradient paints the loaded scene's SR_FILL_PAINT(i) fills refer
  * to (copied; they follow later sr_set_mvp calls).  n = 0 clears the table;
  * a fill that names no paint of the table paints nothing. */

@@ -249,6 +249,35 @@ def fp64_flips(scene, mode, mvp=None, threads=0, image=None):
     return int(np.any(np.asarray(image) != ref, axis=2).sum())
 
 
+def aa_offsets(k):
+    """Sample positions within a pixel for k-sample antialiasing: sample i
+    at (((i * s) mod k + 0.5) / k, (i + 0.5) / k), every sample on a row and
+    a column of its own (s = 5 for k = 16, 3 for k = 4 or 8, 1 otherwise).
+    float32, in the order the renderer computes them."""
+    s = 5 if k == 16 else (3 if k >= 4 else 1)
+    f = np.float32
+    return [((f((i * s) % k) + f(0.5)) / f(k), (f(i) + f(0.5)) / f(k)) for i in range(k)]
+
+
+def render_aa(scene, samples, mvp=None, threads=0):
+    """The antialiased image (sr_render_aa): each sample is the pixel-mode
+    frame with the scene moved by (0.5 - dx, 0.5 - dy) after the matrix (rows
+    0 and 1 plus the translation times row 3, in float32), and a pixel is the
+    rounded average (sum + k/2) // k of its samples per channel."""
+    m = IDENTITY if mvp is None else np.ascontiguousarray(mvp, np.float32).reshape(16)
+    acc = None
+    f = np.float32
+    for ox, oy in aa_offsets(samples):
+        tx, ty = f(0.5) - ox, f(0.5) - oy
+        mm = m.copy()
+        for k in range(4):
+            mm[k] = m[k] + tx * m[12 + k]
+            mm[4 + k] = m[4 + k] + ty * m[12 + k]
+        img = Frame(scene, mvp=mm, mode=MODE_PIXEL, threads=threads).get("image").astype(np.uint32)
+        acc = img if acc is None else acc + img
+    return ((acc + samples // 2) // samples).astype(np.uint8)
+
+
 def resolve(draw, width, height, mode, threads=1):
     """Paint an int32x4 draw list with the oracle's resolve step."""
     d = np.ascontiguousarray(draw, np.int32).reshape(-1, 4)

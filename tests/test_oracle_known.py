@@ -144,3 +144,17 @@ def test_gradient_known_answers(oracle_lib):
     bare.pop("paints")
     img2 = oracle_lib.Frame(scenes.to_oracle(bare), mode=oracle_lib.MODE_PIXEL).get("image")
     assert np.all(img2 == 255)
+
+
+def test_multisampled_edge_coverage(oracle_lib):
+    """A black square from x = 2.25 to 6 over white, 16 samples a pixel: the
+    pixel column 2 has 12 of its 16 samples (columns 4..15 of the comb) inside,
+    so its channels are (255 * 4 + 8) // 16 = 64; the columns fully inside
+    are black and those outside white."""
+    d = scenes.square(w=10, h=8, x0=2.25, y0=2, x1=6, y1=6, rgba=(0, 0, 0, 255))
+    img = oracle_lib.render_aa(scenes.to_oracle(d), 16)
+    assert img[4, 2, 0] == (255 * 4 + 8) // 16
+    assert np.all(img[4, 3:6, :3] == 0) and np.all(img[4, 7, :3] == 255)
+    # one sample is the plain pixel-mode frame with the sample at the centre
+    one = oracle_lib.render_aa(scenes.to_oracle(d), 1)
+    assert np.array_equal(one, oracle_lib.Frame(scenes.to_oracle(d), mode=1).get("image"))

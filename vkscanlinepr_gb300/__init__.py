@@ -181,7 +181,7 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
            "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
            "sr_debug_scan_without_first_tile", "sr_write_image", "sr_rvg_load_full", "sr_set_paints",
-           "sr_scene_buf_paints"]
+           "sr_scene_buf_paints", "sr_render_aa"]
 
 _lib = None
 
@@ -214,6 +214,7 @@ def lib():
     L.sr_rvg_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
     L.sr_rvg_load_full.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp), vp]
     L.sr_set_paints.argtypes = [vp, vp, ctypes.c_uint32]
+    L.sr_render_aa.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_int, vp]
     L.sr_scene_buf_paints.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_uint32)]
     L.sr_scene_buf_view.argtypes = [vp, ctypes.POINTER(SceneView)]
     L.sr_scene_buf_free.argtypes = [vp]
@@ -525,6 +526,14 @@ class ScanlineVGRasterizer:
         paints = getattr(container, "paints", None)
         _check(lib().sr_set_paints(self._ctx, ctypes.cast(paints, ctypes.c_void_p) if paints else None,
                                    len(paints) if paints else 0))
+
+    def render_aa(self, samples, out=None, stream=None):
+        """Antialiased frame: `samples` (1, 2, 4, 8, 16) samples a pixel on a
+        comb (sr_render_aa); returns RGBA8 as (h, w, 4) uint8."""
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.uint8)
+        _check(lib().sr_render_aa(self._ctx, int(samples), out.ctypes.data, 0, stream))
+        return out
 
     def setMVP(self, m):
         a = np.ascontiguousarray(m, np.float32).reshape(16)

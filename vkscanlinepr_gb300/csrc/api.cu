@@ -265,6 +265,7 @@ struct Pipeline {
     // gradient paints (single-scene contexts): as set, and for the resolve
     std::vector<sr_paint> paints_h;
     DevBuf paints_d;
+    DevBuf aa_acc;   // multisampling: per-pixel channel sums (ushort4)
     uint32_t n_paints = 0;
     sr_tuning tune{sizeof(sr_tuning), 12, 8, 8, 0};
     // segmented sort of this frame: merge rounds (-1: radix sort instead) and
@@ -319,7 +320,7 @@ struct Pipeline {
                          &rkeys, &rvals, &rkeys_alt, &rvals_alt, &row_sort_scratch, &row_start, &seg_cut, &row_count, &row_px,
                          &row_scan, &image, &d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey, &path_first, &path_draw,
                          &feats, &preds, &allot, &plan_tot, &judge_out, &seg_scratch, &seg_tiles, &curve_wide,
-                         &wide_curves, &cta_narrow_d, &paints_d};
+                         &wide_curves, &cta_narrow_d, &paints_d, &aa_acc};
         for (DevBuf* b : all) release(*b);
         for (cudaEvent_t e : {ev_fork, ev_merged, ev_join})
             if (e) cudaEventDestroy(e);
@@ -1060,13 +1061,13 @@ sr_status sr_load_scene(sr_ctx* c, const sr_scene_view* s) {
     return c->p.upload_single(s, c->W, c->H, c->mvp);
 }
 
-// The context's paints for its current matrix, on the device.
-static sr_status upload_paints(sr_ctx* c) {
+// The context's paints for matrix m (its own unless given), on the device.
+static sr_status upload_paints(sr_ctx* c, const float* m = nullptr) {
     Pipeline& p = c->p;
     p.n_paints = (uint32_t)p.paints_h.size();
     if (!p.n_paints) return SR_OK;
     std::vector<sr::DevPaint> d(p.n_paints);
-    for (uint32_t i = 0; i < p.n_paints; ++i) d[i] = make_dev_paint(p.paints_h[i], c->mvp);
+    for (uint32_t i = 0; i < p.n_paints; ++i) d[i] = make_dev_paint(p.paints_h[i], m ? m : c->mvp);
     CUDA_TRY(cudaSetDevice(p.device));
     CUDA_TRY(ensure(p.paints_d, sizeof(sr::DevPaint) * d.size()));
     CUDA_TRY(cudaMemcpy(p.paints_d.p, d.data(), sizeof(sr::DevPaint) * d.size(), cudaMemcpyHostToDevice));
@@ -1107,9 +1108,7 @@ sr_status sr_set_paints(sr_ctx* c, const sr_paint* paints, uint32_t n) {
 // frame overflowed (a new matrix or scene that needs more), it is rerun with
 // exact sizing, which waits for the count as the reference does; so does the
 // first frame of a scene.
-sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) {
-    if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+static sr_status render_core(sr_ctx* c, void* rgba_out, int out_is_device, cudaStream_t st) {
     Pipeline& p = c->p;
     const size_t bytes = (size_t)c->W * c->H * 4;
     const bool presized = c->hint_valid && p.loaded && c->hint_C == p.C && c->hint_P == p.P;
@@ -1144,6 +1143,70 @@ sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) 
         c->hint_largest = p.last_largest;
     }
     return s;
+}
+
+sr_status sr_render(sr_ctx* c, void* rgba_out, int out_is_device, void* stream) {
+    if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
+    return render_core(c, rgba_out, out_is_device, static_cast<cudaStream_t>(stream));
+}
+
+// Sample i of k in pixel units: row (i + 0.5) / k, column ((i * s) mod k +
+// 0.5) / k with s coprime to k, so that every sample has a row and a column
+// of its own (an n-rooks comb).
+static void aa_offset(uint32_t k, uint32_t i, float* ox, float* oy) {
+    const uint32_t s = k == 16 ? 5u : k >= 4 ? 3u : 1u;
+    *ox = ((float)((i * s) % k) + 0.5f) / (float)k;
+    *oy = ((float)i + 0.5f) / (float)k;
+}
+
+sr_status sr_render_aa(sr_ctx* c, uint32_t samples, void* rgba_out, int out_is_device, void* stream) {
+    if (!c) return fail(SR_ERR_INVALID_ARG, "NULL context");
+    if (samples != 1 && samples != 2 && samples != 4 && samples != 8 && samples != 16)
+        return fail(SR_ERR_INVALID_ARG, "samples must be 1, 2, 4, 8 or 16");
+    Pipeline& p = c->p;
+    if (p.mode != SR_MODE_PIXEL) return fail(SR_ERR_INVALID_ARG, "multisampling needs SR_MODE_PIXEL");
+    if (!p.loaded) return fail(SR_ERR_NO_SCENE, "render before a scene was loaded");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaSetDevice(p.device));
+    const size_t npx = (size_t)c->W * c->H;
+    CUDA_TRY(ensure(p.aa_acc, 8 * std::max<size_t>(npx, 1)));
+    const uint64_t launches0 = sr::launches_so_far();
+    sr_status s = SR_OK;
+    for (uint32_t i = 0; i < samples && s == SR_OK; ++i) {
+        // the pipeline samples each pixel at its centre: moving the scene by
+        // (0.5 - ox, 0.5 - oy) samples it at (x + ox, y + oy).  Rows 0 and 1
+        // of the matrix take that translation times row 3.
+        float ox, oy;
+        aa_offset(samples, i, &ox, &oy);
+        const float tx = 0.5f - ox, ty = 0.5f - oy;
+        float* m = p.info[0].mvp;
+        for (int k = 0; k < 4; ++k) {
+            m[k] = c->mvp[k] + tx * c->mvp[12 + k];
+            m[4 + k] = c->mvp[4 + k] + ty * c->mvp[12 + k];
+            m[8 + k] = c->mvp[8 + k];
+            m[12 + k] = c->mvp[12 + k];
+        }
+        s = p.upload_table();
+        if (s == SR_OK) s = upload_paints(c, m);   // gradients are sampled at the moved centres too
+        if (s == SR_OK) s = render_core(c, nullptr, 0, st);
+        if (s == SR_OK) {
+            sr::launch_aa_accumulate(p.image.as<uint32_t>(), p.aa_acc.p, npx, i == 0, st);
+            CUDA_TRY(cudaGetLastError());
+        }
+    }
+    std::memcpy(p.info[0].mvp, c->mvp, sizeof c->mvp);
+    sr_status s2 = p.upload_table();
+    if (s2 == SR_OK) s2 = upload_paints(c);
+    SR_TRY(s);
+    SR_TRY(s2);
+    sr::launch_aa_resolve(p.aa_acc.p, p.image.as<uint32_t>(), npx, samples, st);
+    CUDA_TRY(cudaGetLastError());
+    if (rgba_out)
+        CUDA_TRY(cudaMemcpyAsync(rgba_out, p.image.p, npx * 4,
+                                 out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    p.stats.kernel_launches = (uint32_t)(sr::launches_so_far() - launches0);
+    return SR_OK;
 }
 
 sr_status sr_render_draw_list(sr_ctx* c, const int32_t* records, int64_t n, void* rgba_out, int out_is_device,

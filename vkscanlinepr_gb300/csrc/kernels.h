@@ -272,6 +272,10 @@ struct ResolveArgs {
 constexpr int kResolveSeg = 256;
 uint32_t resolve_rows_per_cta(int32_t W, int warps);
 void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st);
+// Multisampling: sum a sample frame into acc (first: start the sums), and
+// write the rounded averages of k frames.
+void launch_aa_accumulate(const uint32_t* img, void* acc, size_t n, bool first, cudaStream_t st);
+void launch_aa_resolve(const void* acc, uint32_t* img, size_t n, uint32_t k, cudaStream_t st);
 // n_dev (optional) holds the record count; n is the capacity.
 void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,
                        cudaStream_t st);

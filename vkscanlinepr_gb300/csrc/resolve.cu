@@ -678,6 +678,40 @@ void launch_resolve(const ResolveArgs& a, uint32_t n_ctas, cudaStream_t st) {
     }
 }
 
+// Multisampling: the sample frames summed per channel (ushort4; 16 samples
+// of 255 fit), then the rounded average (sum + k/2) / k per channel.
+__global__ void k_aa_accumulate(const uint32_t* __restrict__ img, ushort4* __restrict__ acc, size_t n, int first) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t c = img[i];
+    ushort4 v = first ? make_ushort4(0, 0, 0, 0) : acc[i];
+    v.x = (unsigned short)(v.x + (c & 0xFFu));
+    v.y = (unsigned short)(v.y + ((c >> 8) & 0xFFu));
+    v.z = (unsigned short)(v.z + ((c >> 16) & 0xFFu));
+    v.w = (unsigned short)(v.w + (c >> 24));
+    acc[i] = v;
+}
+
+__global__ void k_aa_resolve(const ushort4* __restrict__ acc, uint32_t* __restrict__ img, size_t n, uint32_t k) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ushort4 v = acc[i];
+    const uint32_t h = k / 2u;
+    img[i] = ((v.x + h) / k) | (((v.y + h) / k) << 8) | (((v.z + h) / k) << 16) | (((v.w + h) / k) << 24);
+}
+
+void launch_aa_accumulate(const uint32_t* img, void* acc, size_t n, bool first, cudaStream_t st) {
+    if (!n) return;
+    count_launches(1);
+    k_aa_accumulate<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(img, static_cast<ushort4*>(acc), n, first ? 1 : 0);
+}
+
+void launch_aa_resolve(const void* acc, uint32_t* img, size_t n, uint32_t k, cudaStream_t st) {
+    if (!n) return;
+    count_launches(1);
+    k_aa_resolve<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(static_cast<const ushort4*>(acc), img, n, k);
+}
+
 void launch_row_bounds(const uint32_t* srows, int64_t n, const uint32_t* n_dev, int32_t rows, int32_t* row_start,
                        cudaStream_t st) {
     int64_t work = n + 1;
