@@ -56,7 +56,7 @@ LIMITS = {
     "chains": "the dependent bisection steps of the longest crossing chains",
     "wide": "the longest chain's bisection rounds (lane exchange latency), beside the rest of the frame",
     "sort": "shared-memory ranking latency of the tile sort and merge rounds",
-    "winding_emit": "instruction issue and two chained look-backs, DRAM 11%",
+    "winding_emit": "latency of each tile's flag, look-back and emission phases at 4-5 CTAs per SM, DRAM ~14%",
 }
 STAGE_NAMES = ["transform", "count", "offset_scan", "chains", "merge", "fragment", "sort", "winding_emit",
                "row_sort", "resolve", "wide"]
@@ -196,10 +196,10 @@ def stage_bytes(st, n_curves, n_points, W, H):
         # sorted keys in; draw records (16 B) and their cell rows (4 B) out
         "winding_emit": N * 8 + O * (16 + 4),
         "row_sort": O * 4 + row_passes * O * 2 * (4 + 4),
-        # the image written and the row starts; a segment also reads the draw
-        # records after its collapse cut (about 6% of them in the 4096^2
-        # frame), which depend on the scene and are left out
-        "resolve": W * H * 4 + (H + 1) * 4,
+        # a latency walk to each segment's collapse cut bounds it, and the
+        # records it reads depend on where the cuts fall: no byte count
+        # comparable with the streaming stages (its time is reported)
+        "resolve": 0,
         # the wide chains and their curves' merge and fragments, on a second
         # stream beside chains, merge and fragment (their bytes are counted there)
         "wide": 0,

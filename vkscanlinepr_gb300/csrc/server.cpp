@@ -27,6 +27,9 @@
 
 namespace {
 
+// Batches of at most this many paths are sized by their paths' allotments.
+constexpr size_t kSmallBatchPaths = 8192;
+
 struct Request {
     uint64_t id = 0;
     uint32_t W = 0, H = 0;
@@ -255,10 +258,30 @@ bool sr_server::admit(Slot& sl) {
         }
         int64_t rec = 0, drw = 0;
         uint64_t bytes = 0;
+        size_t paths = 0;
         for (uint32_t i = 0; i < k; ++i) {
             rec += caps[2 * i];
             drw += caps[2 * i + 1];
             bytes += share[i];
+            paths += take[i]->fill_rule.size();
+        }
+        // The frame margin is calibrated where the errors of many paths
+        // average out; a batch of few paths (most batches under a steady
+        // request stream) takes the sum of its paths' own allotments
+        // instead, whose margins make an overflow -- and the whole-batch
+        // rerun with exact sizing that follows it -- rare.  (The sums cover
+        // every planned scene, at least the k admitted.)
+        if (paths <= kSmallBatchPaths && (plan.path_records > rec || plan.path_draws > drw)) {
+            const double before = (double)(rec + drw) + 1.0;
+            rec = std::max<int64_t>(rec, plan.path_records);
+            drw = std::max<int64_t>(drw, plan.path_draws);
+            // the requests hold their shares scaled to the larger capacities
+            const double f = ((double)(rec + drw) + 1.0) / before;
+            bytes = 0;
+            for (uint32_t i = 0; i < k; ++i) {
+                share[i] = (uint64_t)((double)share[i] * f);
+                bytes += share[i];
+            }
         }
         if (k < take.size()) {
             ++st.budget_waits;
