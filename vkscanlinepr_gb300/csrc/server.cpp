@@ -11,6 +11,7 @@
 // the bytes of the batches in flight plus the uncollected images under the
 // memory budget, using the predicted sizes.
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -222,6 +223,37 @@ bool sr_server::admit(Slot& sl) {
             fail_requests(take.size(), s);
             return true;
         }
+        // The frame margin is calibrated where the errors of many paths
+        // average out; a batch of few paths (most batches under a steady
+        // request stream) is sized by the sum of its paths' own allotments
+        // instead, whose margins make an overflow -- and the whole-batch
+        // rerun with exact sizing that follows it -- rare.  Each scene's
+        // capacities grow by the batch's factor before admission, so that
+        // the requests' shares of the budget cover them.
+        {
+            size_t paths = 0;
+            int64_t rall = 0, dall = 0;
+            for (size_t i = 0; i < take.size(); ++i) {
+                paths += take[i]->fill_rule.size();
+                rall += caps[2 * i];
+                dall += caps[2 * i + 1];
+            }
+            if (paths <= kSmallBatchPaths && (plan.path_records > rall || plan.path_draws > dall)) {
+                const double fr = std::max(1.0, (double)plan.path_records / (double)std::max<int64_t>(rall, 1));
+                const double fd = std::max(1.0, (double)plan.path_draws / (double)std::max<int64_t>(dall, 1));
+                int64_t r2 = 0, d2 = 0;
+                for (size_t i = 0; i < take.size(); ++i) {
+                    caps[2 * i] = (int64_t)std::ceil((double)caps[2 * i] * fr);
+                    caps[2 * i + 1] = (int64_t)std::ceil((double)caps[2 * i + 1] * fd);
+                    r2 += caps[2 * i];
+                    d2 += caps[2 * i + 1];
+                }
+                uint64_t fb = 0;
+                if (sr_batch_frame_bytes(sl.batch, r2, std::min<int64_t>(std::max<int64_t>(d2, 1), 2 * std::max<int64_t>(r2, 1)),
+                                         &fb) == SR_OK)
+                    plan.device_bytes = fb;
+            }
+        }
         // each request's share of the batch bytes, by its predicted records
         // and draw records, plus the copy of its finished image
         double weight = 0;
@@ -263,7 +295,6 @@ bool sr_server::admit(Slot& sl) {
             rec += caps[2 * i];
             drw += caps[2 * i + 1];
             bytes += share[i];
-            paths += take[i]->fill_rule.size();
         }
         // The frame margin is calibrated where the errors of many paths
         // average out; a batch of few paths (most batches under a steady
@@ -271,18 +302,7 @@ bool sr_server::admit(Slot& sl) {
         // instead, whose margins make an overflow -- and the whole-batch
         // rerun with exact sizing that follows it -- rare.  (The sums cover
         // every planned scene, at least the k admitted.)
-        if (paths <= kSmallBatchPaths && (plan.path_records > rec || plan.path_draws > drw)) {
-            const double before = (double)(rec + drw) + 1.0;
-            rec = std::max<int64_t>(rec, plan.path_records);
-            drw = std::max<int64_t>(drw, plan.path_draws);
-            // the requests hold their shares scaled to the larger capacities
-            const double f = ((double)(rec + drw) + 1.0) / before;
-            bytes = 0;
-            for (uint32_t i = 0; i < k; ++i) {
-                share[i] = (uint64_t)((double)share[i] * f);
-                bytes += share[i];
-            }
-        }
+        (void)paths;
         if (k < take.size()) {
             ++st.budget_waits;
             take.resize(k);
