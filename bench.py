@@ -521,8 +521,11 @@ def run_serving(sr, args, sz, margins):
     pool = [sr.synth_scene(2, 2, scene_index=i) for i in range(min(n, 1024))]
     rng = np.random.default_rng(4)
     arrivals = list(np.cumsum(rng.exponential(1.0 / args.serve_rate, n)))
-    out = {"requests": n, "rate_per_s": args.serve_rate, "scene_pool": len(pool), "budget_bytes": int(120e9)}
-    for name, sizer, slots in (("learned", sz, 3), ("exact", None, 1)):
+    out = {"requests": n, "rate_per_s": args.serve_rate, "scene_pool": len(pool), "budget_bytes": int(120e9),
+           "slots": {"learned": 2, "exact": 1}}
+    # two batches in flight: at 2,000 requests/s the tail was shortest with
+    # two (three let the largest scenes' frames share the GPU longer)
+    for name, sizer, slots in (("learned", sz, 2), ("exact", None, 1)):
         srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=args.serve_batch, memory_budget=120e9,
                               margins=margins)
         _serve(sr, srv, pool[:64], [None] * 64)                      # warm the slots' buffers
