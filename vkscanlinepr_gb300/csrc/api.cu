@@ -344,7 +344,12 @@ struct Pipeline {
         CUDA_TRY(cudaMallocHost(&h_u64, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(ctl, sizeof(uint32_t) * CTL_WORDS));
         CUDA_TRY(sr::geom_init());
-        CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        // the wide chains are the frame's longest dependency: their stream
+        // takes the highest priority, so that its blocks are placed first
+        // when both streams' chain kernels become ready at once
+        int lo_prio = 0, hi_prio = 0;
+        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+        CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi_prio));
         for (cudaEvent_t* e : {&ev_fork, &ev_merged, &ev_join})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
         return SR_OK;
