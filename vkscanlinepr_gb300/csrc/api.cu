@@ -344,12 +344,13 @@ struct Pipeline {
         CUDA_TRY(cudaMallocHost(&h_u64, sizeof(uint64_t) * 4));
         CUDA_TRY(ensure(ctl, sizeof(uint32_t) * CTL_WORDS));
         CUDA_TRY(sr::geom_init());
-        // the wide chains are the frame's longest dependency: their stream
-        // takes the highest priority, so that its blocks are placed first
-        // when both streams' chain kernels become ready at once
+        // the side stream takes the lowest priority: when both streams'
+        // chain kernels become ready at once, the caller's stream, which
+        // carries the wide chains (the frame's longest dependency), is
+        // placed first
         int lo_prio = 0, hi_prio = 0;
         CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
-        CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi_prio));
+        CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, lo_prio));
         for (cudaEvent_t* e : {&ev_fork, &ev_merged, &ev_join})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
         return SR_OK;
@@ -739,31 +740,33 @@ struct Pipeline {
             dbg.fleft = d_fleft.as<int32_t>();
             CUDA_TRY(cudaMemsetAsync(d_wscan.p, 0, sizeof(int32_t) * ((size_t)std::max<int64_t>(cap, 1) + 1), st));
         }
-        // the wide chains and their curves' merge and fragments on the side
-        // stream, the rest on st; the side stream's merge waits for st's
-        // merge (which marks the wide curves' records pending, and covers the
-        // short chains of the wide curves), and st waits for the side stream
-        // before the sort
+        // The wide chains -- the frame's longest dependency -- and their
+        // curves' merge and fragments stay on st, right behind the count
+        // pass, so that they start first; the other chains, merge and
+        // fragments run on the side stream beside them.  st's merge waits for
+        // the side stream's (which marks the wide curves' records pending and
+        // covers the short chains of the wide curves), and st waits for the
+        // side stream before the sort.
         CUDA_TRY(cudaEventRecord(ev_fork, st));
         CUDA_TRY(cudaStreamWaitEvent(side, ev_fork, 0));
-        mark(ST_WIDE, false, side);
-        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, 0, side);
-        mark(ST_CHAINS, false);
-        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, 1, st);
-        mark(ST_CHAINS, true);
-        mark(ST_MERGE, false);
-        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, 0, st);
-        mark(ST_MERGE, true);
-        CUDA_TRY(cudaEventRecord(ev_merged, st));
-        CUDA_TRY(cudaStreamWaitEvent(side, ev_merged, 0));
-        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, 1, side);
-        mark(ST_FRAGMENT, false);
+        mark(ST_WIDE, false, st);
+        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, 0, st);
+        mark(ST_CHAINS, false, side);
+        launch_chains(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), sm_count, 1, side);
+        mark(ST_CHAINS, true, side);
+        mark(ST_MERGE, false, side);
+        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, 0, side);
+        mark(ST_MERGE, true, side);
+        CUDA_TRY(cudaEventRecord(ev_merged, side));
+        CUDA_TRY(cudaStreamWaitEvent(st, ev_merged, 0));
+        launch_merge(g, offs.as<int32_t>(), cw, cbuf.as<int32_t>(), rec.as<int2>(), status, 1, st);
+        mark(ST_FRAGMENT, false, side);
         launch_fragment(g, rec.as<int2>(), offs.as<int32_t>(), cap, n_dev, keys.as<uint64_t>(),
-                        keep ? wnp.as<uint8_t>() : nullptr, dbg, cw, 0, st);
-        mark(ST_FRAGMENT, true);
+                        keep ? wnp.as<uint8_t>() : nullptr, dbg, cw, 0, side);
+        mark(ST_FRAGMENT, true, side);
         launch_fragment(g, rec.as<int2>(), offs.as<int32_t>(), cap, n_dev, keys.as<uint64_t>(),
-                        keep ? wnp.as<uint8_t>() : nullptr, dbg, cw, 1, side);
-        mark(ST_WIDE, true, side);
+                        keep ? wnp.as<uint8_t>() : nullptr, dbg, cw, 1, st);
+        mark(ST_WIDE, true, st);
         CUDA_TRY(cudaEventRecord(ev_join, side));
         CUDA_TRY(cudaStreamWaitEvent(st, ev_join, 0));
         const KeyLayout L = g.L;
