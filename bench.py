@@ -521,14 +521,22 @@ def run_serving(sr, args, sz, margins):
     pool = [sr.synth_scene(2, 2, scene_index=i) for i in range(min(n, 1024))]
     rng = np.random.default_rng(4)
     arrivals = list(np.cumsum(rng.exponential(1.0 / args.serve_rate, n)))
+    warm_n = min(512, max(len(pool) - 64, 0))
+    warm = list(np.cumsum(np.random.default_rng(3).exponential(1.0 / args.serve_rate, warm_n)))
     out = {"requests": n, "rate_per_s": args.serve_rate, "scene_pool": len(pool), "budget_bytes": int(120e9),
+           "warmup": "64 requests at once, then %d arrivals at the same rate (untimed)" % warm_n,
            "slots": {"learned": 2, "exact": 1}}
     # two batches in flight: at 2,000 requests/s the tail was shortest with
     # two (three let the largest scenes' frames share the GPU longer)
     for name, sizer, slots in (("learned", sz, 2), ("exact", None, 1)):
         srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=args.serve_batch, memory_budget=120e9,
                               margins=margins)
-        _serve(sr, srv, pool[:64], [None] * 64)                      # warm the slots' buffers
+        # untimed warm-up: a burst, then a stream of the same rate, so that
+        # every slot's buffers have grown to the batches a stream forms (a
+        # slot's first batch larger than any before reallocates its buffers,
+        # and a device-wide wait of the free stalls the scheduler)
+        _serve(sr, srv, pool[:64], [None] * 64)
+        _serve(sr, srv, pool[64:64 + warm_n], warm)
         t, imgs = _serve(sr, srv, pool, arrivals,
                          check_every=max(1, n // ORACLE_SAMPLE) if name == "learned" else 0)
         res = _lat_summary(t[:, 0], t[:, 1])

@@ -132,6 +132,7 @@ enum Stage : int {
 static sr_status check_status_word(uint32_t s) {
     if (s == 0) return SR_OK;
     if (s & sr::ERR_LOOKBACK_TIMEOUT) return fail(SR_ERR_TIMEOUT, "device look-back wait timed out (status 0x%x)", s);
+    if (s & sr::ERR_COPY_TIMEOUT) return fail(SR_ERR_TIMEOUT, "device bulk-copy wait timed out (status 0x%x)", s);
     if (s & sr::ERR_CAPACITY) return fail(SR_ERR_OVERFLOW_REFIT, "record capacity exceeded (status 0x%x)", s);
     return fail(SR_ERR_INTERNAL, "device consistency check failed (status 0x%x)", s);
 }
@@ -774,7 +775,7 @@ struct Pipeline {
         mark(ST_SORT, false);
         if (segmented() && seg_levels >= 0)
             launch_segsort(keys.as<uint64_t>(), skeys.as<uint64_t>(), keys_alt.as<uint64_t>(), cap, C, L, seg_levels,
-                           seg_scratch.p, seg_tiles.p, status, st);
+                           seg_scratch.p, seg_tiles.p, sm_count, status, st);
         else
             launch_sort_u64(sp, keys.as<uint64_t>(), nullptr, skeys.as<uint64_t>(),
                             keep ? svals.as<uint32_t>() : nullptr, keys_alt.as<uint64_t>(),

@@ -20,6 +20,7 @@ enum : uint32_t {
     ERR_RECORD_RANGE = 1u << 1,      // a curve produced a different record count than counted
     ERR_CAPACITY = 1u << 2,          // a pre-sized buffer was too small
     ERR_BAD_INDEX = 1u << 3,         // an index read from memory was out of range
+    ERR_COPY_TIMEOUT = 1u << 4,      // a wait for a bulk copy into shared memory gave up
 };
 
 // Polls a bounded spin makes before it gives up (with backoff, ~seconds),
@@ -116,6 +117,54 @@ SR_DEV uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
+}
+
+// ------------------------------------------------- bulk copies (TMA) --
+// One-dimensional bulk copies from global to shared memory, completed on a
+// shared-memory mbarrier (cp.async.bulk with complete_tx).  Addresses and
+// the size must be multiples of 16 bytes.
+SR_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+SR_DEV void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    // make the initialised barrier visible to the copy engine
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+SR_DEV void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+SR_DEV void bulk_load(void* dst_smem, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst_smem)),
+                 "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+SR_DEV bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Waits for phase `parity` of the barrier, at most spin_limit polls; false
+// (and ERR_COPY_TIMEOUT in the status word) when it gave up.
+SR_DEV bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t spin_limit, uint32_t* status) {
+    for (uint32_t i = 0; !mbar_test(bar, parity); ++i) {
+        if (i >= spin_limit) {
+            set_error(status, ERR_COPY_TIMEOUT);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    return true;
 }
 
 // ------------------------------------------------------- scan geometry --

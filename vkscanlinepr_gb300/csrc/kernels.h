@@ -181,10 +181,12 @@ void launch_segsort_tables(const uint32_t* curve_path, const int32_t* offs, uint
 // Device word holding the largest segment of more than half a tile (0 if none).
 const uint32_t* segsort_largest(const void* scratch, uint32_t n_curves);
 // Sorts keys_in[0, N) into keys_out by their key bits (layout L; N from the
-// tables; cap bounds the grid); `levels` merge rounds launched, at least
-// ceil(log2(chunks of the largest segment)).  keys_alt is scratch.
+// tables; cap bounds the tile tables); `levels` merge rounds launched, at
+// least ceil(log2(chunks of the largest segment)).  keys_alt is scratch.
+// The tile sort and the merge rounds run one wave of persistent CTAs.
 void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t n_curves,
-                    const KeyLayout& L, int levels, void* scratch, void* tiles, uint32_t* status, cudaStream_t st);
+                    const KeyLayout& L, int levels, void* scratch, void* tiles, int sm_count, uint32_t* status,
+                    cudaStream_t st);
 
 // ---- winding.cu
 struct WindArgs {

@@ -47,9 +47,13 @@ struct TileTables {
     int32_t* ntiles;       // [C + 2] tiles a segment opens; then exclusive scan -> first tile
     uint4* desc;           // [max_tiles] {start, segment size, k | rounds << 16 | chunk bit, -}
     uint32_t* tile_end;    // [max_tiles] end of a group tile (atomic max over its segments)
+    uint32_t* chunks;      // [max_tiles] the chunk tiles (of large segments), in no order
     uint64_t* scan_status;
-    uint32_t* ctl;         // [0] scan counter
+    // [0] scan counter, [1] chunk tiles, [2] next tile of the tile sort,
+    // [3 + l] next work item of merge round l
+    uint32_t* ctl;
 };
+constexpr int kCtlChunks = 1, kCtlSortNext = 2, kCtlMergeNext = 3;
 
 size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 size_t scan_area(uint32_t C) { return round256(scan_status_words((int64_t)C + 1) * 8); }
@@ -86,6 +90,8 @@ TileTables carve_back(void* base, uint32_t C, int64_t cap) {
     t.desc = reinterpret_cast<uint4*>(b);
     b += round256(mt * 16);
     t.tile_end = reinterpret_cast<uint32_t*>(b);
+    b += round256(mt * 4);
+    t.chunks = reinterpret_cast<uint32_t*>(b);
     b += round256(mt * 4);
     t.scan_status = reinterpret_cast<uint64_t*>(b);
     b += scan_area(C);
@@ -166,8 +172,12 @@ __global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
     const int32_t n = u.ntiles[s + 1] - first;
     if (size > (uint32_t)kGroup) {
         const uint32_t rounds = rounds_of((uint32_t)n);
-        for (int32_t k = 0; k < n && (uint32_t)(first + k) < mt; ++k)
+        const int32_t m = (int32_t)min((uint32_t)n, mt - min(mt, (uint32_t)first));   // chunks that fit the table
+        const uint32_t at = m > 0 ? atomicAdd(&u.ctl[kCtlChunks], (uint32_t)m) : 0u;
+        for (int32_t k = 0; k < m; ++k) {
             u.desc[first + k] = make_uint4(a, size, (uint32_t)k | (rounds << 16) | kChunkBit, 0u);
+            u.chunks[at + k] = (uint32_t)(first + k);
+        }
         return;
     }
     // a non-head small segment belongs to the tile opened just before it
@@ -179,11 +189,13 @@ __global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
 
 // ----------------------------------------------------------- local sort ---
 struct LocalSmem {
-    uint64_t buf[2][kTile];
+    uint64_t buf[kTile + 2];   // the tile; its bulk copy may start one key early
     uint32_t warp_hist[kWarps][kRadix];
     uint32_t digit_start[kRadix];
     uint32_t scan_tmp[kWarps];
-    uint64_t kmin[kWarps], kmax[kWarps];
+    uint32_t red[kWarps][6];
+    uint64_t kred[kWarps][3];
+    uint64_t bar;
 };
 
 SR_DEV uint32_t same_digit_lanes(uint32_t d) {
@@ -205,35 +217,28 @@ struct KeyFields {
     SR_DEV uint32_t p(uint64_t k) const { return (uint32_t)((k >> (xb + rb)) & ((1ull << pb) - 1)); }
 };
 
-SR_DEV uint32_t block_min_max(uint32_t v, bool is_max, uint32_t* red) {
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        const uint32_t u = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-        v = is_max ? max(v, u) : min(v, u);
-    }
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    v = red[0];
-#pragma unroll
-    for (int w = 1; w < kWarps; ++w) v = is_max ? max(v, red[w]) : min(v, red[w]);
-    __syncthreads();
-    return v;
-}
+SR_DEV uint32_t bits_of(uint32_t v) { return v ? 32u - (uint32_t)__clz((int)v) : 0u; }
+SR_DEV uint32_t low_mask(uint32_t b) { return b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u; }
 
 // CTA b sorts tile b (a group of small segments, or a chunk of a large one).
-// Within a tile the order is that of a compact local key, the mixed-radix
-// number (path - pmin, rank - rmin, x - xmin) over the tile's ranges, which
-// usually needs 2-3 digit passes where the whole key needs 4-6.
-__global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __restrict__ keys_in,
-                                                            uint64_t* __restrict__ keys_out,
-                                                            uint64_t* __restrict__ keys_alt, uint32_t C,
-                                                            KeyFields kf, uint32_t n_cap, TileTables u) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    LocalSmem& S = *reinterpret_cast<LocalSmem*>(smem_raw);
+//   * The tile reaches shared memory by one bulk copy (TMA) of its 16-byte
+//     aligned span; an odd last key comes by a plain load.
+//   * Within a tile the order is that of a compact item: the fields
+//     (path - pmin, rank - rmin, x - xmin) packed in the fewest bits their
+//     ranges need, in the low 32 bits, the payload above.  It usually needs
+//     2-3 digit passes where the whole key needs 4-6, and a digit is one
+//     shift of a 32-bit word.  A tile whose fields need more than 32 bits
+//     sorts the bits where its keys differ instead.
+//   * Each pass ranks the digits per warp in registers, scans the counts and
+//     scatters back into the same buffer (every read is done by then).
+//   * The CTAs are persistent (one wave) and take tiles from a counter, so
+//     the grid does not follow the table's bound on the tiles.
+// Returns false when a copy wait gave up (the CTA then leaves).
+SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64_t* __restrict__ keys_in,
+                      uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt, const KeyFields& kf,
+                      uint32_t n_cap, const TileTables& u, uint32_t* status, uint32_t spin_limit) {
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
-    if ((int32_t)blockIdx.x >= u.ntiles[C]) return;
-    const uint4 d = u.desc[blockIdx.x];
+    const uint4 d = u.desc[tile];
     uint32_t a, e;
     bool to_alt = false;
     if (d.z & kChunkBit) {
@@ -243,77 +248,132 @@ __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __re
         to_alt = (rounds & 1u) != 0;   // the segment's last merge round lands in keys_out
     } else {
         a = d.x;
-        e = u.tile_end[blockIdx.x];
+        e = u.tile_end[tile];
     }
     // a frame whose records overflowed the buffers is redone: never read past them
     a = min(a, n_cap);
     e = min(max(e, a), n_cap);
     const uint32_t len = e - a;
-    if (len == 0) return;
+    if (len == 0 || len > (uint32_t)kTile) return true;
     uint64_t* dst = to_alt ? keys_alt : keys_out;
 
-    // load (coalesced); ranges of the key fields and of the whole key
-    const uint64_t kmask = (1ull << (kf.xb + kf.rb + kf.pb)) - 1ull;
+    // stage the tile: keys [a0, e0) by one bulk copy, key e - 1 by a load when e is odd
+    uint32_t off = 0;
+    if ((reinterpret_cast<uintptr_t>(keys_in) & 15u) == 0) {
+        const uint32_t a0 = a & ~1u, e0 = e & ~1u;
+        const uint32_t nb = e0 - a0;   // e > a >= a0, so e0 >= a0
+        off = a - a0;
+        if (tid == 0) {
+            if (nb) {
+                // the previous tile's reads of the buffer came before (the
+                // caller's barrier); order them before the copy's writes
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(&S.bar, nb * 8u);
+                bulk_load(S.buf, keys_in + a0, nb * 8u, &S.bar);
+            }
+            if (e & 1u) S.buf[nb] = keys_in[e - 1];
+        }
+        __syncthreads();
+        const bool ok = nb == 0 || mbar_wait_bounded(&S.bar, phase, spin_limit, status);
+        if (__syncthreads_or(!ok)) {
+            // gave up: let the copy land before the CTA leaves
+            if (nb) mbar_wait_bounded(&S.bar, phase, spin_limit, nullptr);
+            return false;
+        }
+        if (nb) phase ^= 1u;
+    } else {
+        for (uint32_t j = tid; j < len; j += kThreads) S.buf[j] = keys_in[a + j];
+        __syncthreads();
+    }
+
+    // ranges of the key fields, of the key bits and of the whole key
+    const uint32_t kbits = kf.xb + kf.rb + kf.pb;
+    const uint64_t kmask = (1ull << kbits) - 1ull;
     uint32_t pmin = ~0u, pmax = 0, rmin = ~0u, rmax = 0, xmin = ~0u, xmax = 0;
-    uint64_t lo = ~0ull, hi = 0;
+    uint64_t lo = ~0ull, hi = 0, top = 0;
     for (uint32_t j = tid; j < len; j += kThreads) {
-        const uint64_t k = keys_in[a + j];
-        S.buf[0][j] = k;
-        pmin = min(pmin, kf.p(k)); pmax = max(pmax, kf.p(k));
-        rmin = min(rmin, kf.r(k)); rmax = max(rmax, kf.r(k));
-        xmin = min(xmin, kf.x(k)); xmax = max(xmax, kf.x(k));
-        lo = min(lo, k & kmask);
-        hi = max(hi, k & kmask);
+        {
+            const uint64_t k = S.buf[off + j];
+            const uint32_t p = kf.p(k), r = kf.r(k), x = kf.x(k);
+            pmin = min(pmin, p); pmax = max(pmax, p);
+            rmin = min(rmin, r); rmax = max(rmax, r);
+            xmin = min(xmin, x); xmax = max(xmax, x);
+            lo = min(lo, k & kmask);
+            hi = max(hi, k & kmask);
+            top = max(top, k);
+        }
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
+        pmin = min(pmin, __shfl_xor_sync(0xFFFFFFFFu, pmin, o));
+        pmax = max(pmax, __shfl_xor_sync(0xFFFFFFFFu, pmax, o));
+        rmin = min(rmin, __shfl_xor_sync(0xFFFFFFFFu, rmin, o));
+        rmax = max(rmax, __shfl_xor_sync(0xFFFFFFFFu, rmax, o));
+        xmin = min(xmin, __shfl_xor_sync(0xFFFFFFFFu, xmin, o));
+        xmax = max(xmax, __shfl_xor_sync(0xFFFFFFFFu, xmax, o));
         lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
         hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+        top = max(top, __shfl_xor_sync(0xFFFFFFFFu, top, o));
     }
     if (lane == 0) {
-        S.kmin[warp] = lo;
-        S.kmax[warp] = hi;
+        S.red[warp][0] = pmin; S.red[warp][1] = pmax;
+        S.red[warp][2] = rmin; S.red[warp][3] = rmax;
+        S.red[warp][4] = xmin; S.red[warp][5] = xmax;
+        S.kred[warp][0] = lo; S.kred[warp][1] = hi; S.kred[warp][2] = top;
     }
-    uint32_t* red = S.scan_tmp;
-    pmin = block_min_max(pmin, false, red); pmax = block_min_max(pmax, true, red);
-    rmin = block_min_max(rmin, false, red); rmax = block_min_max(rmax, true, red);
-    xmin = block_min_max(xmin, false, red); xmax = block_min_max(xmax, true, red);
-    lo = S.kmin[0];
-    hi = S.kmax[0];
+    __syncthreads();
 #pragma unroll
-    for (int w = 1; w < kWarps; ++w) {
-        lo = min(lo, S.kmin[w]);
-        hi = max(hi, S.kmax[w]);
+    for (int w = 0; w < kWarps; ++w) {
+        pmin = min(pmin, S.red[w][0]); pmax = max(pmax, S.red[w][1]);
+        rmin = min(rmin, S.red[w][2]); rmax = max(rmax, S.red[w][3]);
+        xmin = min(xmin, S.red[w][4]); xmax = max(xmax, S.red[w][5]);
+        lo = min(lo, S.kred[w][0]); hi = max(hi, S.kred[w][1]); top = max(top, S.kred[w][2]);
     }
-    const uint64_t Rx = (uint64_t)(xmax - xmin) + 1, Rr = (uint64_t)(rmax - rmin) + 1, Rp = (uint64_t)(pmax - pmin) + 1;
-    // the compact key when the product of the ranges fits 32 bits; else the
-    // bits where the tile's keys differ
-    const bool fits = Rp * Rr <= 0xFFFFFFFFull && Rp * Rr * Rx <= 0x100000000ull;
-    const uint64_t span = fits ? Rp * Rr * Rx : 0;
-    const uint32_t bits = fits ? (span <= 1 ? 0u : 64u - (uint32_t)__clzll((long long)(span - 1)))
-                               : (lo == hi ? 0u : 64u - (uint32_t)__clzll((long long)(lo ^ hi)));
+    const uint32_t bp = bits_of(pmax - pmin), br = bits_of(rmax - rmin), bx = bits_of(xmax - xmin);
+    // compact items when the fields fit 32 bits and the payload the other 32
+    const bool compact = bp + br + bx <= 32u && (top >> kbits) <= 0xFFFFFFFFull;
+    const uint32_t bits = compact ? bp + br + bx : (lo == hi ? 0u : 64u - (uint32_t)__clzll((long long)(lo ^ hi)));
     const uint32_t passes = (bits + kRadixBits - 1) / kRadixBits;
-    const uint32_t rr = (uint32_t)Rr, rx = (uint32_t)Rx;
-    auto digit = [&](uint64_t k, uint32_t shift) -> uint32_t {
-        if (fits) return ((((kf.p(k) - pmin) * rr + (kf.r(k) - rmin)) * rx + (kf.x(k) - xmin)) >> shift) & (kRadix - 1);
-        return (uint32_t)((k & kmask) >> shift) & (kRadix - 1);
+    auto to_item = [&](uint64_t k) -> uint64_t {
+        const uint64_t c = ((uint64_t)(kf.p(k) - pmin) << (br + bx)) | ((uint64_t)(kf.r(k) - rmin) << bx) |
+                           (uint64_t)(kf.x(k) - xmin);
+        return ((k >> kbits) << 32) | c;
     };
-
-    int cur = 0;
+    auto digit = [&](uint64_t v, uint32_t shift) -> uint32_t {
+        if (compact) return ((uint32_t)v >> shift) & (kRadix - 1);
+        return (uint32_t)((v & kmask) >> shift) & (kRadix - 1);
+    };
+    // the items, from slot 0 (every read of the staged keys preceded the
+    // reduction's barrier; the first pass's barrier publishes the writes)
+    if (passes > 0 && (compact || off)) {
+        uint64_t kv[kItems];
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) {
+            const uint32_t j = tid + (uint32_t)i * kThreads;
+            kv[i] = j < len ? S.buf[off + j] : 0ull;
+        }
+        if (off) __syncthreads();   // the items move down one slot
+#pragma unroll
+        for (int i = 0; i < kItems; ++i) {
+            const uint32_t j = tid + (uint32_t)i * kThreads;
+            if (j < len) S.buf[j] = compact ? to_item(kv[i]) : kv[i];
+        }
+    }
+    const uint32_t src = passes > 0 ? 0u : off;
     for (uint32_t pass = 0; pass < passes; ++pass) {
         const uint32_t shift = pass * kRadixBits;
         for (int i = tid; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
         __syncthreads();
         // rank within the warp: warp w holds slots [w*512, w*512 + 512)
         uint64_t k[kItems];
-        uint32_t rank[kItems], dig[kItems];
+        uint32_t rd[kItems];   // rank | digit << 16
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
             const uint32_t j = warp * (32 * kItems) + it * 32 + lane;
             const bool ok = j < len;
-            k[it] = ok ? S.buf[cur][j] : 0ull;
-            const uint32_t dg = ok ? digit(k[it], shift) : (uint32_t)kRadix;
-            dig[it] = dg;
+            const uint64_t v = ok ? S.buf[j] : 0ull;
+            k[it] = v;
+            const uint32_t dg = ok ? digit(v, shift) : (uint32_t)kRadix;
             const uint32_t peers = same_digit_lanes(dg);
             const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
             uint32_t before = 0;
@@ -322,7 +382,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __re
                 S.warp_hist[warp][dg] = before + (uint32_t)__popc(peers);
             }
             before = __shfl_sync(0xFFFFFFFFu, before, leader);
-            rank[it] = before + (uint32_t)__popc(peers & lanemask_lt());
+            rd[it] = (before + (uint32_t)__popc(peers & lanemask_lt())) | (dg << 16);
             __syncwarp();
         }
         __syncthreads();
@@ -356,16 +416,62 @@ __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __re
         __syncthreads();
         S.digit_start[dd] = S.scan_tmp[warp] + x - cnt;
         __syncthreads();
-        // scatter into the other buffer (stable: digit, then warp, then slot)
+        // scatter (stable: digit, then warp, then slot)
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
             const uint32_t j = warp * (32 * kItems) + it * 32 + lane;
-            if (j < len) S.buf[cur ^ 1][S.digit_start[dig[it]] + S.warp_hist[warp][dig[it]] + rank[it]] = k[it];
+            const uint32_t dg = rd[it] >> 16;
+            if (j < len) S.buf[S.digit_start[dg] + S.warp_hist[warp][dg] + (rd[it] & 0xFFFFu)] = k[it];
         }
         __syncthreads();
-        cur ^= 1;
     }
-    for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[cur][j];
+    if (compact && passes > 0) {
+        // the fields' minima again from shared memory (fewer live registers
+        // through the passes)
+        uint32_t p0 = S.red[0][0], r0 = S.red[0][2], x0 = S.red[0][4];
+        uint32_t p1 = S.red[0][1], r1 = S.red[0][3], x1 = S.red[0][5];
+#pragma unroll
+        for (int w = 1; w < kWarps; ++w) {
+            p0 = min(p0, S.red[w][0]); r0 = min(r0, S.red[w][2]); x0 = min(x0, S.red[w][4]);
+            p1 = max(p1, S.red[w][1]); r1 = max(r1, S.red[w][3]); x1 = max(x1, S.red[w][5]);
+        }
+        const uint32_t rb = bits_of(r1 - r0), xb = bits_of(x1 - x0);
+        const uint32_t kb = kf.xb + kf.rb + kf.pb;
+        for (uint32_t j = tid; j < len; j += kThreads) {
+            const uint64_t v = S.buf[j];
+            const uint32_t c = (uint32_t)v;
+            const uint32_t x = x0 + (c & low_mask(xb));
+            const uint32_t r = r0 + (uint32_t)(((uint64_t)c >> xb) & low_mask(rb));
+            const uint32_t p = p0 + (uint32_t)((uint64_t)c >> (rb + xb));
+            dst[a + j] = ((v >> 32) << kb) | ((uint64_t)p << (kf.xb + kf.rb)) | ((uint64_t)r << kf.xb) | (uint64_t)x;
+        }
+        (void)p1;
+    } else {
+        for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[src + j];
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __restrict__ keys_in,
+                                                            uint64_t* __restrict__ keys_out,
+                                                            uint64_t* __restrict__ keys_alt, uint32_t C,
+                                                            KeyFields kf, uint32_t n_cap, uint32_t mt,
+                                                            TileTables u, uint32_t* status, uint32_t spin_limit) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LocalSmem& S = *reinterpret_cast<LocalSmem*>(smem_raw);
+    __shared__ uint32_t next;
+    // tiles past the table exist only in a frame whose records overflowed (redone)
+    const uint32_t n_tiles = min((uint32_t)u.ntiles[C], mt);
+    if (threadIdx.x == 0) mbar_init(&S.bar, 1);
+    uint32_t phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(&u.ctl[kCtlSortNext], 1u);
+        __syncthreads();   // also: the previous tile is done with the buffers
+        const uint32_t tile = next;
+        __syncthreads();
+        if (tile >= n_tiles) break;
+        if (!sort_tile(S, tile, phase, keys_in, keys_out, keys_alt, kf, n_cap, u, status, spin_limit)) return;
+    }
 }
 
 // ---------------------------------------------------------------- merge ---
@@ -415,21 +521,18 @@ SR_DEV uint32_t warp_merge_split(const uint64_t* A, uint32_t na, const uint64_t*
     return lo;
 }
 
-__global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__ keys_out,
-                                                          uint64_t* __restrict__ keys_alt, uint32_t C, uint32_t level,
-                                                          uint32_t key_bits, uint32_t n_cap, TileTables u) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    MergeSmem& S = *reinterpret_cast<MergeSmem*>(smem_raw);
-    if ((int32_t)(blockIdx.x >> 1) >= u.ntiles[C]) return;
-    const uint4 desc = u.desc[blockIdx.x >> 1];
-    if (!(desc.z & kChunkBit)) return;
+// Work item w is half w & 1 of chunk tile chunks[w >> 1]; the CTAs are
+// persistent (one wave) and take items from the round's counter.
+SR_DEV void merge_item(MergeSmem& S, uint32_t item, uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt,
+                       uint32_t level, uint32_t key_bits, uint32_t n_cap, const TileTables& u) {
+    const uint4 desc = u.desc[u.chunks[item >> 1]];
     const uint32_t k = desc.z & 0xFFFFu, rounds = (desc.z >> 16) & 0x7FFFu;
     if (level >= rounds) return;
     const uint64_t* src = ((rounds - level) & 1u) ? keys_alt : keys_out;
     uint64_t* dst = ((rounds - level) & 1u) ? keys_out : keys_alt;
     const uint32_t s0 = desc.x, size = desc.y;
     if ((uint64_t)s0 + size > n_cap) return;   // overflowed frame: redone
-    const uint32_t o0 = k * (uint32_t)kTile + (blockIdx.x & 1u) * (uint32_t)kMergeOut;
+    const uint32_t o0 = k * (uint32_t)kTile + (item & 1u) * (uint32_t)kMergeOut;
     if (o0 >= size) return;
     const uint32_t o1 = min(o0 + (uint32_t)kMergeOut, size);
     const uint32_t W = (uint32_t)kTile << level;
@@ -472,12 +575,29 @@ __global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__
     for (uint32_t j = tid; j < n; j += kThreads) dst[s0 + o0 + j] = S.out[j];
 }
 
+__global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__ keys_out,
+                                                          uint64_t* __restrict__ keys_alt, uint32_t level,
+                                                          uint32_t key_bits, uint32_t n_cap, TileTables u) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MergeSmem& S = *reinterpret_cast<MergeSmem*>(smem_raw);
+    __shared__ uint32_t next;
+    const uint32_t n_items = 2u * u.ctl[kCtlChunks];
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(&u.ctl[kCtlMergeNext + level], 1u);
+        __syncthreads();   // also: the previous item is done with the buffers
+        const uint32_t item = next;
+        __syncthreads();
+        if (item >= n_items) break;
+        merge_item(S, item, keys_out, keys_alt, level, key_bits, n_cap, u);
+    }
+}
+
 // ------------------------------------------------------------- launches --
 size_t segsort_scratch_bytes(uint32_t C) { return 2 * round256(((size_t)C + 2) * 4) + scan_area(C) + 256; }
 
 size_t segsort_tile_bytes(uint32_t C, int64_t cap) {
     const size_t mt = max_tiles(C, cap);
-    return round256(((size_t)C + 2) * 4) + round256(mt * 16) + round256(mt * 4) + scan_area(C) + 256;
+    return round256(((size_t)C + 2) * 4) + round256(mt * 16) + 2 * round256(mt * 4) + scan_area(C) + 256;
 }
 
 int segsort_tile() { return kTile; }
@@ -501,7 +621,7 @@ const uint32_t* segsort_largest(const void* scratch, uint32_t C) {
 }
 
 void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t C,
-                    const KeyLayout& L, int levels, void* scratch, void* tiles, uint32_t* status,
+                    const KeyLayout& L, int levels, void* scratch, void* tiles, int sm_count, uint32_t* status,
                     cudaStream_t st) {
     if (cap <= 0 || C == 0) return;
     SegTables t = carve_front(scratch, C);
@@ -517,17 +637,29 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     k_seg_desc<<<g, 256, 0, st>>>(C, (uint32_t)mt, t, u);
     const uint32_t key_bits = L.pbits + L.rbits + L.xbits;
     const KeyFields kf{L.xbits, L.rbits, L.pbits};
+    // resident CTAs per SM of the two persistent kernels (same on every
+    // device of the build's architecture)
     static std::atomic<uint32_t> attr{0};
+    static std::atomic<int> occ_sort{0}, occ_merge{0};
     once_per_device(attr, [] {
         cudaFuncSetAttribute(k_local_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LocalSmem));
         cudaFuncSetAttribute(k_merge_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
+        int a = 0, b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_local_sort, kThreads, sizeof(LocalSmem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_merge_level, kThreads, sizeof(MergeSmem));
+        occ_sort.store(std::max(a, 1));
+        occ_merge.store(std::max(b, 1));
     });
+    const int sms = std::max(sm_count, 1);
+    const unsigned g_sort = (unsigned)std::min<size_t>(mt, (size_t)sms * (size_t)std::max(occ_sort.load(), 1));
+    const unsigned g_merge = (unsigned)std::min<size_t>(2 * mt, (size_t)sms * (size_t)std::max(occ_merge.load(), 1));
     count_launches(1 + (uint32_t)levels);
     const uint32_t n_cap = (uint32_t)cap;
-    k_local_sort<<<(unsigned)mt, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap, u);
+    k_local_sort<<<g_sort, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap,
+                                                              (uint32_t)mt, u, status, spin_limit());
     for (int lv = 0; lv < levels; ++lv)
-        k_merge_level<<<(unsigned)(2 * mt), kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, C, (uint32_t)lv, key_bits,
-                                                                         n_cap, u);
+        k_merge_level<<<g_merge, kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, (uint32_t)lv, key_bits, n_cap,
+                                                                    u);
 }
 
 }  // namespace sr

@@ -288,21 +288,14 @@ bool sr_server::admit(Slot& sl) {
             budget_blocked = true;
             return false;
         }
+        // capacities of the admitted scenes (grown by the batch factor above)
         int64_t rec = 0, drw = 0;
         uint64_t bytes = 0;
-        size_t paths = 0;
         for (uint32_t i = 0; i < k; ++i) {
             rec += caps[2 * i];
             drw += caps[2 * i + 1];
             bytes += share[i];
         }
-        // The frame margin is calibrated where the errors of many paths
-        // average out; a batch of few paths (most batches under a steady
-        // request stream) takes the sum of its paths' own allotments
-        // instead, whose margins make an overflow -- and the whole-batch
-        // rerun with exact sizing that follows it -- rare.  (The sums cover
-        // every planned scene, at least the k admitted.)
-        (void)paths;
         if (k < take.size()) {
             ++st.budget_waits;
             take.resize(k);
