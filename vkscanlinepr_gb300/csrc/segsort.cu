@@ -189,7 +189,7 @@ __global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
 
 // ----------------------------------------------------------- local sort ---
 struct LocalSmem {
-    uint64_t buf[kTile + 2];   // the tile; its bulk copy may start one key early
+    uint64_t buf[2][kTile + 2];   // the tile (its bulk copy may start one key early), and the pass target
     uint32_t warp_hist[kWarps][kRadix];
     uint32_t digit_start[kRadix];
     uint32_t scan_tmp[kWarps];
@@ -269,9 +269,9 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
                 // caller's barrier); order them before the copy's writes
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_expect_tx(&S.bar, nb * 8u);
-                bulk_load(S.buf, keys_in + a0, nb * 8u, &S.bar);
+                bulk_load(S.buf[0], keys_in + a0, nb * 8u, &S.bar);
             }
-            if (e & 1u) S.buf[nb] = keys_in[e - 1];
+            if (e & 1u) S.buf[0][nb] = keys_in[e - 1];
         }
         __syncthreads();
         const bool ok = nb == 0 || mbar_wait_bounded(&S.bar, phase, spin_limit, status);
@@ -282,7 +282,7 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         }
         if (nb) phase ^= 1u;
     } else {
-        for (uint32_t j = tid; j < len; j += kThreads) S.buf[j] = keys_in[a + j];
+        for (uint32_t j = tid; j < len; j += kThreads) S.buf[0][j] = keys_in[a + j];
         __syncthreads();
     }
 
@@ -293,7 +293,7 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
     uint64_t lo = ~0ull, hi = 0, top = 0;
     for (uint32_t j = tid; j < len; j += kThreads) {
         {
-            const uint64_t k = S.buf[off + j];
+            const uint64_t k = S.buf[0][off + j];
             const uint32_t p = kf.p(k), r = kf.r(k), x = kf.x(k);
             pmin = min(pmin, p); pmax = max(pmax, p);
             rmin = min(rmin, r); rmax = max(rmax, r);
@@ -343,37 +343,33 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         if (compact) return ((uint32_t)v >> shift) & (kRadix - 1);
         return (uint32_t)((v & kmask) >> shift) & (kRadix - 1);
     };
-    // the items, from slot 0 (every read of the staged keys preceded the
-    // reduction's barrier; the first pass's barrier publishes the writes)
+    // the items from slot 0 of the other buffer (staged keys sit at off)
+    uint32_t cur = 0, src = off;
     if (passes > 0 && (compact || off)) {
-        uint64_t kv[kItems];
-#pragma unroll
-        for (int i = 0; i < kItems; ++i) {
-            const uint32_t j = tid + (uint32_t)i * kThreads;
-            kv[i] = j < len ? S.buf[off + j] : 0ull;
+        for (uint32_t j = tid; j < len; j += kThreads) {
+            const uint64_t k = S.buf[0][off + j];
+            S.buf[1][j] = compact ? to_item(k) : k;
         }
-        if (off) __syncthreads();   // the items move down one slot
-#pragma unroll
-        for (int i = 0; i < kItems; ++i) {
-            const uint32_t j = tid + (uint32_t)i * kThreads;
-            if (j < len) S.buf[j] = compact ? to_item(kv[i]) : kv[i];
-        }
+        cur = 1;
+        src = 0;
     }
-    const uint32_t src = passes > 0 ? 0u : off;
     for (uint32_t pass = 0; pass < passes; ++pass) {
         const uint32_t shift = pass * kRadixBits;
+        const uint64_t* in = S.buf[cur] + src;
         for (int i = tid; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
         __syncthreads();
-        // rank within the warp: warp w holds slots [w*512, w*512 + 512)
-        uint64_t k[kItems];
+        // rank within the warp: warp w holds slots [w*512, w*512 + 512); rows
+        // of slots past the tile's end are skipped whole (a tile is about
+        // half full on average)
+        const uint32_t wfirst = warp * (32u * kItems);
+        const uint32_t rows = wfirst >= len ? 0u : min((uint32_t)kItems, (len - wfirst + 31u) / 32u);
         uint32_t rd[kItems];   // rank | digit << 16
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
-            const uint32_t j = warp * (32 * kItems) + it * 32 + lane;
+            if ((uint32_t)it >= rows) break;
+            const uint32_t j = wfirst + (uint32_t)it * 32u + lane;
             const bool ok = j < len;
-            const uint64_t v = ok ? S.buf[j] : 0ull;
-            k[it] = v;
-            const uint32_t dg = ok ? digit(v, shift) : (uint32_t)kRadix;
+            const uint32_t dg = ok ? digit(in[j], shift) : (uint32_t)kRadix;
             const uint32_t peers = same_digit_lanes(dg);
             const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
             uint32_t before = 0;
@@ -416,14 +412,18 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         __syncthreads();
         S.digit_start[dd] = S.scan_tmp[warp] + x - cnt;
         __syncthreads();
-        // scatter (stable: digit, then warp, then slot)
+        // scatter into the other buffer (stable: digit, then warp, then slot)
+        uint64_t* out = S.buf[cur ^ 1u];
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
-            const uint32_t j = warp * (32 * kItems) + it * 32 + lane;
+            if ((uint32_t)it >= rows) break;
+            const uint32_t j = wfirst + (uint32_t)it * 32u + lane;
             const uint32_t dg = rd[it] >> 16;
-            if (j < len) S.buf[S.digit_start[dg] + S.warp_hist[warp][dg] + (rd[it] & 0xFFFFu)] = k[it];
+            if (j < len) out[S.digit_start[dg] + S.warp_hist[warp][dg] + (rd[it] & 0xFFFFu)] = in[j];
         }
         __syncthreads();
+        cur ^= 1u;
+        src = 0;
     }
     if (compact && passes > 0) {
         // the fields' minima again from shared memory (fewer live registers
@@ -438,7 +438,7 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         const uint32_t rb = bits_of(r1 - r0), xb = bits_of(x1 - x0);
         const uint32_t kb = kf.xb + kf.rb + kf.pb;
         for (uint32_t j = tid; j < len; j += kThreads) {
-            const uint64_t v = S.buf[j];
+            const uint64_t v = S.buf[cur][j];
             const uint32_t c = (uint32_t)v;
             const uint32_t x = x0 + (c & low_mask(xb));
             const uint32_t r = r0 + (uint32_t)(((uint64_t)c >> xb) & low_mask(rb));
@@ -447,7 +447,7 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         }
         (void)p1;
     } else {
-        for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[src + j];
+        for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[cur][src + j];
     }
     return true;
 }
