@@ -310,6 +310,12 @@ void sr_set_spin_limit(uint32_t polls);
  * reference counterpart. */
 sr_status sr_debug_scan_without_first_tile(const int32_t* d_in, int32_t* d_out, int64_t n, void* stream);
 
+/* Tiles of the last frame's per-path sort and, of those, the ones sorted
+ * with 64-bit items (their packed key fields and payload need more than 32
+ * bits); both 0 when the frame took the radix sort.  Waits for the device.
+ * No reference counterpart. */
+sr_status sr_debug_sort_tiles(sr_ctx* ctx, uint32_t* tiles, uint32_t* wide_tiles);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* sr_last_error(void);
 

@@ -74,3 +74,33 @@ def test_many_tiny_paths(gpu, oracle_lib):
     want = oracle_lib.Frame(scenes.to_oracle(d), mode=1).get("image")
     img, _ = _render(gpu, d)
     assert np.array_equal(img, want)
+
+
+def _scattered(w, h, n, seed):
+    # many small paths spread over a wide canvas (some reaching past its
+    # edges): a tile holds paths far apart, so its packed key fields need
+    # more than the 32-bit items' bits and it is sorted with 64-bit items
+    rng = np.random.default_rng(seed)
+    b = scenes.Builder(w, h)
+    for i in range(n):
+        x, y = rng.uniform(-8, w + 8), rng.uniform(-8, h + 8)
+        s = rng.uniform(2.0, 9.0)
+        b.path(rule=int(i % 2), rgba=(int(i % 251), 90, 30, 100 + i % 150))
+        b.polygon([(x, y), (x + s, y + 0.3 * s), (x + 0.4 * s, y + s)])
+    return b.arrays()
+
+
+@pytest.mark.parametrize("w,h,n,seed", [(16384, 1024, 2500, 5), (4096, 4096, 3000, 6)])
+def test_tiles_sorted_with_64bit_items(gpu, oracle_lib, w, h, n, seed):
+    d = _scattered(w, h, n, seed)
+    of = oracle_lib.Frame(scenes.to_oracle(d), mode=1)
+    r = gpu.ScanlineVGRasterizer(mode=1)
+    r.initialize(None, w, h)
+    r.loadVG(scenes.to_container(d))
+    img = r.render()
+    tiles, wide = r.sort_tiles()
+    assert tiles > 0 and wide > 0
+    # the draw list follows the sorted order record by record
+    assert np.array_equal(r.dump("draw_list"), of.get("draw_list"))
+    assert np.array_equal(img, of.get("image"))
+    r.close()

@@ -181,7 +181,7 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
            "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
            "sr_debug_scan_without_first_tile", "sr_write_image", "sr_rvg_load_full", "sr_set_paints",
-           "sr_scene_buf_paints", "sr_render_aa"]
+           "sr_scene_buf_paints", "sr_render_aa", "sr_debug_sort_tiles"]
 
 _lib = None
 
@@ -222,6 +222,7 @@ def lib():
     L.sr_set_spin_limit.argtypes = [ctypes.c_uint32]
     L.sr_set_spin_limit.restype = None
     L.sr_debug_scan_without_first_tile.argtypes = [vp, vp, ctypes.c_int64, vp]
+    L.sr_debug_sort_tiles.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]
     L.sr_write_image.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
     L.sr_scene_buf_free.restype = None
     L.sr_scene_buf_size.argtypes = [vp, vp]
@@ -573,6 +574,13 @@ class ScanlineVGRasterizer:
         d = {k: getattr(s, k) for k, _ in Stats._fields_ if k != "stage_ms"}
         d["stage_ms"] = dict(zip(STAGE_NAMES, [float(x) for x in s.stage_ms]))
         return d
+
+    def sort_tiles(self):
+        """(tiles, tiles sorted with 64-bit items) of the last frame's per-path
+        sort; (0, 0) when it took the radix sort."""
+        t, w = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        _check(lib().sr_debug_sort_tiles(self._ctx, ctypes.byref(t), ctypes.byref(w)))
+        return int(t.value), int(w.value)
 
     def dump(self, stage):
         L = lib()

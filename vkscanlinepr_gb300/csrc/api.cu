@@ -304,6 +304,7 @@ struct Pipeline {
     int64_t last_N = 0, last_O = 0, last_cap = 0, last_dcap = 0;
     uint32_t last_largest = 0;   // records of the frame's largest sort segment
     bool stages_valid = false;
+    bool last_segsort = false;   // the last frame sorted its records per path (segsort.cu)
     // profiling
     cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
     bool ev_pending = false, capturing = false;
@@ -773,7 +774,8 @@ struct Pipeline {
         const KeyLayout L = g.L;
         SortPlan sp = sort_plan(cap, L.pbits + L.rbits + L.xbits, n_dev, tune.sort_items);
         mark(ST_SORT, false);
-        if (segmented() && seg_levels >= 0)
+        last_segsort = segmented() && seg_levels >= 0;
+        if (last_segsort)
             launch_segsort(keys.as<uint64_t>(), skeys.as<uint64_t>(), keys_alt.as<uint64_t>(), cap, C, L, seg_levels,
                            seg_scratch.p, seg_tiles.p, sm_count, status, st);
         else
@@ -1330,6 +1332,20 @@ sr_status sr_debug_dump(sr_ctx* c, int stage, void* dst, size_t* bytes) {
     CUDA_TRY(cudaSetDevice(p.device));
     if (need) CUDA_TRY(cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost));
     *bytes = need;
+    return SR_OK;
+}
+
+sr_status sr_debug_sort_tiles(sr_ctx* c, uint32_t* tiles, uint32_t* wide_tiles) {
+    if (!c || !tiles || !wide_tiles) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    Pipeline& p = c->p;
+    *tiles = *wide_tiles = 0;
+    if (!p.last_segsort || !p.seg_tiles.p || p.C == 0 || p.last_cap <= 0) return SR_OK;
+    CUDA_TRY(cudaSetDevice(p.device));
+    CUDA_TRY(cudaDeviceSynchronize());
+    uint32_t v[2] = {0, 0};
+    CUDA_TRY(sr::segsort_tile_counts(p.seg_tiles.p, p.C, p.last_cap, v));
+    *tiles = v[0];
+    *wide_tiles = v[1];
     return SR_OK;
 }
 

@@ -178,6 +178,9 @@ size_t segsort_tile_bytes(uint32_t n_curves, int64_t cap);
 int segsort_tile();
 void launch_segsort_tables(const uint32_t* curve_path, const int32_t* offs, uint32_t n_curves, uint32_t max_size,
                            void* scratch, uint32_t* status, cudaStream_t st);
+// Tiles of the last segmented sort with these tables, and of those the
+// ones sorted with 64-bit items (synchronous copies).
+cudaError_t segsort_tile_counts(const void* tiles, uint32_t n_curves, int64_t cap, uint32_t out[2]);
 // Device word holding the largest segment of more than half a tile (0 if none).
 const uint32_t* segsort_largest(const void* scratch, uint32_t n_curves);
 // Sorts keys_in[0, N) into keys_out by their key bits (layout L; N from the

@@ -48,12 +48,14 @@ struct TileTables {
     uint4* desc;           // [max_tiles] {start, segment size, k | rounds << 16 | chunk bit, -}
     uint32_t* tile_end;    // [max_tiles] end of a group tile (atomic max over its segments)
     uint32_t* chunks;      // [max_tiles] the chunk tiles (of large segments), in no order
+    uint32_t* fallback;    // [max_tiles] tiles left to the 64-bit tile sort, in no order
     uint64_t* scan_status;
     // [0] scan counter, [1] chunk tiles, [2] next tile of the tile sort,
-    // [3 + l] next work item of merge round l
+    // [3] tiles left to the 64-bit sort, [4] its next, [5 + l] next work
+    // item of merge round l
     uint32_t* ctl;
 };
-constexpr int kCtlChunks = 1, kCtlSortNext = 2, kCtlMergeNext = 3;
+constexpr int kCtlChunks = 1, kCtlSortNext = 2, kCtlFallback = 3, kCtlFallbackNext = 4, kCtlMergeNext = 5;
 
 size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 size_t scan_area(uint32_t C) { return round256(scan_status_words((int64_t)C + 1) * 8); }
@@ -92,6 +94,8 @@ TileTables carve_back(void* base, uint32_t C, int64_t cap) {
     t.tile_end = reinterpret_cast<uint32_t*>(b);
     b += round256(mt * 4);
     t.chunks = reinterpret_cast<uint32_t*>(b);
+    b += round256(mt * 4);
+    t.fallback = reinterpret_cast<uint32_t*>(b);
     b += round256(mt * 4);
     t.scan_status = reinterpret_cast<uint64_t*>(b);
     b += scan_area(C);
@@ -188,15 +192,33 @@ __global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
 }
 
 // ----------------------------------------------------------- local sort ---
-struct LocalSmem {
-    uint64_t buf[2][kTile + 2];   // the tile (its bulk copy may start one key early), and the pass target
-    uint32_t warp_hist[kWarps][kRadix];
-    uint32_t digit_start[kRadix];
-    uint32_t scan_tmp[kWarps];
-    uint32_t red[kWarps][6];
-    uint64_t kred[kWarps][3];
-    uint64_t bar;
+// A tile is sorted by one CTA of a persistent kernel (one wave; tiles come
+// from a counter, so the grid does not follow the table's bound on them).
+//   * The tile reaches shared memory by one bulk copy (TMA) of its 16-byte
+//     aligned span; an odd last key comes by a plain load.
+//   * Within a tile the order is that of a compact item: the fields
+//     (path - pmin, rank - rmin, x - xmin) packed in the fewest bits their
+//     ranges need.  It usually needs 2-3 digit passes where the whole key
+//     needs 4-6, and a digit is one shift of a 32-bit word.
+//   * k_tile_sort32 sorts the tiles whose compact fields and payload fit one
+//     32-bit word: half the shared memory, so more CTAs per SM.  It hands
+//     the others to k_local_sort, whose items are 64-bit (the payload in the
+//     high word, or the raw key when the fields need more than 32 bits).
+//   * A pass ranks the digits per warp (match_any + a per-warp histogram),
+//     scans the counts and scatters into the other buffer (stable: digit,
+//     then warp, then slot).  Rows of slots past the tile's end are skipped.
+
+// Fields of a key: path, row rank, x (payload bits above the key ignored).
+struct KeyFields {
+    uint32_t xb, rb, pb;
+    SR_DEV uint32_t x(uint64_t k) const { return (uint32_t)(k & ((1ull << xb) - 1)); }
+    SR_DEV uint32_t r(uint64_t k) const { return (uint32_t)((k >> xb) & ((1ull << rb) - 1)); }
+    SR_DEV uint32_t p(uint64_t k) const { return (uint32_t)((k >> (xb + rb)) & ((1ull << pb) - 1)); }
+    SR_DEV uint32_t kbits() const { return xb + rb + pb; }
 };
+
+SR_DEV uint32_t bits_of(uint32_t v) { return v ? 32u - (uint32_t)__clz((int)v) : 0u; }
+SR_DEV uint32_t low_mask(uint32_t b) { return b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u; }
 
 SR_DEV uint32_t same_digit_lanes(uint32_t d) {
     if (kMatchAny) return __match_any_sync(0xFFFFFFFFu, d);
@@ -209,43 +231,29 @@ SR_DEV uint32_t same_digit_lanes(uint32_t d) {
     return peers;
 }
 
-// Fields of a key: path, row rank, x (payload bits above the key ignored).
-struct KeyFields {
-    uint32_t xb, rb, pb;
-    SR_DEV uint32_t x(uint64_t k) const { return (uint32_t)(k & ((1ull << xb) - 1)); }
-    SR_DEV uint32_t r(uint64_t k) const { return (uint32_t)((k >> xb) & ((1ull << rb) - 1)); }
-    SR_DEV uint32_t p(uint64_t k) const { return (uint32_t)((k >> (xb + rb)) & ((1ull << pb) - 1)); }
+// Shared memory of the pass machinery and the range reduction.
+struct PassSmem {
+    uint32_t warp_hist[kWarps][kRadix];
+    uint32_t digit_start[kRadix];
+    uint32_t scan_tmp[kWarps];
+    uint32_t red[kWarps][6];
+    uint64_t kred[kWarps][3];
+    uint64_t bar;
+    uint32_t next;
 };
 
-SR_DEV uint32_t bits_of(uint32_t v) { return v ? 32u - (uint32_t)__clz((int)v) : 0u; }
-SR_DEV uint32_t low_mask(uint32_t b) { return b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u; }
-
-// CTA b sorts tile b (a group of small segments, or a chunk of a large one).
-//   * The tile reaches shared memory by one bulk copy (TMA) of its 16-byte
-//     aligned span; an odd last key comes by a plain load.
-//   * Within a tile the order is that of a compact item: the fields
-//     (path - pmin, rank - rmin, x - xmin) packed in the fewest bits their
-//     ranges need, in the low 32 bits, the payload above.  It usually needs
-//     2-3 digit passes where the whole key needs 4-6, and a digit is one
-//     shift of a 32-bit word.  A tile whose fields need more than 32 bits
-//     sorts the bits where its keys differ instead.
-//   * Each pass ranks the digits per warp in registers, scans the counts and
-//     scatters back into the same buffer (every read is done by then).
-//   * The CTAs are persistent (one wave) and take tiles from a counter, so
-//     the grid does not follow the table's bound on the tiles.
-// Returns false when a copy wait gave up (the CTA then leaves).
-SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64_t* __restrict__ keys_in,
-                      uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt, const KeyFields& kf,
-                      uint32_t n_cap, const TileTables& u, uint32_t* status, uint32_t spin_limit) {
-    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+// Tile `tile`'s records [a, a + len) and whether its output goes to
+// keys_alt (a chunk whose segment's merge rounds end in keys_out); false
+// for an empty tile.
+SR_DEV bool tile_span(const TileTables& u, uint32_t tile, uint32_t n_cap, uint32_t& a, uint32_t& len, bool& to_alt) {
     const uint4 d = u.desc[tile];
-    uint32_t a, e;
-    bool to_alt = false;
+    uint32_t e;
+    to_alt = false;
     if (d.z & kChunkBit) {
         const uint32_t k = d.z & 0xFFFFu, rounds = (d.z >> 16) & 0x7FFFu;
         a = d.x + k * (uint32_t)kTile;
         e = min(a + (uint32_t)kTile, d.x + d.y);
-        to_alt = (rounds & 1u) != 0;   // the segment's last merge round lands in keys_out
+        to_alt = (rounds & 1u) != 0;
     } else {
         a = d.x;
         e = u.tile_end[tile];
@@ -253,116 +261,136 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
     // a frame whose records overflowed the buffers is redone: never read past them
     a = min(a, n_cap);
     e = min(max(e, a), n_cap);
-    const uint32_t len = e - a;
-    if (len == 0 || len > (uint32_t)kTile) return true;
-    uint64_t* dst = to_alt ? keys_alt : keys_out;
+    len = e - a;
+    return len > 0 && len <= (uint32_t)kTile;
+}
 
-    // stage the tile: keys [a0, e0) by one bulk copy, key e - 1 by a load when e is odd
-    uint32_t off = 0;
-    if ((reinterpret_cast<uintptr_t>(keys_in) & 15u) == 0) {
-        const uint32_t a0 = a & ~1u, e0 = e & ~1u;
-        const uint32_t nb = e0 - a0;   // e > a >= a0, so e0 >= a0
-        off = a - a0;
-        if (tid == 0) {
-            if (nb) {
-                // the previous tile's reads of the buffer came before (the
-                // caller's barrier); order them before the copy's writes
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(&S.bar, nb * 8u);
-                bulk_load(S.buf[0], keys_in + a0, nb * 8u, &S.bar);
-            }
-            if (e & 1u) S.buf[0][nb] = keys_in[e - 1];
-        }
+// Stages keys [a, a + len) in buf: [a & ~1, e & ~1) by one bulk copy, key
+// e - 1 by a load when e is odd.  Returns the slot of key a (0 or 1), or -1
+// when the copy wait gave up (uniform over the CTA, which then leaves).
+SR_DEV int stage_tile(uint64_t* buf, uint64_t* bar, uint32_t& phase, const uint64_t* __restrict__ keys_in,
+                      uint32_t a, uint32_t len, uint32_t* status, uint32_t spin_limit) {
+    const uint32_t e = a + len;
+    if ((reinterpret_cast<uintptr_t>(keys_in) & 15u) != 0) {
+        for (uint32_t j = threadIdx.x; j < len; j += kThreads) buf[j] = keys_in[a + j];
         __syncthreads();
-        const bool ok = nb == 0 || mbar_wait_bounded(&S.bar, phase, spin_limit, status);
-        if (__syncthreads_or(!ok)) {
-            // gave up: let the copy land before the CTA leaves
-            if (nb) mbar_wait_bounded(&S.bar, phase, spin_limit, nullptr);
-            return false;
+        return 0;
+    }
+    const uint32_t a0 = a & ~1u, e0 = e & ~1u;
+    const uint32_t nb = e0 - a0;   // e > a >= a0, so e0 >= a0
+    if (threadIdx.x == 0) {
+        if (nb) {
+            // the previous tile's reads of the buffer came before (the
+            // caller's barrier); order them before the copy's writes
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bar, nb * 8u);
+            bulk_load(buf, keys_in + a0, nb * 8u, bar);
         }
-        if (nb) phase ^= 1u;
-    } else {
-        for (uint32_t j = tid; j < len; j += kThreads) S.buf[0][j] = keys_in[a + j];
-        __syncthreads();
-    }
-
-    // ranges of the key fields, of the key bits and of the whole key
-    const uint32_t kbits = kf.xb + kf.rb + kf.pb;
-    const uint64_t kmask = (1ull << kbits) - 1ull;
-    uint32_t pmin = ~0u, pmax = 0, rmin = ~0u, rmax = 0, xmin = ~0u, xmax = 0;
-    uint64_t lo = ~0ull, hi = 0, top = 0;
-    for (uint32_t j = tid; j < len; j += kThreads) {
-        {
-            const uint64_t k = S.buf[0][off + j];
-            const uint32_t p = kf.p(k), r = kf.r(k), x = kf.x(k);
-            pmin = min(pmin, p); pmax = max(pmax, p);
-            rmin = min(rmin, r); rmax = max(rmax, r);
-            xmin = min(xmin, x); xmax = max(xmax, x);
-            lo = min(lo, k & kmask);
-            hi = max(hi, k & kmask);
-            top = max(top, k);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        pmin = min(pmin, __shfl_xor_sync(0xFFFFFFFFu, pmin, o));
-        pmax = max(pmax, __shfl_xor_sync(0xFFFFFFFFu, pmax, o));
-        rmin = min(rmin, __shfl_xor_sync(0xFFFFFFFFu, rmin, o));
-        rmax = max(rmax, __shfl_xor_sync(0xFFFFFFFFu, rmax, o));
-        xmin = min(xmin, __shfl_xor_sync(0xFFFFFFFFu, xmin, o));
-        xmax = max(xmax, __shfl_xor_sync(0xFFFFFFFFu, xmax, o));
-        lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
-        top = max(top, __shfl_xor_sync(0xFFFFFFFFu, top, o));
-    }
-    if (lane == 0) {
-        S.red[warp][0] = pmin; S.red[warp][1] = pmax;
-        S.red[warp][2] = rmin; S.red[warp][3] = rmax;
-        S.red[warp][4] = xmin; S.red[warp][5] = xmax;
-        S.kred[warp][0] = lo; S.kred[warp][1] = hi; S.kred[warp][2] = top;
+        if (e & 1u) buf[nb] = keys_in[e - 1];
     }
     __syncthreads();
+    const bool ok = nb == 0 || mbar_wait_bounded(bar, phase, spin_limit, status);
+    if (__syncthreads_or(!ok)) {
+        // gave up: let the copy land before the CTA leaves
+        if (nb) mbar_wait_bounded(bar, phase, spin_limit, nullptr);
+        return -1;
+    }
+    if (nb) phase ^= 1u;
+    return (int)(a - a0);
+}
+
+// Field ranges of a tile, reduced over the CTA (every thread gets them).
+struct Ranges {
+    uint32_t pmin, pmax, rmin, rmax, xmin, xmax;
+    uint64_t lo, hi, top;   // key bits' min and max, whole key's max
+    SR_DEV void init() {
+        pmin = rmin = xmin = ~0u;
+        pmax = rmax = xmax = 0;
+        lo = ~0ull;
+        hi = top = 0;
+    }
+    SR_DEV void add(const KeyFields& kf, uint64_t k, uint64_t kmask) {
+        const uint32_t p = kf.p(k), r = kf.r(k), x = kf.x(k);
+        pmin = min(pmin, p); pmax = max(pmax, p);
+        rmin = min(rmin, r); rmax = max(rmax, r);
+        xmin = min(xmin, x); xmax = max(xmax, x);
+        lo = min(lo, k & kmask);
+        hi = max(hi, k & kmask);
+        top = max(top, k);
+    }
+    SR_DEV void reduce(PassSmem& S) {
+        const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-        pmin = min(pmin, S.red[w][0]); pmax = max(pmax, S.red[w][1]);
-        rmin = min(rmin, S.red[w][2]); rmax = max(rmax, S.red[w][3]);
-        xmin = min(xmin, S.red[w][4]); xmax = max(xmax, S.red[w][5]);
-        lo = min(lo, S.kred[w][0]); hi = max(hi, S.kred[w][1]); top = max(top, S.kred[w][2]);
-    }
-    const uint32_t bp = bits_of(pmax - pmin), br = bits_of(rmax - rmin), bx = bits_of(xmax - xmin);
-    // compact items when the fields fit 32 bits and the payload the other 32
-    const bool compact = bp + br + bx <= 32u && (top >> kbits) <= 0xFFFFFFFFull;
-    const uint32_t bits = compact ? bp + br + bx : (lo == hi ? 0u : 64u - (uint32_t)__clzll((long long)(lo ^ hi)));
-    const uint32_t passes = (bits + kRadixBits - 1) / kRadixBits;
-    auto to_item = [&](uint64_t k) -> uint64_t {
-        const uint64_t c = ((uint64_t)(kf.p(k) - pmin) << (br + bx)) | ((uint64_t)(kf.r(k) - rmin) << bx) |
-                           (uint64_t)(kf.x(k) - xmin);
-        return ((k >> kbits) << 32) | c;
-    };
-    auto digit = [&](uint64_t v, uint32_t shift) -> uint32_t {
-        if (compact) return ((uint32_t)v >> shift) & (kRadix - 1);
-        return (uint32_t)((v & kmask) >> shift) & (kRadix - 1);
-    };
-    // the items from slot 0 of the other buffer (staged keys sit at off)
-    uint32_t cur = 0, src = off;
-    if (passes > 0 && (compact || off)) {
-        for (uint32_t j = tid; j < len; j += kThreads) {
-            const uint64_t k = S.buf[0][off + j];
-            S.buf[1][j] = compact ? to_item(k) : k;
+        for (int o = 16; o; o >>= 1) {
+            pmin = min(pmin, __shfl_xor_sync(0xFFFFFFFFu, pmin, o));
+            pmax = max(pmax, __shfl_xor_sync(0xFFFFFFFFu, pmax, o));
+            rmin = min(rmin, __shfl_xor_sync(0xFFFFFFFFu, rmin, o));
+            rmax = max(rmax, __shfl_xor_sync(0xFFFFFFFFu, rmax, o));
+            xmin = min(xmin, __shfl_xor_sync(0xFFFFFFFFu, xmin, o));
+            xmax = max(xmax, __shfl_xor_sync(0xFFFFFFFFu, xmax, o));
+            lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+            top = max(top, __shfl_xor_sync(0xFFFFFFFFu, top, o));
         }
-        cur = 1;
-        src = 0;
+        if (lane == 0) {
+            S.red[warp][0] = pmin; S.red[warp][1] = pmax;
+            S.red[warp][2] = rmin; S.red[warp][3] = rmax;
+            S.red[warp][4] = xmin; S.red[warp][5] = xmax;
+            S.kred[warp][0] = lo; S.kred[warp][1] = hi; S.kred[warp][2] = top;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            pmin = min(pmin, S.red[w][0]); pmax = max(pmax, S.red[w][1]);
+            rmin = min(rmin, S.red[w][2]); rmax = max(rmax, S.red[w][3]);
+            xmin = min(xmin, S.red[w][4]); xmax = max(xmax, S.red[w][5]);
+            lo = min(lo, S.kred[w][0]); hi = max(hi, S.kred[w][1]); top = max(top, S.kred[w][2]);
+        }
     }
+};
+
+// The minima of the fields and their widths, read back from the
+// reduction's shared words (fewer live registers through the passes).
+struct Unpack {
+    uint32_t pmin, rmin, xmin, rb, xb;
+    SR_DEV void load(const PassSmem& S) {
+        uint32_t r1 = S.red[0][3], x1 = S.red[0][5];
+        pmin = S.red[0][0];
+        rmin = S.red[0][2];
+        xmin = S.red[0][4];
+#pragma unroll
+        for (int w = 1; w < kWarps; ++w) {
+            pmin = min(pmin, S.red[w][0]);
+            rmin = min(rmin, S.red[w][2]); r1 = max(r1, S.red[w][3]);
+            xmin = min(xmin, S.red[w][4]); x1 = max(x1, S.red[w][5]);
+        }
+        rb = bits_of(r1 - rmin);
+        xb = bits_of(x1 - xmin);
+    }
+    // the key of compact fields c
+    SR_DEV uint64_t key(const KeyFields& kf, uint32_t c) const {
+        const uint32_t x = xmin + (c & low_mask(xb));
+        const uint32_t r = rmin + (uint32_t)(((uint64_t)c >> xb) & low_mask(rb));
+        const uint32_t p = pmin + (uint32_t)((uint64_t)c >> (rb + xb));
+        return ((uint64_t)p << (kf.xb + kf.rb)) | ((uint64_t)r << kf.xb) | (uint64_t)x;
+    }
+};
+
+// `passes` digit passes over items buf[cur][0, len), each into the other
+// buffer; returns the buffer holding the result.  digit(item, shift).
+template <typename T, typename Digit>
+SR_DEV uint32_t radix_passes(PassSmem& S, T* buf0, T* buf1, uint32_t cur, uint32_t len, uint32_t passes,
+                             Digit digit) {
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    const uint32_t wfirst = warp * (32u * kItems);
+    const uint32_t rows = wfirst >= len ? 0u : min((uint32_t)kItems, (len - wfirst + 31u) / 32u);
     for (uint32_t pass = 0; pass < passes; ++pass) {
         const uint32_t shift = pass * kRadixBits;
-        const uint64_t* in = S.buf[cur] + src;
+        const T* in = cur ? buf1 : buf0;
+        T* out = cur ? buf0 : buf1;
         for (int i = tid; i < kWarps * kRadix; i += kThreads) (&S.warp_hist[0][0])[i] = 0;
         __syncthreads();
-        // rank within the warp: warp w holds slots [w*512, w*512 + 512); rows
-        // of slots past the tile's end are skipped whole (a tile is about
-        // half full on average)
-        const uint32_t wfirst = warp * (32u * kItems);
-        const uint32_t rows = wfirst >= len ? 0u : min((uint32_t)kItems, (len - wfirst + 31u) / 32u);
+        // rank within the warp: warp w holds slots [w*512, w*512 + 512)
         uint32_t rd[kItems];   // rank | digit << 16
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
@@ -412,8 +440,6 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         __syncthreads();
         S.digit_start[dd] = S.scan_tmp[warp] + x - cnt;
         __syncthreads();
-        // scatter into the other buffer (stable: digit, then warp, then slot)
-        uint64_t* out = S.buf[cur ^ 1u];
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
             if ((uint32_t)it >= rows) break;
@@ -423,29 +449,173 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
         }
         __syncthreads();
         cur ^= 1u;
+    }
+    return cur;
+}
+
+// ---- 32-bit items
+struct Sort32Smem {
+    union {
+        uint64_t keys[kTile + 2];        // the staged tile
+        uint32_t items[2][kTile + 4];    // the passes' buffers, once the keys are read
+    };
+    PassSmem ps;
+};
+
+// Sorts tile `tile` with 32-bit items (payload above the compact fields), or
+// hands it to the 64-bit kernel (queued in u.fallback).  False when a copy
+// wait gave up.
+SR_DEV bool sort_tile32(Sort32Smem& S, uint32_t tile, uint32_t& phase, const uint64_t* __restrict__ keys_in,
+                        uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt, const KeyFields& kf,
+                        uint32_t n_cap, const TileTables& u, uint32_t* status, uint32_t spin_limit) {
+    const uint32_t tid = threadIdx.x;
+    uint32_t a, len;
+    bool to_alt;
+    if (!tile_span(u, tile, n_cap, a, len, to_alt)) return true;
+    uint64_t* dst = to_alt ? keys_alt : keys_out;
+    const int off = stage_tile(S.keys, &S.ps.bar, phase, keys_in, a, len, status, spin_limit);
+    if (off < 0) return false;
+
+    // the tile's ranges
+    const uint32_t kbits = kf.kbits();
+    const uint64_t kmask = (1ull << kbits) - 1ull;
+    const uint32_t base = (uint32_t)off;
+    Ranges R;
+    R.init();
+    for (uint32_t j = tid; j < len; j += kThreads) R.add(kf, S.keys[base + j], kmask);
+    R.reduce(S.ps);
+    const uint32_t bp = bits_of(R.pmax - R.pmin), br = bits_of(R.rmax - R.rmin), bx = bits_of(R.xmax - R.xmin);
+    const uint32_t bits = bp + br + bx;
+    const uint64_t pay_max = R.top >> kbits;
+    const uint32_t payb = pay_max > 0xFFFFFFFFull ? 33u : bits_of((uint32_t)pay_max);
+    if (bits + payb > 32u) {
+        if (tid == 0) u.fallback[atomicAdd(&u.ctl[kCtlFallback], 1u)] = tile;
+        return true;
+    }
+    if (bits == 0) {   // one key: already in order
+        for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.keys[base + j];
+        return true;
+    }
+    // the items (payload above the fields; a field shifts only when it is
+    // not empty, so no shift reaches 32), through registers: they overwrite
+    // the staged keys
+    uint32_t iv[kItems];
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        if ((uint32_t)i * kThreads >= len) break;
+        const uint32_t j = tid + (uint32_t)i * kThreads;
+        if (j < len) {
+            const uint64_t k = S.keys[base + j];
+            const uint32_t pc = bp ? (kf.p(k) - R.pmin) << (br + bx) : 0u;
+            const uint32_t rc = br ? (kf.r(k) - R.rmin) << bx : 0u;
+            iv[i] = (bits < 32u ? (uint32_t)(k >> kbits) << bits : 0u) | pc | rc | (kf.x(k) - R.xmin);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        if ((uint32_t)i * kThreads >= len) break;
+        const uint32_t j = tid + (uint32_t)i * kThreads;
+        if (j < len) S.items[0][j] = iv[i];
+    }
+    const uint32_t cmask = low_mask(bits);
+    const uint32_t passes = (bits + kRadixBits - 1) / kRadixBits;
+    const uint32_t cur = radix_passes<uint32_t>(S.ps, S.items[0], S.items[1], 0u, len, passes,
+                                                [cmask](uint32_t v, uint32_t shift) -> uint32_t {
+                                                    return ((v & cmask) >> shift) & (kRadix - 1);
+                                                });
+    Unpack U;
+    U.load(S.ps);
+    for (uint32_t j = tid; j < len; j += kThreads) {
+        const uint32_t v = S.items[cur][j];
+        const uint64_t pay = bits < 32u ? (uint64_t)(v >> bits) : 0ull;
+        dst[a + j] = (pay << kbits) | U.key(kf, v & cmask);
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_tile_sort32(const uint64_t* __restrict__ keys_in,
+                                                             uint64_t* __restrict__ keys_out,
+                                                             uint64_t* __restrict__ keys_alt, uint32_t C,
+                                                             KeyFields kf, uint32_t n_cap, uint32_t mt,
+                                                             TileTables u, uint32_t* status, uint32_t spin_limit) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Sort32Smem& S = *reinterpret_cast<Sort32Smem*>(smem_raw);
+    // tiles past the table exist only in a frame whose records overflowed (redone)
+    const uint32_t n_tiles = min((uint32_t)u.ntiles[C], mt);
+    if (threadIdx.x == 0) mbar_init(&S.ps.bar, 1);
+    uint32_t phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) S.ps.next = atomicAdd(&u.ctl[kCtlSortNext], 1u);
+        __syncthreads();   // also: the previous tile is done with the buffers
+        const uint32_t tile = S.ps.next;
+        __syncthreads();
+        if (tile >= n_tiles) break;
+        if (!sort_tile32(S, tile, phase, keys_in, keys_out, keys_alt, kf, n_cap, u, status, spin_limit)) return;
+    }
+}
+
+// ---- 64-bit items (the tiles k_tile_sort32 handed over)
+struct LocalSmem {
+    uint64_t buf[2][kTile + 2];   // the staged tile, and the passes' second buffer
+    PassSmem ps;
+};
+
+SR_DEV bool sort_tile64(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64_t* __restrict__ keys_in,
+                        uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt, const KeyFields& kf,
+                        uint32_t n_cap, const TileTables& u, uint32_t* status, uint32_t spin_limit) {
+    const uint32_t tid = threadIdx.x;
+    uint32_t a, len;
+    bool to_alt;
+    if (!tile_span(u, tile, n_cap, a, len, to_alt)) return true;
+    uint64_t* dst = to_alt ? keys_alt : keys_out;
+    const int soff = stage_tile(S.buf[0], &S.ps.bar, phase, keys_in, a, len, status, spin_limit);
+    if (soff < 0) return false;
+    const uint32_t off = (uint32_t)soff;
+
+    const uint32_t kbits = kf.kbits();
+    const uint64_t kmask = (1ull << kbits) - 1ull;
+    Ranges R;
+    R.init();
+    for (uint32_t j = tid; j < len; j += kThreads) R.add(kf, S.buf[0][off + j], kmask);
+    R.reduce(S.ps);
+    const uint32_t bp = bits_of(R.pmax - R.pmin), br = bits_of(R.rmax - R.rmin), bx = bits_of(R.xmax - R.xmin);
+    // compact items when the fields fit 32 bits and the payload the other 32
+    const bool compact = bp + br + bx <= 32u && (R.top >> kbits) <= 0xFFFFFFFFull;
+    const uint32_t bits =
+        compact ? bp + br + bx : (R.lo == R.hi ? 0u : 64u - (uint32_t)__clzll((long long)(R.lo ^ R.hi)));
+    const uint32_t passes = (bits + kRadixBits - 1) / kRadixBits;
+    // the items from slot 0 of the other buffer (the staged keys sit at off)
+    uint32_t cur = 0, src = off;
+    if (passes > 0 && (compact || off)) {
+        for (uint32_t j = tid; j < len; j += kThreads) {
+            const uint64_t k = S.buf[0][off + j];
+            const uint64_t c = ((uint64_t)(kf.p(k) - R.pmin) << (br + bx)) |
+                               ((uint64_t)(kf.r(k) - R.rmin) << bx) | (uint64_t)(kf.x(k) - R.xmin);
+            S.buf[1][j] = compact ? ((k >> kbits) << 32) | c : k;
+        }
+        cur = 1;
         src = 0;
     }
+    if (passes > 0) {
+        if (compact)
+            cur = radix_passes<uint64_t>(S.ps, S.buf[0], S.buf[1], cur, len, passes,
+                                         [](uint64_t v, uint32_t shift) -> uint32_t {
+                                             return ((uint32_t)v >> shift) & (kRadix - 1);
+                                         });
+        else
+            cur = radix_passes<uint64_t>(S.ps, S.buf[0], S.buf[1], cur, len, passes,
+                                         [kmask](uint64_t v, uint32_t shift) -> uint32_t {
+                                             return (uint32_t)((v & kmask) >> shift) & (kRadix - 1);
+                                         });
+    }
     if (compact && passes > 0) {
-        // the fields' minima again from shared memory (fewer live registers
-        // through the passes)
-        uint32_t p0 = S.red[0][0], r0 = S.red[0][2], x0 = S.red[0][4];
-        uint32_t p1 = S.red[0][1], r1 = S.red[0][3], x1 = S.red[0][5];
-#pragma unroll
-        for (int w = 1; w < kWarps; ++w) {
-            p0 = min(p0, S.red[w][0]); r0 = min(r0, S.red[w][2]); x0 = min(x0, S.red[w][4]);
-            p1 = max(p1, S.red[w][1]); r1 = max(r1, S.red[w][3]); x1 = max(x1, S.red[w][5]);
-        }
-        const uint32_t rb = bits_of(r1 - r0), xb = bits_of(x1 - x0);
-        const uint32_t kb = kf.xb + kf.rb + kf.pb;
+        Unpack U;
+        U.load(S.ps);
         for (uint32_t j = tid; j < len; j += kThreads) {
             const uint64_t v = S.buf[cur][j];
-            const uint32_t c = (uint32_t)v;
-            const uint32_t x = x0 + (c & low_mask(xb));
-            const uint32_t r = r0 + (uint32_t)(((uint64_t)c >> xb) & low_mask(rb));
-            const uint32_t p = p0 + (uint32_t)((uint64_t)c >> (rb + xb));
-            dst[a + j] = ((v >> 32) << kb) | ((uint64_t)p << (kf.xb + kf.rb)) | ((uint64_t)r << kf.xb) | (uint64_t)x;
+            dst[a + j] = ((v >> 32) << kbits) | U.key(kf, (uint32_t)v);
         }
-        (void)p1;
     } else {
         for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[cur][src + j];
     }
@@ -454,23 +624,22 @@ SR_DEV bool sort_tile(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64
 
 __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __restrict__ keys_in,
                                                             uint64_t* __restrict__ keys_out,
-                                                            uint64_t* __restrict__ keys_alt, uint32_t C,
-                                                            KeyFields kf, uint32_t n_cap, uint32_t mt,
-                                                            TileTables u, uint32_t* status, uint32_t spin_limit) {
+                                                            uint64_t* __restrict__ keys_alt, KeyFields kf,
+                                                            uint32_t n_cap, TileTables u, uint32_t* status,
+                                                            uint32_t spin_limit) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LocalSmem& S = *reinterpret_cast<LocalSmem*>(smem_raw);
-    __shared__ uint32_t next;
-    // tiles past the table exist only in a frame whose records overflowed (redone)
-    const uint32_t n_tiles = min((uint32_t)u.ntiles[C], mt);
-    if (threadIdx.x == 0) mbar_init(&S.bar, 1);
+    const uint32_t n_tiles = u.ctl[kCtlFallback];
+    if (threadIdx.x == 0) mbar_init(&S.ps.bar, 1);
     uint32_t phase = 0;
     for (;;) {
-        if (threadIdx.x == 0) next = atomicAdd(&u.ctl[kCtlSortNext], 1u);
+        if (threadIdx.x == 0) S.ps.next = atomicAdd(&u.ctl[kCtlFallbackNext], 1u);
         __syncthreads();   // also: the previous tile is done with the buffers
-        const uint32_t tile = next;
+        const uint32_t i = S.ps.next;
         __syncthreads();
-        if (tile >= n_tiles) break;
-        if (!sort_tile(S, tile, phase, keys_in, keys_out, keys_alt, kf, n_cap, u, status, spin_limit)) return;
+        if (i >= n_tiles) break;
+        if (!sort_tile64(S, u.fallback[i], phase, keys_in, keys_out, keys_alt, kf, n_cap, u, status, spin_limit))
+            return;
     }
 }
 
@@ -597,7 +766,7 @@ size_t segsort_scratch_bytes(uint32_t C) { return 2 * round256(((size_t)C + 2) *
 
 size_t segsort_tile_bytes(uint32_t C, int64_t cap) {
     const size_t mt = max_tiles(C, cap);
-    return round256(((size_t)C + 2) * 4) + round256(mt * 16) + 2 * round256(mt * 4) + scan_area(C) + 256;
+    return round256(((size_t)C + 2) * 4) + round256(mt * 16) + 3 * round256(mt * 4) + scan_area(C) + 256;
 }
 
 int segsort_tile() { return kTile; }
@@ -614,6 +783,14 @@ void launch_segsort_tables(const uint32_t* curve_path, const int32_t* offs, uint
     launch_exclusive_scan_i32(t.flag, t.flag, C + 1, t.scan_status, t.ctl + 0, status, st);
     k_seg_starts<<<g, 256, 0, st>>>(offs, C, t);
     k_seg_largest<<<g, 256, 0, st>>>(C, max_size, t, status);
+}
+
+cudaError_t segsort_tile_counts(const void* tiles, uint32_t C, int64_t cap, uint32_t out[2]) {
+    TileTables u = carve_back(const_cast<void*>(tiles), C, cap);
+    cudaError_t e = cudaMemcpy(&out[0], u.ntiles + C, 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&out[1], u.ctl + kCtlFallback, 4, cudaMemcpyDeviceToHost);
+    out[0] = std::min<uint32_t>(out[0], (uint32_t)max_tiles(C, cap));
+    return e;
 }
 
 const uint32_t* segsort_largest(const void* scratch, uint32_t C) {
@@ -640,23 +817,29 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     // resident CTAs per SM of the two persistent kernels (same on every
     // device of the build's architecture)
     static std::atomic<uint32_t> attr{0};
-    static std::atomic<int> occ_sort{0}, occ_merge{0};
+    static std::atomic<int> occ_sort32{0}, occ_sort{0}, occ_merge{0};
     once_per_device(attr, [] {
+        cudaFuncSetAttribute(k_tile_sort32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sort32Smem));
         cudaFuncSetAttribute(k_local_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LocalSmem));
         cudaFuncSetAttribute(k_merge_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
-        int a = 0, b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_local_sort, kThreads, sizeof(LocalSmem));
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_merge_level, kThreads, sizeof(MergeSmem));
-        occ_sort.store(std::max(a, 1));
-        occ_merge.store(std::max(b, 1));
+        int a = 0, b = 0, c = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_tile_sort32, kThreads, sizeof(Sort32Smem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_local_sort, kThreads, sizeof(LocalSmem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_merge_level, kThreads, sizeof(MergeSmem));
+        occ_sort32.store(std::max(a, 1));
+        occ_sort.store(std::max(b, 1));
+        occ_merge.store(std::max(c, 1));
     });
-    const int sms = std::max(sm_count, 1);
-    const unsigned g_sort = (unsigned)std::min<size_t>(mt, (size_t)sms * (size_t)std::max(occ_sort.load(), 1));
-    const unsigned g_merge = (unsigned)std::min<size_t>(2 * mt, (size_t)sms * (size_t)std::max(occ_merge.load(), 1));
-    count_launches(1 + (uint32_t)levels);
+    const size_t sms = (size_t)std::max(sm_count, 1);
+    const unsigned g_sort32 = (unsigned)std::min<size_t>(mt, sms * (size_t)std::max(occ_sort32.load(), 1));
+    const unsigned g_sort = (unsigned)std::min<size_t>(mt, sms * (size_t)std::max(occ_sort.load(), 1));
+    const unsigned g_merge = (unsigned)std::min<size_t>(2 * mt, sms * (size_t)std::max(occ_merge.load(), 1));
+    count_launches(2 + (uint32_t)levels);
     const uint32_t n_cap = (uint32_t)cap;
-    k_local_sort<<<g_sort, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap,
-                                                              (uint32_t)mt, u, status, spin_limit());
+    k_tile_sort32<<<g_sort32, kThreads, sizeof(Sort32Smem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap,
+                                                                  (uint32_t)mt, u, status, spin_limit());
+    k_local_sort<<<g_sort, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, kf, n_cap, u, status,
+                                                              spin_limit());
     for (int lv = 0; lv < levels; ++lv)
         k_merge_level<<<g_merge, kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, (uint32_t)lv, key_bits, n_cap,
                                                                     u);
