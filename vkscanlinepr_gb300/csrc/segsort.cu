@@ -630,6 +630,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __re
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LocalSmem& S = *reinterpret_cast<LocalSmem*>(smem_raw);
     const uint32_t n_tiles = u.ctl[kCtlFallback];
+    if (n_tiles == 0) return;   // the usual case: nothing handed over
     if (threadIdx.x == 0) mbar_init(&S.ps.bar, 1);
     uint32_t phase = 0;
     for (;;) {
@@ -832,7 +833,9 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     });
     const size_t sms = (size_t)std::max(sm_count, 1);
     const unsigned g_sort32 = (unsigned)std::min<size_t>(mt, sms * (size_t)std::max(occ_sort32.load(), 1));
-    const unsigned g_sort = (unsigned)std::min<size_t>(mt, sms * (size_t)std::max(occ_sort.load(), 1));
+    // the 64-bit sort takes the few tiles the 32-bit one hands over
+    const unsigned g_sort = (unsigned)std::min<size_t>(mt, sms);
+    (void)occ_sort;
     const unsigned g_merge = (unsigned)std::min<size_t>(2 * mt, sms * (size_t)std::max(occ_merge.load(), 1));
     count_launches(2 + (uint32_t)levels);
     const uint32_t n_cap = (uint32_t)cap;
