@@ -531,12 +531,11 @@ def run_serving(sr, args, sz, margins):
     for name, sizer, slots in (("learned", sz, 2), ("exact", None, 1)):
         srv = sr.RenderServer(sizer=sizer, slots=slots, max_batch_scenes=args.serve_batch, memory_budget=120e9,
                               margins=margins)
-        # untimed warm-up: a burst, then a stream of the same rate, so that
-        # every slot's buffers have grown to the batches a stream forms (a
-        # slot's first batch larger than any before reallocates its buffers,
-        # and a device-wide wait of the free stalls the scheduler)
+        # untimed warm-up: a burst, then a stream of the same rate with
+        # images fetched as in the timed run, so that every slot's buffers
+        # have grown to the batches a stream forms and the fetch path has run
         _serve(sr, srv, pool[:64], [None] * 64)
-        _serve(sr, srv, pool[64:64 + warm_n], warm)
+        _serve(sr, srv, pool[64:64 + warm_n], warm, check_every=32)
         t, imgs = _serve(sr, srv, pool, arrivals,
                          check_every=max(1, n // ORACLE_SAMPLE) if name == "learned" else 0)
         res = _lat_summary(t[:, 0], t[:, 1])

@@ -520,6 +520,13 @@ sr_status sr_batch_frame_bytes(sr_batch* b, int64_t records, int64_t draws, uint
 sr_status sr_batch_release(sr_batch* b);
 /* Device bytes the batch holds now. */
 sr_status sr_batch_held_bytes(const sr_batch* b, uint64_t* bytes);
+/* Grows b's device buffers to at least the sizes model's hold (no frame of
+ * b in flight).  A batch whose frame outgrows its buffers reallocates them
+ * before it starts, behind a device-wide wait; a server grows its idle
+ * slots like its largest one so that this happens once, not per slot.
+ * When a buffer moves, b's images and plan are dropped and its next frame
+ * uploads its scenes again. */
+sr_status sr_batch_reserve_like(sr_batch* b, const sr_batch* model);
 
 /* ------------------------------------------------------------------ */
 /* Continuous-batching render server (no reference counterpart).       */

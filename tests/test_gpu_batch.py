@@ -122,3 +122,29 @@ def test_autotune_caches_its_choice(gpu, tmp_path):
     assert b2.autotune(path) == t1
     b.close()
     b2.close()
+
+
+def test_reserve_like_grows_buffers_and_keeps_images(gpu, oracle_lib):
+    # a small batch grown like a large one renders the same images; its
+    # scenes are uploaded again after its buffers moved
+    big = gpu.SceneBatch(mode=1)
+    big.add_synth(2, 7, 24)
+    big.render()
+    scs = [oracle_lib.synth(2, 8, scene_index=i) for i in range(2)]
+    want = _oracle_images(oracle_lib, scs, 1)
+    small = gpu.SceneBatch(mode=1)
+    for s in scs:
+        small.add_scene(_container(gpu, s))
+    small.render()
+    assert all(np.array_equal(small.image(i), w) for i, w in enumerate(want))
+    before = small.held_bytes()
+    small.reserve_like(big)
+    assert small.held_bytes() >= big.held_bytes() > before
+    small.reserve_like(big)   # nothing moves the second time
+    small.render()
+    assert all(np.array_equal(small.image(i), w) for i, w in enumerate(want))
+    n = small.stats()["n_intersections"]
+    small.render(capacity=n, graph=True)   # a captured frame on the grown buffers
+    assert all(np.array_equal(small.image(i), w) for i, w in enumerate(want))
+    big.close()
+    small.close()

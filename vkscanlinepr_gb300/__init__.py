@@ -181,7 +181,7 @@ EXPORTS = ["sr_create", "sr_load_scene", "sr_set_mvp", "sr_render", "sr_get_stat
            "sr_admission_take", "sr_set_tuning", "sr_batch_set_tuning", "sr_batch_get_tuning",
            "sr_batch_tuning_class", "sr_batch_autotune", "sr_scan_status", "sr_set_spin_limit",
            "sr_debug_scan_without_first_tile", "sr_write_image", "sr_rvg_load_full", "sr_set_paints",
-           "sr_scene_buf_paints", "sr_render_aa", "sr_debug_sort_tiles"]
+           "sr_scene_buf_paints", "sr_render_aa", "sr_debug_sort_tiles", "sr_batch_reserve_like"]
 
 _lib = None
 
@@ -284,6 +284,7 @@ def lib():
     L.sr_batch_frame_bytes.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
     L.sr_batch_release.argtypes = [vp]
     L.sr_batch_held_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+    L.sr_batch_reserve_like.argtypes = [vp, vp]
     L.sr_device_alloc.argtypes = [ctypes.c_int, ctypes.c_size_t]
     L.sr_device_alloc.restype = vp
     L.sr_device_free.argtypes = [vp]
@@ -745,6 +746,11 @@ class SceneBatch:
         b = ctypes.c_uint64()
         _check(lib().sr_batch_held_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+    def reserve_like(self, model):
+        """Grows this batch's buffers to at least model's (images and plan
+        dropped when a buffer moves; the next frame uploads the scenes)."""
+        _check(lib().sr_batch_reserve_like(self._h, model._h))
 
     def frame_bytes(self, records, draws=-1):
         b = ctypes.c_uint64()

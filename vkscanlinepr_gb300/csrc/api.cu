@@ -67,14 +67,15 @@ struct DevBuf {
     template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
-cudaError_t ensure(DevBuf& b, size_t bytes) {
+// Grows b to hold `bytes`, with `slack` (a quarter by default) to spare.
+cudaError_t ensure(DevBuf& b, size_t bytes, bool slack = true) {
     if (bytes <= b.cap && b.p) return cudaSuccess;
     if (b.p) {
         cudaFree(b.p);
         b.p = nullptr;
         b.cap = 0;
     }
-    size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    size_t want = std::max<size_t>(slack ? bytes + bytes / 4 : bytes, 256);
     want = (want + 255) & ~(size_t)255;
     cudaError_t e = cudaMalloc(&b.p, want);
     if (e != cudaSuccess) {
@@ -143,7 +144,13 @@ struct HostScenes {
     std::vector<uint32_t> pos_path, curve_pos, curve_type, curve_path, fill_rule, fill_info, path_scene;
     std::vector<sr::SceneInfo> info;
 
-    void clear() { *this = HostScenes(); }
+    // keeps the vectors' storage: a batch re-formed for every frame (the
+    // server's) reuses host pages that are already mapped
+    void clear() {
+        pos.clear();
+        for (auto* v : {&pos_path, &curve_pos, &curve_type, &curve_path, &fill_rule, &fill_info, &path_scene}) v->clear();
+        info.clear();
+    }
     uint32_t n_points() const { return (uint32_t)pos_path.size(); }
     uint32_t n_curves() const { return (uint32_t)curve_type.size(); }
     uint32_t n_paths() const { return (uint32_t)fill_rule.size(); }
@@ -296,6 +303,18 @@ struct Pipeline {
     bool path_first_valid = false, count_paths = false, planned = false;
     unsigned long long* h_plan_ptr = nullptr;   // pinned plan totals
     size_t h_plan_words = 0;
+    // Host-to-device uploads of scenes and tables go through one pinned
+    // staging buffer on a stream of their own: a copy from pageable memory
+    // runs at a fraction of DMA speed and, on first use of fresh host pages,
+    // took tens of milliseconds on the Grace host.
+    unsigned char* h_stage = nullptr;
+    size_t h_stage_cap = 0, h_stage_used = 0;
+    cudaStream_t up_stream = nullptr;
+    struct StagedCopy {
+        void* dst;
+        size_t off, bytes;
+    };
+    std::vector<StagedCopy> staged;
     // host scalars (pinned): N, status; fragments, spans
     uint32_t* h_u32 = nullptr;
     uint64_t* h_u64 = nullptr;
@@ -332,7 +351,39 @@ struct Pipeline {
         if (h_u32) cudaFreeHost(h_u32);
         if (h_u64) cudaFreeHost(h_u64);
         if (h_plan_ptr) cudaFreeHost(h_plan_ptr);
+        if (h_stage) cudaFreeHost(h_stage);
+        if (up_stream) cudaStreamDestroy(up_stream);
     }
+
+    // Grows the pinned staging buffer to `bytes` (nothing staged).
+    sr_status stage_reserve(size_t bytes) {
+        if (bytes <= h_stage_cap) return SR_OK;
+        if (h_stage) cudaFreeHost(h_stage);
+        h_stage = nullptr;
+        h_stage_cap = 0;
+        const size_t want = std::max<size_t>(bytes + bytes / 2, 1 << 16);
+        CUDA_TRY(cudaMallocHost(&h_stage, want));
+        h_stage_cap = want;
+        return SR_OK;
+    }
+    // Queues a copy of src into dst through the staging buffer (room was
+    // reserved by the caller); stage_flush issues and waits for them.
+    void stage(void* dst, const void* src, size_t bytes) {
+        if (!bytes) return;
+        std::memcpy(h_stage + h_stage_used, src, bytes);
+        staged.push_back({dst, h_stage_used, bytes});
+        h_stage_used += (bytes + 255) & ~(size_t)255;
+    }
+    sr_status stage_flush() {
+        if (!up_stream) CUDA_TRY(cudaStreamCreateWithFlags(&up_stream, cudaStreamNonBlocking));
+        for (const StagedCopy& c : staged)
+            CUDA_TRY(cudaMemcpyAsync(c.dst, h_stage + c.off, c.bytes, cudaMemcpyHostToDevice, up_stream));
+        staged.clear();
+        h_stage_used = 0;
+        CUDA_TRY(cudaStreamSynchronize(up_stream));
+        return SR_OK;
+    }
+    static size_t staged_size(size_t bytes) { return (bytes + 255) & ~(size_t)255; }
 
     sr_status init(int dev, int32_t m, uint32_t fl) {
         device = dev;
@@ -380,7 +431,7 @@ struct Pipeline {
     sr::SceneTable table() const { return sr::SceneTable{scenes_d.as<sr::SceneInfo>(), path_scene.as<uint32_t>(), S}; }
 
     // Places the scenes' rows and framebuffers and uploads the scene table.
-    sr_status upload_table() {
+    sr_status upload_table(bool flush = true) {
         total_rows = 0;
         total_pixels = 0;
         res_ctas = 0;
@@ -408,11 +459,19 @@ struct Pipeline {
         CUDA_TRY(ensure(scenes_d, sizeof(sr::SceneInfo) * std::max<uint32_t>(S, 1)));
         CUDA_TRY(ensure(cta_base_d, sizeof(uint32_t) * (S + 1)));
         CUDA_TRY(ensure(image, 4 * std::max<uint64_t>(total_pixels, 1)));
-        if (S) CUDA_TRY(cudaMemcpy(scenes_d.p, info.data(), sizeof(sr::SceneInfo) * S, cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(cta_base_d.p, cta_base.data(), sizeof(uint32_t) * (S + 1), cudaMemcpyHostToDevice));
         CUDA_TRY(ensure(cta_narrow_d, std::max<size_t>(res_ctas, 1)));
-        if (res_ctas) CUDA_TRY(cudaMemcpy(cta_narrow_d.p, cta_narrow.data(), res_ctas, cudaMemcpyHostToDevice));
-        return SR_OK;
+        if (!flush) return SR_OK;   // upload() stages the table with the scenes
+        SR_TRY(stage_reserve(table_stage_bytes()));
+        stage_table();
+        return stage_flush();
+    }
+    size_t table_stage_bytes() const {
+        return staged_size(sizeof(sr::SceneInfo) * S) + staged_size(sizeof(uint32_t) * (S + 1)) + staged_size(res_ctas);
+    }
+    void stage_table() {
+        stage(scenes_d.p, info.data(), sizeof(sr::SceneInfo) * S);
+        stage(cta_base_d.p, cta_base.data(), sizeof(uint32_t) * (S + 1));
+        stage(cta_narrow_d.p, cta_narrow.data(), res_ctas);
     }
 
     sr_status upload(const HostScenes& h) {
@@ -431,19 +490,22 @@ struct Pipeline {
         CUDA_TRY(ensure(fill_rule, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
         CUDA_TRY(ensure(fill_info, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
         CUDA_TRY(ensure(path_scene, sizeof(uint32_t) * std::max<uint32_t>(P, 1)));
-        auto up = [](DevBuf& d, const void* src, size_t bytes) -> cudaError_t {
-            return bytes ? cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
-        };
-        CUDA_TRY(up(pos, h.pos.data(), sizeof(float) * h.pos.size()));
-        CUDA_TRY(up(pos_path, h.pos_path.data(), sizeof(uint32_t) * V));
-        CUDA_TRY(up(curve_pos, h.curve_pos.data(), sizeof(uint32_t) * C));
-        CUDA_TRY(up(curve_type, h.curve_type.data(), sizeof(uint32_t) * C));
-        CUDA_TRY(up(curve_path, h.curve_path.data(), sizeof(uint32_t) * C));
-        CUDA_TRY(up(fill_rule, h.fill_rule.data(), sizeof(uint32_t) * P));
-        CUDA_TRY(up(fill_info, h.fill_info.data(), sizeof(uint32_t) * P));
-        CUDA_TRY(up(path_scene, h.path_scene.data(), sizeof(uint32_t) * P));
         arcs = std::find(h.curve_type.begin(), h.curve_type.end(), (uint32_t)SR_CURVE_ARC) != h.curve_type.end();
-        SR_TRY(upload_table());
+        SR_TRY(upload_table(false));
+        const size_t need = staged_size(sizeof(float) * h.pos.size()) + staged_size(sizeof(uint32_t) * V) +
+                            3 * staged_size(sizeof(uint32_t) * C) + 3 * staged_size(sizeof(uint32_t) * P) +
+                            table_stage_bytes();
+        SR_TRY(stage_reserve(need));
+        stage(pos.p, h.pos.data(), sizeof(float) * h.pos.size());
+        stage(pos_path.p, h.pos_path.data(), sizeof(uint32_t) * V);
+        stage(curve_pos.p, h.curve_pos.data(), sizeof(uint32_t) * C);
+        stage(curve_type.p, h.curve_type.data(), sizeof(uint32_t) * C);
+        stage(curve_path.p, h.curve_path.data(), sizeof(uint32_t) * C);
+        stage(fill_rule.p, h.fill_rule.data(), sizeof(uint32_t) * P);
+        stage(fill_info.p, h.fill_info.data(), sizeof(uint32_t) * P);
+        stage(path_scene.p, h.path_scene.data(), sizeof(uint32_t) * P);
+        stage_table();
+        SR_TRY(stage_flush());
         loaded = true;
         stages_valid = false;
         path_first_valid = false;
@@ -646,6 +708,45 @@ struct Pipeline {
         DevBuf* dbg[] = {&d_fkey, &d_fwn, &d_fleft, &d_wscan, &d_fflag, &d_sflag, &d_skey};
         for (DevBuf* b : dbg) release(*b);
         stages_valid = false;
+    }
+
+    // Grows every device buffer to at least m's capacity for the same
+    // buffer (a second batch that will see frames like m's); the pinned
+    // plan totals too.  True when a buffer moved.
+    sr_status reserve_like(const Pipeline& m, bool* moved) {
+        static DevBuf Pipeline::* const bufs[] = {
+            &Pipeline::pos, &Pipeline::pos_path, &Pipeline::curve_pos, &Pipeline::curve_type,
+            &Pipeline::curve_path, &Pipeline::fill_rule, &Pipeline::fill_info, &Pipeline::path_scene,
+            &Pipeline::scenes_d, &Pipeline::cta_base_d, &Pipeline::tpos, &Pipeline::path_visible, &Pipeline::cut,
+            &Pipeline::count, &Pipeline::offs, &Pipeline::ctl, &Pipeline::scan_status, &Pipeline::pieces,
+            &Pipeline::chain_lists, &Pipeline::chain_sort_scratch, &Pipeline::long_list, &Pipeline::cbuf,
+            &Pipeline::rec, &Pipeline::keys, &Pipeline::keys_alt, &Pipeline::wnp, &Pipeline::skeys,
+            &Pipeline::svals, &Pipeline::vals_alt, &Pipeline::sort_scratch, &Pipeline::wind_status,
+            &Pipeline::draw, &Pipeline::draw_row, &Pipeline::totals, &Pipeline::rkeys, &Pipeline::rvals,
+            &Pipeline::rkeys_alt, &Pipeline::rvals_alt, &Pipeline::row_sort_scratch, &Pipeline::row_start,
+            &Pipeline::seg_cut, &Pipeline::row_count, &Pipeline::row_px, &Pipeline::row_scan, &Pipeline::image,
+            &Pipeline::path_first, &Pipeline::path_draw, &Pipeline::feats, &Pipeline::preds, &Pipeline::allot,
+            &Pipeline::plan_tot, &Pipeline::judge_out, &Pipeline::seg_scratch, &Pipeline::seg_tiles,
+            &Pipeline::curve_wide, &Pipeline::wide_curves, &Pipeline::cta_narrow_d};
+        *moved = false;
+        CUDA_TRY(cudaSetDevice(device));
+        for (DevBuf Pipeline::* b : bufs) {
+            DevBuf& mine = this->*b;
+            const size_t want = (m.*b).cap;
+            if (want > mine.cap) {
+                CUDA_TRY(ensure(mine, want, false));
+                *moved = true;
+            }
+        }
+        SR_TRY(stage_reserve(m.h_stage_cap));
+        if (h_plan_words < m.h_plan_words) {
+            if (h_plan_ptr) cudaFreeHost(h_plan_ptr);
+            h_plan_ptr = nullptr;
+            h_plan_words = 0;
+            CUDA_TRY(cudaMallocHost(&h_plan_ptr, sizeof(unsigned long long) * m.h_plan_words));
+            h_plan_words = m.h_plan_words;
+        }
+        return SR_OK;
     }
 
     // Device bytes currently held by this pipeline.
@@ -2251,6 +2352,31 @@ sr_status sr_batch_release(sr_batch* b) {
 sr_status sr_batch_held_bytes(const sr_batch* b, uint64_t* bytes) {
     if (!b || !bytes) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     *bytes = b->p.held_bytes();
+    return SR_OK;
+}
+
+sr_status sr_batch_reserve_like(sr_batch* b, const sr_batch* model) {
+    if (!b || !model) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (b == model) return SR_OK;
+    if (b->inflight) return fail(SR_ERR_INVALID_ARG, "reserve while a frame is in flight");
+    if (b->p.device != model->p.device) return fail(SR_ERR_INVALID_ARG, "batches on different devices");
+    bool moved = false;
+    SR_TRY(b->p.reserve_like(model->p, &moved));
+    if (moved) {
+        // the moved buffers' contents are gone: the next frame uploads the
+        // scenes again (and plans again); a captured frame holds the old
+        // addresses
+        b->committed = false;
+        b->p.planned = false;
+        b->p.path_first_valid = false;
+        b->p.stages_valid = false;
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        b->graph_cap = -1;
+        b->graph_dcap = -1;
+    }
     return SR_OK;
 }
 

@@ -96,6 +96,13 @@ struct sr_server {
     std::vector<Slot> slots;
     cudaMemPool_t pool = nullptr;
     cudaStream_t copy_stream = nullptr;
+    // Images fetched to host memory pass through this pinned buffer: a copy
+    // straight into pageable memory went through a slow path whose first
+    // use took about 20 ms, and other threads' CUDA calls (the scheduler's)
+    // waited behind it.
+    std::mutex bounce_mu;
+    unsigned char* bounce = nullptr;
+    size_t bounce_cap = 0;
     std::thread worker;
     bool stop = false;
     uint64_t next_id = 1;
@@ -108,6 +115,7 @@ struct sr_server {
     void run();
     void retire(Slot& sl);
     void hand_over(Slot& sl, sr_status s);
+    void grow_idle_slots(const Slot& model);
     bool admit(Slot& sl);
 };
 
@@ -175,6 +183,22 @@ void sr_server::hand_over(Slot& sl, sr_status s) {
     sl.busy = false;
     sl.bytes = 0;
     cv_done.notify_all();
+    grow_idle_slots(sl);
+}
+
+// A slot's first batch larger than any before reallocates its buffers
+// behind a device-wide wait (about 10 ms at serving sizes, which the queue
+// behind it pays).  When a slot's buffers have grown, the idle slots grow
+// like it at once, so that each size is paid for once, not once per slot.
+void sr_server::grow_idle_slots(const Slot& model) {
+    uint64_t want = 0;
+    if (sr_batch_held_bytes(model.batch, &want) != SR_OK) return;
+    for (Slot& other : slots) {
+        if (&other == &model || other.busy) continue;
+        uint64_t have = 0;
+        if (sr_batch_held_bytes(other.batch, &have) != SR_OK || have >= want) continue;
+        sr_batch_reserve_like(other.batch, model.batch);   // best effort: a failure only leaves it smaller
+    }
 }
 
 // Forms, sizes and enqueues one batch in a free slot; false when nothing
@@ -516,10 +540,25 @@ sr_status sr_server_wait(sr_server* s, uint64_t ticket, void* rgba_out, int out_
     if (r->d_image) {
         cudaSetDevice(s->o.device);
         if (rgba_out && status == SR_OK) {
-            cudaError_t e = cudaMemcpyAsync(rgba_out, r->d_image, r->image_bytes(),
-                                            out_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                            s->copy_stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
+            const size_t bytes = r->image_bytes();
+            cudaError_t e = cudaSuccess;
+            if (out_is_device) {
+                e = cudaMemcpyAsync(rgba_out, r->d_image, bytes, cudaMemcpyDeviceToDevice, s->copy_stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
+            } else {
+                std::lock_guard<std::mutex> bl(s->bounce_mu);
+                if (s->bounce_cap < bytes) {
+                    if (s->bounce) cudaFreeHost(s->bounce);
+                    s->bounce = nullptr;
+                    s->bounce_cap = 0;
+                    e = cudaMallocHost(&s->bounce, bytes + bytes / 2);
+                    if (e == cudaSuccess) s->bounce_cap = bytes + bytes / 2;
+                }
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(s->bounce, r->d_image, bytes, cudaMemcpyDeviceToHost, s->copy_stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s->copy_stream);
+                if (e == cudaSuccess) std::memcpy(rgba_out, s->bounce, bytes);
+            }
             if (e != cudaSuccess) status = srv_fail(SR_ERR_CUDA, cudaGetErrorString(e));
         }
         cudaFreeAsync(r->d_image, s->copy_stream);
@@ -570,6 +609,7 @@ void sr_server_destroy(sr_server* s) {
     }
     cudaStreamDestroy(s->copy_stream);
     cudaMemPoolDestroy(s->pool);
+    if (s->bounce) cudaFreeHost(s->bounce);
     delete s;
 }
 
