@@ -79,6 +79,12 @@ SR_DEV float interp(uint32_t type, float t, const float* p) {
     return 0.0f;
 }
 
+// The fragment size F is 1 (pixel mode) or 2 (reference mode).  v / F for
+// v >= 0 or a multiple of F (cell coordinates are), by a shift rather than
+// an integer division; and 1 / F, exactly.
+SR_DEV int32_t div_F(int32_t v, int32_t F) { return F == 2 ? (v >> 1) : v; }
+SR_DEV float inv_F(int32_t F) { return F == 2 ? 0.5f : 1.0f; }
+
 SR_DEV void set_error(uint32_t* status, uint32_t bit) {
     if (status) atomicOr(status, bit);
 }
@@ -186,9 +192,9 @@ SR_DEV uint64_t pack_key(const KeyLayout& L, uint32_t path, bool valid, int32_t 
         rank = (uint32_t)(L.Hy - 1);
         xo = 0;
     } else {
-        int32_t yy = pos_y / L.F;
+        int32_t yy = div_F(pos_y, L.F);
         rank = yy == 0 ? (uint32_t)L.Hy : (uint32_t)(yy - 1);
-        xo = (uint32_t)(pos_x / L.F + 1);
+        xo = (uint32_t)(div_F(pos_x, L.F) + 1);
     }
     return ((uint64_t)path << (L.rbits + L.xbits)) | ((uint64_t)rank << L.xbits) | (uint64_t)xo;
 }

@@ -187,7 +187,7 @@ constexpr uint32_t kChainKeyBits = 6;
 // (make_intersection_1.comp:150-213): number of grid crossings, first
 // grid line and step.
 SR_DEV int32_t axis_range_rd(float a0, float a1, int32_t size, int32_t F, float& start, bool& neg) {
-    const float invF = 1.0f / (float)F;   // x / F == x * (1/F) exactly for F in {1, 2}
+    const float invF = inv_F(F);   // x / F == x * (1/F) exactly for F in {1, 2}
     int32_t b, e;
     if (a0 <= a1) {
         b = wadd(wmul(float2int_rd(__fmul_rn(a0, invF)), F), F);
@@ -1006,7 +1006,7 @@ SR_DEV void fragment_record(const GeomArgs& g, const int2* __restrict__ rec, con
         float plx = interp(type, t1, P.x), ply = interp(type, t1, P.y);
         const int32_t F = g.F;
         const SceneInfo& si = scene_of_path(g.st, path);
-        const float invF = 1.0f / (float)F;   // exact: F is 1 or 2
+        const float invF = inv_F(F);
         int32_t rx = wmul(float2int_rd(__fmul_rn(__fmul_rn(__fadd_rn(pfx, plx), 0.5f), invF)), F);
         int32_t ry = wmul(float2int_rd(__fmul_rn(__fmul_rn(__fadd_rn(pfy, ply), 0.5f), invF)), F);
         pos_x = imin(imax(rx, -F), wadd(si.W & (int32_t)0xFFFFFFFE, F));

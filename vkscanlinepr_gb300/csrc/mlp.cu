@@ -98,7 +98,7 @@ __global__ void k_path_features(const GeomArgs g, const uint32_t* __restrict__ p
         bw = fmaxf(fminf(xmax, W + 1.0f) - fmaxf(xmin, -1.0f), 0.0f);
         bh = fmaxf(fminf(ymax, H + 1.0f) - fmaxf(ymin, -1.0f), 0.0f);
     }
-    const float invF = 1.0f / (float)g.F;
+    const float invF = inv_F(g.F);
     float* f = feats + (size_t)p * kIn;
     f[0] = log1pf((float)segs);
     f[1] = log1pf(bw * invF);

@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_resolve_ref(const ResolveArgs a)
                 rr.x0 = d.x & 0xFFFF;
                 rr.x1 = wadd(rr.x0, d.y);
                 rr.col = (uint32_t)d.z;
-                rr.row = (d.x >> 16) / a.F - w.r0;
+                rr.row = div_F(d.x >> 16, a.F) - w.r0;
                 sq[q] = rr;
             }
             __syncthreads();

@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(THREADS, 5) k_winding_emit(const WindArgs a,
 #pragma unroll
         for (int k = 1; k < ITEMS; ++k) starts_here = starts_here || kp[k - 1] != pl || kl[k - 1] != ll;
         const uint32_t rankl = (ll >> xbits) & rmask, xol = ll & xmask;
-        const uint32_t xo_maxl = (uint32_t)(((multi ? scene_of_path(a.st, pl).W : a.W) + a.F - 1) / a.F);
+        const uint32_t xo_maxl = (uint32_t)div_F((multi ? scene_of_path(a.st, pl).W : a.W) + a.F - 1, a.F);
         int32_t tail = 0;
         if (cont_last && starts_here && rankl != off_rank && xol >= 1u && xol <= xo_maxl) {
             uint32_t t = threadIdx.x + 1;
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(THREADS, 5) k_winding_emit(const WindArgs a,
     uint32_t ffm = 0, sfm = 0;
     const int32_t F = a.F;
     // on the canvas: a row of it, and 0 <= x = (xo - 1) F < W, i.e. 1 <= xo <= ceil(W / F)
-    const uint32_t xo_max1 = (uint32_t)((a.W + F - 1) / F);
+    const uint32_t xo_max1 = (uint32_t)div_F(a.W + F - 1, F);
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
         if ((heads >> k) & 1u) wrun = 0;
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(THREADS, 5) k_winding_emit(const WindArgs a,
         const uint32_t p1 = kp[k], l1 = kl[k];
         const uint32_t p0 = k == 0 ? pprev : kp[k - 1], l0 = k == 0 ? lprev : kl[k - 1];
         const uint32_t xo1 = l1 & xmask, rank1 = l1 >> xbits;
-        const uint32_t xo_max = multi ? (uint32_t)((scene_of_path(a.st, p1).W + F - 1) / F) : xo_max1;
+        const uint32_t xo_max = multi ? (uint32_t)div_F(scene_of_path(a.st, p1).W + F - 1, F) : xo_max1;
         const bool on = rank1 != off_rank && xo1 >= 1u && xo1 <= xo_max;
         const bool first = ibase + k == 0;
         bool ff = on && (first || p0 != p1 || l0 != l1);
