@@ -651,10 +651,11 @@ __global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __re
 // rounds has its chunks sorted into keys_out (r even) or keys_alt (r odd),
 // and each round flips buffer, so its last round lands in keys_out; rounds
 // past r do nothing for it.
-constexpr int kMergeOut = kTile / 2;   // outputs a merge CTA writes (half a chunk)
+constexpr int kMergeParts = 4;                   // work items per chunk
+constexpr int kMergeOut = kTile / kMergeParts;   // outputs a merge work item writes
 constexpr int kMergeItems = kMergeOut / kThreads;
 struct MergeSmem {
-    uint64_t in[kMergeOut];    // A part then B part of this half chunk
+    uint64_t in[kMergeOut];    // A part then B part of this item's outputs
     uint64_t out[kMergeOut];
     uint32_t split[4];
 };
@@ -691,18 +692,18 @@ SR_DEV uint32_t warp_merge_split(const uint64_t* A, uint32_t na, const uint64_t*
     return lo;
 }
 
-// Work item w is half w & 1 of chunk tile chunks[w >> 1]; the CTAs are
+// Work item w is part w % kMergeParts of chunk tile chunks[w / kMergeParts]; the CTAs are
 // persistent (one wave) and take items from the round's counter.
 SR_DEV void merge_item(MergeSmem& S, uint32_t item, uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt,
                        uint32_t level, uint32_t key_bits, uint32_t n_cap, const TileTables& u) {
-    const uint4 desc = u.desc[u.chunks[item >> 1]];
+    const uint4 desc = u.desc[u.chunks[item / kMergeParts]];
     const uint32_t k = desc.z & 0xFFFFu, rounds = (desc.z >> 16) & 0x7FFFu;
     if (level >= rounds) return;
     const uint64_t* src = ((rounds - level) & 1u) ? keys_alt : keys_out;
     uint64_t* dst = ((rounds - level) & 1u) ? keys_out : keys_alt;
     const uint32_t s0 = desc.x, size = desc.y;
     if ((uint64_t)s0 + size > n_cap) return;   // overflowed frame: redone
-    const uint32_t o0 = k * (uint32_t)kTile + (item & 1u) * (uint32_t)kMergeOut;
+    const uint32_t o0 = k * (uint32_t)kTile + (item % kMergeParts) * (uint32_t)kMergeOut;
     if (o0 >= size) return;
     const uint32_t o1 = min(o0 + (uint32_t)kMergeOut, size);
     const uint32_t W = (uint32_t)kTile << level;
@@ -751,7 +752,7 @@ __global__ void __launch_bounds__(kThreads) k_merge_level(uint64_t* __restrict__
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MergeSmem& S = *reinterpret_cast<MergeSmem*>(smem_raw);
     __shared__ uint32_t next;
-    const uint32_t n_items = 2u * u.ctl[kCtlChunks];
+    const uint32_t n_items = (uint32_t)kMergeParts * u.ctl[kCtlChunks];
     for (;;) {
         if (threadIdx.x == 0) next = atomicAdd(&u.ctl[kCtlMergeNext + level], 1u);
         __syncthreads();   // also: the previous item is done with the buffers
@@ -836,7 +837,8 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     // the 64-bit sort takes the few tiles the 32-bit one hands over
     const unsigned g_sort = (unsigned)std::min<size_t>(mt, sms);
     (void)occ_sort;
-    const unsigned g_merge = (unsigned)std::min<size_t>(2 * mt, sms * (size_t)std::max(occ_merge.load(), 1));
+    const unsigned g_merge =
+        (unsigned)std::min<size_t>(kMergeParts * mt, sms * (size_t)std::max(occ_merge.load(), 1));
     count_launches(2 + (uint32_t)levels);
     const uint32_t n_cap = (uint32_t)cap;
     k_tile_sort32<<<g_sort32, kThreads, sizeof(Sort32Smem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap,
