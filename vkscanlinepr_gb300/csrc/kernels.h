@@ -187,7 +187,9 @@ const uint32_t* segsort_largest(const void* scratch, uint32_t n_curves);
 // tables; cap bounds the tile tables); `levels` merge rounds launched, at
 // least ceil(log2(chunks of the largest segment)).  keys_alt is scratch.
 // The tile sort and the merge rounds run one wave of persistent CTAs.
-void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t n_curves,
+// keys_in[0, N) is left unspecified (the tiles that need 64-bit items sort
+// through it).
+void launch_segsort(uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t n_curves,
                     const KeyLayout& L, int levels, void* scratch, void* tiles, int sm_count, uint32_t* status,
                     cudaStream_t st);
 

@@ -555,92 +555,75 @@ __global__ void __launch_bounds__(kThreads, 4) k_tile_sort32(const uint64_t* __r
     }
 }
 
-// ---- 64-bit items (the tiles k_tile_sort32 handed over)
-struct LocalSmem {
-    uint64_t buf[2][kTile + 2];   // the staged tile, and the passes' second buffer
-    PassSmem ps;
-};
-
-SR_DEV bool sort_tile64(LocalSmem& S, uint32_t tile, uint32_t& phase, const uint64_t* __restrict__ keys_in,
-                        uint64_t* __restrict__ keys_out, uint64_t* __restrict__ keys_alt, const KeyFields& kf,
-                        uint32_t n_cap, const TileTables& u, uint32_t* status, uint32_t spin_limit) {
+// ---- 64-bit items (the tiles k_tile_sort32 handed over; rare).  The
+// passes run between the tile's range of the input array (scratch by now:
+// the 32-bit kernel has staged every tile) and of the output, with the
+// histograms in static shared memory (the kernel is launched every frame,
+// mostly with nothing handed over, so it holds no large buffers).
+SR_DEV void sort_tile64(PassSmem& S, uint32_t tile, uint64_t* keys_in, uint64_t* __restrict__ keys_out,
+                        uint64_t* __restrict__ keys_alt, const KeyFields& kf, uint32_t n_cap, const TileTables& u) {
     const uint32_t tid = threadIdx.x;
     uint32_t a, len;
     bool to_alt;
-    if (!tile_span(u, tile, n_cap, a, len, to_alt)) return true;
-    uint64_t* dst = to_alt ? keys_alt : keys_out;
-    const int soff = stage_tile(S.buf[0], &S.ps.bar, phase, keys_in, a, len, status, spin_limit);
-    if (soff < 0) return false;
-    const uint32_t off = (uint32_t)soff;
-
+    if (!tile_span(u, tile, n_cap, a, len, to_alt)) return;
+    uint64_t* src = keys_in + a;
+    uint64_t* dst = (to_alt ? keys_alt : keys_out) + a;
     const uint32_t kbits = kf.kbits();
     const uint64_t kmask = (1ull << kbits) - 1ull;
     Ranges R;
     R.init();
-    for (uint32_t j = tid; j < len; j += kThreads) R.add(kf, S.buf[0][off + j], kmask);
-    R.reduce(S.ps);
+    for (uint32_t j = tid; j < len; j += kThreads) R.add(kf, src[j], kmask);
+    R.reduce(S);
     const uint32_t bp = bits_of(R.pmax - R.pmin), br = bits_of(R.rmax - R.rmin), bx = bits_of(R.xmax - R.xmin);
     // compact items when the fields fit 32 bits and the payload the other 32
     const bool compact = bp + br + bx <= 32u && (R.top >> kbits) <= 0xFFFFFFFFull;
     const uint32_t bits =
         compact ? bp + br + bx : (R.lo == R.hi ? 0u : 64u - (uint32_t)__clzll((long long)(R.lo ^ R.hi)));
     const uint32_t passes = (bits + kRadixBits - 1) / kRadixBits;
-    // the items from slot 0 of the other buffer (the staged keys sit at off)
-    uint32_t cur = 0, src = off;
-    if (passes > 0 && (compact || off)) {
-        for (uint32_t j = tid; j < len; j += kThreads) {
-            const uint64_t k = S.buf[0][off + j];
-            const uint64_t c = ((uint64_t)(kf.p(k) - R.pmin) << (br + bx)) |
-                               ((uint64_t)(kf.r(k) - R.rmin) << bx) | (uint64_t)(kf.x(k) - R.xmin);
-            S.buf[1][j] = compact ? ((k >> kbits) << 32) | c : k;
-        }
-        cur = 1;
-        src = 0;
+    if (passes == 0) {
+        for (uint32_t j = tid; j < len; j += kThreads) dst[j] = src[j];
+        return;
     }
-    if (passes > 0) {
-        if (compact)
-            cur = radix_passes<uint64_t>(S.ps, S.buf[0], S.buf[1], cur, len, passes,
-                                         [](uint64_t v, uint32_t shift) -> uint32_t {
-                                             return ((uint32_t)v >> shift) & (kRadix - 1);
-                                         });
-        else
-            cur = radix_passes<uint64_t>(S.ps, S.buf[0], S.buf[1], cur, len, passes,
-                                         [kmask](uint64_t v, uint32_t shift) -> uint32_t {
-                                             return (uint32_t)((v & kmask) >> shift) & (kRadix - 1);
-                                         });
+    // the items start where the last pass ends in dst (a thread rewrites only
+    // its own slots here; the first pass's barrier publishes them)
+    uint64_t* first = (passes & 1u) ? src : dst;
+    uint64_t* other = (passes & 1u) ? dst : src;
+    for (uint32_t j = tid; j < len; j += kThreads) {
+        const uint64_t k = src[j];
+        const uint64_t c = ((uint64_t)(kf.p(k) - R.pmin) << (br + bx)) | ((uint64_t)(kf.r(k) - R.rmin) << bx) |
+                           (uint64_t)(kf.x(k) - R.xmin);
+        first[j] = compact ? ((k >> kbits) << 32) | c : k;
     }
-    if (compact && passes > 0) {
+    if (compact) {
+        radix_passes<uint64_t>(S, first, other, 0u, len, passes, [](uint64_t v, uint32_t shift) -> uint32_t {
+            return ((uint32_t)v >> shift) & (kRadix - 1);
+        });
         Unpack U;
-        U.load(S.ps);
+        U.load(S);
         for (uint32_t j = tid; j < len; j += kThreads) {
-            const uint64_t v = S.buf[cur][j];
-            dst[a + j] = ((v >> 32) << kbits) | U.key(kf, (uint32_t)v);
+            const uint64_t v = dst[j];
+            dst[j] = ((v >> 32) << kbits) | U.key(kf, (uint32_t)v);
         }
     } else {
-        for (uint32_t j = tid; j < len; j += kThreads) dst[a + j] = S.buf[cur][src + j];
+        radix_passes<uint64_t>(S, first, other, 0u, len, passes, [kmask](uint64_t v, uint32_t shift) -> uint32_t {
+            return (uint32_t)((v & kmask) >> shift) & (kRadix - 1);
+        });
     }
-    return true;
 }
 
-__global__ void __launch_bounds__(kThreads, 3) k_local_sort(const uint64_t* __restrict__ keys_in,
-                                                            uint64_t* __restrict__ keys_out,
-                                                            uint64_t* __restrict__ keys_alt, KeyFields kf,
-                                                            uint32_t n_cap, TileTables u, uint32_t* status,
-                                                            uint32_t spin_limit) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    LocalSmem& S = *reinterpret_cast<LocalSmem*>(smem_raw);
+__global__ void __launch_bounds__(kThreads) k_local_sort(uint64_t* keys_in, uint64_t* __restrict__ keys_out,
+                                                         uint64_t* __restrict__ keys_alt, KeyFields kf, uint32_t n_cap,
+                                                         TileTables u) {
+    __shared__ PassSmem S;
     const uint32_t n_tiles = u.ctl[kCtlFallback];
     if (n_tiles == 0) return;   // the usual case: nothing handed over
-    if (threadIdx.x == 0) mbar_init(&S.ps.bar, 1);
-    uint32_t phase = 0;
     for (;;) {
-        if (threadIdx.x == 0) S.ps.next = atomicAdd(&u.ctl[kCtlFallbackNext], 1u);
-        __syncthreads();   // also: the previous tile is done with the buffers
-        const uint32_t i = S.ps.next;
+        if (threadIdx.x == 0) S.next = atomicAdd(&u.ctl[kCtlFallbackNext], 1u);
+        __syncthreads();   // also: the previous tile is done with the histograms
+        const uint32_t i = S.next;
         __syncthreads();
         if (i >= n_tiles) break;
-        if (!sort_tile64(S, u.fallback[i], phase, keys_in, keys_out, keys_alt, kf, n_cap, u, status, spin_limit))
-            return;
+        sort_tile64(S, u.fallback[i], keys_in, keys_out, keys_alt, kf, n_cap, u);
     }
 }
 
@@ -799,7 +782,7 @@ const uint32_t* segsort_largest(const void* scratch, uint32_t C) {
     return carve_front(const_cast<void*>(scratch), C).ctl + 1;
 }
 
-void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t C,
+void launch_segsort(uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, int64_t cap, uint32_t C,
                     const KeyLayout& L, int levels, void* scratch, void* tiles, int sm_count, uint32_t* status,
                     cudaStream_t st) {
     if (cap <= 0 || C == 0) return;
@@ -819,32 +802,27 @@ void launch_segsort(const uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_
     // resident CTAs per SM of the two persistent kernels (same on every
     // device of the build's architecture)
     static std::atomic<uint32_t> attr{0};
-    static std::atomic<int> occ_sort32{0}, occ_sort{0}, occ_merge{0};
+    static std::atomic<int> occ_sort32{0}, occ_merge{0};
     once_per_device(attr, [] {
         cudaFuncSetAttribute(k_tile_sort32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sort32Smem));
-        cudaFuncSetAttribute(k_local_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LocalSmem));
         cudaFuncSetAttribute(k_merge_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
-        int a = 0, b = 0, c = 0;
+        int a = 0, c = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_tile_sort32, kThreads, sizeof(Sort32Smem));
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_local_sort, kThreads, sizeof(LocalSmem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_merge_level, kThreads, sizeof(MergeSmem));
         occ_sort32.store(std::max(a, 1));
-        occ_sort.store(std::max(b, 1));
         occ_merge.store(std::max(c, 1));
     });
     const size_t sms = (size_t)std::max(sm_count, 1);
     const unsigned g_sort32 = (unsigned)std::min<size_t>(mt, sms * (size_t)std::max(occ_sort32.load(), 1));
     // the 64-bit sort takes the few tiles the 32-bit one hands over
     const unsigned g_sort = (unsigned)std::min<size_t>(mt, sms);
-    (void)occ_sort;
     const unsigned g_merge =
         (unsigned)std::min<size_t>(kMergeParts * mt, sms * (size_t)std::max(occ_merge.load(), 1));
     count_launches(2 + (uint32_t)levels);
     const uint32_t n_cap = (uint32_t)cap;
     k_tile_sort32<<<g_sort32, kThreads, sizeof(Sort32Smem), st>>>(keys_in, keys_out, keys_alt, C, kf, n_cap,
                                                                   (uint32_t)mt, u, status, spin_limit());
-    k_local_sort<<<g_sort, kThreads, sizeof(LocalSmem), st>>>(keys_in, keys_out, keys_alt, kf, n_cap, u, status,
-                                                              spin_limit());
+    k_local_sort<<<g_sort, kThreads, 0, st>>>(keys_in, keys_out, keys_alt, kf, n_cap, u);
     for (int lv = 0; lv < levels; ++lv)
         k_merge_level<<<g_merge, kThreads, sizeof(MergeSmem), st>>>(keys_out, keys_alt, (uint32_t)lv, key_bits, n_cap,
                                                                     u);
