@@ -303,10 +303,9 @@ struct Pipeline {
     bool path_first_valid = false, count_paths = false, planned = false;
     unsigned long long* h_plan_ptr = nullptr;   // pinned plan totals
     size_t h_plan_words = 0;
-    // Host-to-device uploads of scenes and tables go through one pinned
-    // staging buffer on a stream of their own: a copy from pageable memory
-    // runs at a fraction of DMA speed and, on first use of fresh host pages,
-    // took tens of milliseconds on the Grace host.
+    // Host-to-device uploads of tables and of small scene sets go through one
+    // pinned staging buffer on a stream of their own: one wait instead of a
+    // synchronous call per array.
     unsigned char* h_stage = nullptr;
     size_t h_stage_cap = 0, h_stage_used = 0;
     cudaStream_t up_stream = nullptr;
@@ -384,6 +383,7 @@ struct Pipeline {
         return SR_OK;
     }
     static size_t staged_size(size_t bytes) { return (bytes + 255) & ~(size_t)255; }
+    static constexpr size_t kStagedUploadMax = 1u << 20;
 
     sr_status init(int dev, int32_t m, uint32_t fl) {
         device = dev;
@@ -495,15 +495,33 @@ struct Pipeline {
         const size_t need = staged_size(sizeof(float) * h.pos.size()) + staged_size(sizeof(uint32_t) * V) +
                             3 * staged_size(sizeof(uint32_t) * C) + 3 * staged_size(sizeof(uint32_t) * P) +
                             table_stage_bytes();
-        SR_TRY(stage_reserve(need));
-        stage(pos.p, h.pos.data(), sizeof(float) * h.pos.size());
-        stage(pos_path.p, h.pos_path.data(), sizeof(uint32_t) * V);
-        stage(curve_pos.p, h.curve_pos.data(), sizeof(uint32_t) * C);
-        stage(curve_type.p, h.curve_type.data(), sizeof(uint32_t) * C);
-        stage(curve_path.p, h.curve_path.data(), sizeof(uint32_t) * C);
-        stage(fill_rule.p, h.fill_rule.data(), sizeof(uint32_t) * P);
-        stage(fill_info.p, h.fill_info.data(), sizeof(uint32_t) * P);
-        stage(path_scene.p, h.path_scene.data(), sizeof(uint32_t) * P);
+        if (need <= kStagedUploadMax) {
+            // a small set (a serving batch): one stream, one wait
+            SR_TRY(stage_reserve(need));
+            stage(pos.p, h.pos.data(), sizeof(float) * h.pos.size());
+            stage(pos_path.p, h.pos_path.data(), sizeof(uint32_t) * V);
+            stage(curve_pos.p, h.curve_pos.data(), sizeof(uint32_t) * C);
+            stage(curve_type.p, h.curve_type.data(), sizeof(uint32_t) * C);
+            stage(curve_path.p, h.curve_path.data(), sizeof(uint32_t) * C);
+            stage(fill_rule.p, h.fill_rule.data(), sizeof(uint32_t) * P);
+            stage(fill_info.p, h.fill_info.data(), sizeof(uint32_t) * P);
+            stage(path_scene.p, h.path_scene.data(), sizeof(uint32_t) * P);
+        } else {
+            // a large one goes straight from the host vectors: the extra host
+            // copy into the staging buffer would cost more than it saves
+            auto up = [](DevBuf& d, const void* src, size_t bytes) -> cudaError_t {
+                return bytes ? cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+            };
+            CUDA_TRY(up(pos, h.pos.data(), sizeof(float) * h.pos.size()));
+            CUDA_TRY(up(pos_path, h.pos_path.data(), sizeof(uint32_t) * V));
+            CUDA_TRY(up(curve_pos, h.curve_pos.data(), sizeof(uint32_t) * C));
+            CUDA_TRY(up(curve_type, h.curve_type.data(), sizeof(uint32_t) * C));
+            CUDA_TRY(up(curve_path, h.curve_path.data(), sizeof(uint32_t) * C));
+            CUDA_TRY(up(fill_rule, h.fill_rule.data(), sizeof(uint32_t) * P));
+            CUDA_TRY(up(fill_info, h.fill_info.data(), sizeof(uint32_t) * P));
+            CUDA_TRY(up(path_scene, h.path_scene.data(), sizeof(uint32_t) * P));
+            SR_TRY(stage_reserve(table_stage_bytes()));
+        }
         stage_table();
         SR_TRY(stage_flush());
         loaded = true;
