@@ -211,6 +211,7 @@ __global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
 // Fields of a key: path, row rank, x (payload bits above the key ignored).
 struct KeyFields {
     uint32_t xb, rb, pb;
+    uint32_t off_rank;   // rank of the off-canvas records (Hy - 1); row 0 ranks one above
     SR_DEV uint32_t x(uint64_t k) const { return (uint32_t)(k & ((1ull << xb) - 1)); }
     SR_DEV uint32_t r(uint64_t k) const { return (uint32_t)((k >> xb) & ((1ull << rb) - 1)); }
     SR_DEV uint32_t p(uint64_t k) const { return (uint32_t)((k >> (xb + rb)) & ((1ull << pb) - 1)); }
@@ -236,7 +237,7 @@ struct PassSmem {
     uint32_t warp_hist[kWarps][kRadix];
     uint32_t digit_start[kRadix];
     uint32_t scan_tmp[kWarps];
-    uint32_t red[kWarps][6];
+    uint32_t red[kWarps][10];
     uint64_t kred[kWarps][3];
     uint64_t bar;
     uint32_t next;
@@ -376,6 +377,114 @@ struct Unpack {
     }
 };
 
+// Ranges of a tile for its 32-bit items, with the row ranks compacted: the
+// ranks in use below the off-canvas rank (a band), then the off-canvas rank,
+// then row 0's rank above it take consecutive codes, so a tile holding off-
+// canvas or row-0 records does not need the whole rank range; the x of the
+// off-canvas records (all the same when they are packed as keys are) is kept
+// aside, so they do not widen the x range either.  The order of the codes
+// is the order of the ranks, and equal keys keep equal codes.
+struct TileRanges {
+    uint32_t pmin, pmax, bmin, bmax, xmin, xmax, xomin, xomax, has_off, has_top;
+    uint64_t top;   // the whole key's max (its payload's max)
+    SR_DEV void init() {
+        pmin = bmin = xmin = xomin = ~0u;
+        pmax = bmax = xmax = xomax = 0;
+        has_off = has_top = 0;
+        top = 0;
+    }
+    SR_DEV void add(const KeyFields& kf, uint64_t k) {
+        const uint32_t p = kf.p(k), r = kf.r(k), x = kf.x(k);
+        pmin = min(pmin, p); pmax = max(pmax, p);
+        if (r == kf.off_rank) {
+            has_off = 1;
+            xomin = min(xomin, x); xomax = max(xomax, x);
+        } else {
+            if (r < kf.off_rank) {
+                bmin = min(bmin, r); bmax = max(bmax, r);
+            } else {
+                has_top = 1;
+            }
+            xmin = min(xmin, x); xmax = max(xmax, x);
+        }
+        top = max(top, k);
+    }
+    SR_DEV void reduce(PassSmem& S) {
+        const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            pmin = min(pmin, __shfl_xor_sync(0xFFFFFFFFu, pmin, o));
+            pmax = max(pmax, __shfl_xor_sync(0xFFFFFFFFu, pmax, o));
+            bmin = min(bmin, __shfl_xor_sync(0xFFFFFFFFu, bmin, o));
+            bmax = max(bmax, __shfl_xor_sync(0xFFFFFFFFu, bmax, o));
+            xmin = min(xmin, __shfl_xor_sync(0xFFFFFFFFu, xmin, o));
+            xmax = max(xmax, __shfl_xor_sync(0xFFFFFFFFu, xmax, o));
+            xomin = min(xomin, __shfl_xor_sync(0xFFFFFFFFu, xomin, o));
+            xomax = max(xomax, __shfl_xor_sync(0xFFFFFFFFu, xomax, o));
+            top = max(top, __shfl_xor_sync(0xFFFFFFFFu, top, o));
+        }
+        has_off = __any_sync(0xFFFFFFFFu, has_off) ? 1u : 0u;
+        has_top = __any_sync(0xFFFFFFFFu, has_top) ? 1u : 0u;
+        if (lane == 0) {
+            uint32_t* w = S.red[warp];
+            w[0] = pmin; w[1] = pmax; w[2] = bmin; w[3] = bmax; w[4] = xmin;
+            w[5] = xmax; w[6] = xomin; w[7] = xomax; w[8] = has_off; w[9] = has_top;
+            S.kred[warp][2] = top;
+        }
+        __syncthreads();
+        load(S);
+        top = S.kred[0][2];
+#pragma unroll
+        for (int w = 1; w < kWarps; ++w) top = max(top, S.kred[w][2]);
+    }
+    // the reduced values from the warps' shared words (also used to reload
+    // them after the passes, with fewer live registers through them)
+    SR_DEV void load(const PassSmem& S) {
+        init();
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t* v = S.red[w];
+            pmin = min(pmin, v[0]); pmax = max(pmax, v[1]);
+            bmin = min(bmin, v[2]); bmax = max(bmax, v[3]);
+            xmin = min(xmin, v[4]); xmax = max(xmax, v[5]);
+            xomin = min(xomin, v[6]); xomax = max(xomax, v[7]);
+            has_off |= v[8]; has_top |= v[9];
+        }
+        // off-canvas records of different x (not how keys are packed) share
+        // the x range like the others
+        if (has_off && xomin != xomax) {
+            xmin = min(xmin, xomin);
+            xmax = max(xmax, xomax);
+        }
+    }
+    SR_DEV bool off_x_apart() const { return has_off && xomin == xomax; }
+    SR_DEV uint32_t band() const { return bmin <= bmax ? bmax - bmin + 1u : 0u; }
+    SR_DEV uint32_t rank_codes() const { return band() + has_off + has_top; }
+    SR_DEV uint32_t bits_p() const { return bits_of(pmax - pmin); }
+    SR_DEV uint32_t bits_r() const { return bits_of(rank_codes() - 1u); }
+    SR_DEV uint32_t bits_x() const { return xmin <= xmax ? bits_of(xmax - xmin) : 0u; }
+    // compact fields of key k (br, bx: bits_r(), bits_x())
+    SR_DEV uint32_t code(const KeyFields& kf, uint64_t k, uint32_t br, uint32_t bx) const {
+        const uint32_t p = kf.p(k), r = kf.r(k), x = kf.x(k);
+        const uint32_t nb = band();
+        const bool off = r == kf.off_rank;
+        const uint32_t rc = r < kf.off_rank ? r - bmin : (off ? nb : nb + has_off);
+        const uint32_t xc = off && off_x_apart() ? 0u : x - xmin;
+        const uint32_t pc = bits_p() ? (p - pmin) << (br + bx) : 0u;
+        return pc | (br ? rc << bx : 0u) | xc;
+    }
+    // the key of compact fields c
+    SR_DEV uint64_t key(const KeyFields& kf, uint32_t c, uint32_t br, uint32_t bx) const {
+        const uint32_t xc = c & low_mask(bx);
+        const uint32_t rc = (uint32_t)(((uint64_t)c >> bx) & low_mask(br));
+        const uint32_t p = pmin + (uint32_t)((uint64_t)c >> (br + bx));
+        const uint32_t nb = band();
+        const uint32_t r = rc < nb ? bmin + rc : (has_off && rc == nb ? kf.off_rank : kf.off_rank + 1u);
+        const uint32_t x = r == kf.off_rank && off_x_apart() ? xomin : xmin + xc;
+        return ((uint64_t)p << (kf.xb + kf.rb)) | ((uint64_t)r << kf.xb) | (uint64_t)x;
+    }
+};
+
 // `passes` digit passes over items buf[cur][0, len), each into the other
 // buffer; returns the buffer holding the result.  digit(item, shift).
 template <typename T, typename Digit>
@@ -480,14 +589,15 @@ SR_DEV bool sort_tile32(Sort32Smem& S, uint32_t tile, uint32_t& phase, const uin
     const uint32_t kbits = kf.kbits();
     const uint64_t kmask = (1ull << kbits) - 1ull;
     const uint32_t base = (uint32_t)off;
-    Ranges R;
+    TileRanges R;
     R.init();
-    for (uint32_t j = tid; j < len; j += kThreads) R.add(kf, S.keys[base + j], kmask);
+    for (uint32_t j = tid; j < len; j += kThreads) R.add(kf, S.keys[base + j]);
     R.reduce(S.ps);
-    const uint32_t bp = bits_of(R.pmax - R.pmin), br = bits_of(R.rmax - R.rmin), bx = bits_of(R.xmax - R.xmin);
-    const uint32_t bits = bp + br + bx;
+    const uint32_t br = R.bits_r(), bx = R.bits_x();
+    const uint32_t bits = R.bits_p() + br + bx;
     const uint64_t pay_max = R.top >> kbits;
     const uint32_t payb = pay_max > 0xFFFFFFFFull ? 33u : bits_of((uint32_t)pay_max);
+    (void)kmask;
     if (bits + payb > 32u) {
         if (tid == 0) u.fallback[atomicAdd(&u.ctl[kCtlFallback], 1u)] = tile;
         return true;
@@ -506,9 +616,7 @@ SR_DEV bool sort_tile32(Sort32Smem& S, uint32_t tile, uint32_t& phase, const uin
         const uint32_t j = tid + (uint32_t)i * kThreads;
         if (j < len) {
             const uint64_t k = S.keys[base + j];
-            const uint32_t pc = bp ? (kf.p(k) - R.pmin) << (br + bx) : 0u;
-            const uint32_t rc = br ? (kf.r(k) - R.rmin) << bx : 0u;
-            iv[i] = (bits < 32u ? (uint32_t)(k >> kbits) << bits : 0u) | pc | rc | (kf.x(k) - R.xmin);
+            iv[i] = (bits < 32u ? (uint32_t)(k >> kbits) << bits : 0u) | R.code(kf, k, br, bx);
         }
     }
     __syncthreads();
@@ -524,12 +632,14 @@ SR_DEV bool sort_tile32(Sort32Smem& S, uint32_t tile, uint32_t& phase, const uin
                                                 [cmask](uint32_t v, uint32_t shift) -> uint32_t {
                                                     return ((v & cmask) >> shift) & (kRadix - 1);
                                                 });
-    Unpack U;
+    TileRanges U;
     U.load(S.ps);
+    const uint32_t ubr = U.bits_r(), ubx = U.bits_x(), ubits = U.bits_p() + ubr + ubx;
+    const uint32_t umask = low_mask(ubits);
     for (uint32_t j = tid; j < len; j += kThreads) {
         const uint32_t v = S.items[cur][j];
-        const uint64_t pay = bits < 32u ? (uint64_t)(v >> bits) : 0ull;
-        dst[a + j] = (pay << kbits) | U.key(kf, v & cmask);
+        const uint64_t pay = ubits < 32u ? (uint64_t)(v >> ubits) : 0ull;
+        dst[a + j] = (pay << kbits) | U.key(kf, v & umask, ubr, ubx);
     }
     return true;
 }
@@ -798,7 +908,7 @@ void launch_segsort(uint64_t* keys_in, uint64_t* keys_out, uint64_t* keys_alt, i
     launch_exclusive_scan_i32(u.ntiles, u.ntiles, C + 1, u.scan_status, u.ctl + 0, status, st);
     k_seg_desc<<<g, 256, 0, st>>>(C, (uint32_t)mt, t, u);
     const uint32_t key_bits = L.pbits + L.rbits + L.xbits;
-    const KeyFields kf{L.xbits, L.rbits, L.pbits};
+    const KeyFields kf{L.xbits, L.rbits, L.pbits, (uint32_t)(L.Hy - 1)};
     // resident CTAs per SM of the two persistent kernels (same on every
     // device of the build's architecture)
     static std::atomic<uint32_t> attr{0};
