@@ -1117,11 +1117,16 @@ void launch_chains(const GeomArgs& g, const int32_t* offs, const ChainWork& w, i
                    cudaStream_t st) {
     if (g.n_curves == 0) return;
     count_launches(1);
+    // Part 1 runs two CTAs (8 warps) an SM.  Fewer warps share each SM's
+    // issue slots, so each group of chains, the longest first, finishes
+    // sooner, and the wide chains beside them and the merge waiting on them
+    // start earlier: on the 4096^2 frame its stage took 0.83 / 0.61 / 0.73 /
+    // 0.75 / 0.78 ms at 1 / 2 / 4 / 8 / 16 CTAs an SM.
     if (part == 0)
         k_chains<<<sm_count * 4, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
                                                w.chain_count, w.wide_count, w.wide_queue, cbuf, 0);
     else
-        k_chains<<<sm_count * 16, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
+        k_chains<<<sm_count * 2, 128, 0, st>>>(g, offs, w.pieces, w.sorted_items, w.sorted_keys, w.list_cap,
                                                 w.chain_count, w.wide_count, w.chain_queue, cbuf, 1);
 }
 
