@@ -213,11 +213,11 @@ typedef struct sr_stats {
     uint32_t reruns;           /* sr_render: pre-sized frames of this context
                                 * that overflowed and were rerun with exact
                                 * sizing (cumulative; 0 for batches)        */
-    /* with SR_FLAG_PROFILE: device time of each stage (CUDA events on the
-     * render stream): transform, count, offset scan, crossing chains,
-     * record merge, fragments, sort, winding+emit, row sort, resolve; then
-     * the wide chains with their curves' merge and fragments, which run on
-     * a second stream beside chains, merge and fragments */
+    /* with SR_FLAG_PROFILE: device time of each stage (CUDA events):
+     * transform, count, offset scan, crossing chains, record merge,
+     * fragments (these three on the context's second stream), sort,
+     * winding+emit, row sort, resolve; then the wide chains with their
+     * curves' merge and fragments, on the render stream beside them */
     float stage_ms[12];
 } sr_stats;
 sr_status sr_get_stats(const sr_ctx* ctx, sr_stats* out);

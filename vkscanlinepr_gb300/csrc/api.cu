@@ -327,8 +327,9 @@ struct Pipeline {
     cudaEvent_t ev[2 * ST_COUNT_ALL] = {};
     bool ev_pending = false, capturing = false;
     cudaStream_t cur = nullptr;
-    // second stream of a frame: the wide chains and their curves' merge and
-    // fragments run on it beside the rest (forked and joined by events)
+    // second stream of a frame (lowest priority): the chains other than the
+    // wide ones, and their curves' merge and fragments, run on it beside the
+    // wide chains on the frame's stream (forked and joined by events)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_merged = nullptr, ev_join = nullptr;
 
