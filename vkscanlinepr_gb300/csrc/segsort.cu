@@ -27,8 +27,11 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;   // records a CTA sorts or merges
 constexpr int kGroup = kTile / 2;          // largest segment packed into a group tile
-constexpr int kRadixBits = 8;
+// 9-bit digits: a tile's compact items need 2.3 passes a record on the
+// 4096^2 frame against 2.7 with 8-bit ones, for a histogram of 8 x 512 words
+constexpr int kRadixBits = 9;
 constexpr int kRadix = 1 << kRadixBits;
+constexpr int kDigitsPerThread = kRadix / 256;   // of the pass's digit scan
 constexpr uint32_t kChunkBit = 1u << 31;   // descriptor .z: a chunk of a large segment
 // Lanes with the same digit: __match_any_sync (tiles hold runs of nearly
 // sorted keys, so a warp sees few distinct digits), or one ballot per bit.
@@ -519,14 +522,23 @@ SR_DEV uint32_t radix_passes(PassSmem& S, T* buf0, T* buf1, uint32_t cur, uint32
             __syncwarp();
         }
         __syncthreads();
-        // per digit: exclusive over warps, then over digits
-        const uint32_t dd = tid;   // kThreads == kRadix
+        // per digit: exclusive over warps, then over digits (a thread takes
+        // kDigitsPerThread adjacent digits)
+        static_assert(kThreads * kDigitsPerThread == kRadix, "digits per thread");
+        uint32_t dcnt[kDigitsPerThread];
         uint32_t cnt = 0;
 #pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = S.warp_hist[w][dd];
-            S.warp_hist[w][dd] = cnt;
-            cnt += c;
+        for (int q = 0; q < kDigitsPerThread; ++q) {
+            const uint32_t dd = tid * kDigitsPerThread + (uint32_t)q;
+            uint32_t sum = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+                const uint32_t c = S.warp_hist[w][dd];
+                S.warp_hist[w][dd] = sum;
+                sum += c;
+            }
+            dcnt[q] = sum;
+            cnt += sum;
         }
         uint32_t x = cnt;
 #pragma unroll
@@ -547,7 +559,12 @@ SR_DEV uint32_t radix_passes(PassSmem& S, T* buf0, T* buf1, uint32_t cur, uint32
             if (lane < kWarps) S.scan_tmp[lane] = wi - w;
         }
         __syncthreads();
-        S.digit_start[dd] = S.scan_tmp[warp] + x - cnt;
+        uint32_t start = S.scan_tmp[warp] + x - cnt;
+#pragma unroll
+        for (int q = 0; q < kDigitsPerThread; ++q) {
+            S.digit_start[tid * kDigitsPerThread + (uint32_t)q] = start;
+            start += dcnt[q];
+        }
         __syncthreads();
 #pragma unroll
         for (int it = 0; it < kItems; ++it) {
