@@ -753,8 +753,8 @@ struct Pipeline {
             DevBuf& mine = this->*b;
             const size_t want = (m.*b).cap;
             if (want > mine.cap) {
+                *moved = true;   // before: a failed ensure has freed the old buffer too
                 CUDA_TRY(ensure(mine, want, false));
-                *moved = true;
             }
         }
         SR_TRY(stage_reserve(m.h_stage_cap));
@@ -2380,7 +2380,7 @@ sr_status sr_batch_reserve_like(sr_batch* b, const sr_batch* model) {
     if (b->inflight) return fail(SR_ERR_INVALID_ARG, "reserve while a frame is in flight");
     if (b->p.device != model->p.device) return fail(SR_ERR_INVALID_ARG, "batches on different devices");
     bool moved = false;
-    SR_TRY(b->p.reserve_like(model->p, &moved));
+    const sr_status rs = b->p.reserve_like(model->p, &moved);
     if (moved) {
         // the moved buffers' contents are gone: the next frame uploads the
         // scenes again (and plans again); a captured frame holds the old
@@ -2396,7 +2396,7 @@ sr_status sr_batch_reserve_like(sr_batch* b, const sr_batch* model) {
         b->graph_cap = -1;
         b->graph_dcap = -1;
     }
-    return SR_OK;
+    return rs;
 }
 
 sr_status sr_batch_frame_bytes(sr_batch* b, int64_t records, int64_t draws, uint64_t* bytes) {
