@@ -200,13 +200,15 @@ __global__ void k_seg_desc(uint32_t C, uint32_t mt, SegTables t, TileTables u) {
 //   * The tile reaches shared memory by one bulk copy (TMA) of its 16-byte
 //     aligned span; an odd last key comes by a plain load.
 //   * Within a tile the order is that of a compact item: the fields
-//     (path - pmin, rank - rmin, x - xmin) packed in the fewest bits their
-//     ranges need.  It usually needs 2-3 digit passes where the whole key
+//     (path - pmin, row-rank code, x - xmin) packed in the fewest bits their
+//     ranges need (the rank codes of k_tile_sort32 are compacted, see
+//     TileRanges).  It usually needs 2-3 digit passes where the whole key
 //     needs 4-6, and a digit is one shift of a 32-bit word.
 //   * k_tile_sort32 sorts the tiles whose compact fields and payload fit one
 //     32-bit word: half the shared memory, so more CTAs per SM.  It hands
-//     the others to k_local_sort, whose items are 64-bit (the payload in the
-//     high word, or the raw key when the fields need more than 32 bits).
+//     the others to k_local_sort, whose items are 64-bit (rank - rmin codes,
+//     the payload in the high word, or the raw key when the fields need
+//     more than 32 bits), sorted through global memory.
 //   * A pass ranks the digits per warp (match_any + a per-warp histogram),
 //     scans the counts and scatters into the other buffer (stable: digit,
 //     then warp, then slot).  Rows of slots past the tile's end are skipped.
